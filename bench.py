@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark: batched path-dependent GBM pricing on one GB300.
+
+Workload (the reference's batched path-dependent configuration): 4096 GBM
+contracts in one launch -- arithmetic/geometric x fixed/floating x call/put
+Asians, all 8 barrier types, fixed/floating lookbacks and cash digitals --
+with S0=100, K~U[80,120], sigma~U[.1,.5], r~U[0,.06], T~U[.25,2], monitoring
+steps ~U{12..252}, paths log-uniform in [1e4, 1e6], seed 42+i.  Barrier levels
+H = S0(1 +/- U[.05,.3]), rebate 0.  Parameters come from numpy's default_rng(42)
+(synthetic data with the configuration's distributions).
+
+A step prices the whole batch once: FP32 paths, FP64 accumulation, one
+persistent-kernel launch (plus the fixed-order merge) replayed from a CUDA
+graph.  `value` is paths/s with the batch resident on the device; `e2e` is the
+same metric through the C ABI with host arrays (copies inside the timed
+region).  The L2 is flushed (256 MB write) between timed steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "derivative-pricing_gb300")
+sys.path.insert(0, PKG)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "paths_per_second"
+UNIT = "paths/s"
+WORKLOAD = "batch of 4096 path-dependent GBM contracts (asian/barrier/lookback/digital), FP32 paths"
+
+
+def make_batch(n=4096, seed=42):
+    """The configuration's contract list (mcd_contract records)."""
+    import mcd_gpu as M
+    rng = np.random.default_rng(seed)
+    c = M.contracts(n)
+    variants = []
+    for avg in (0, 1):
+        for style in (0, 1):
+            for ty in (0, 1):
+                variants.append(dict(product=M.ASIAN, average_style=avg, strike_style=style, type=ty))
+    for d in (0, 1):
+        for k in (0, 1):
+            for ty in (0, 1):
+                variants.append(dict(product=M.BARRIER, direction=d, knock=k, type=ty))
+    for style in (0, 1):
+        for ty in (0, 1):
+            variants.append(dict(product=M.LOOKBACK, strike_style=style, type=ty))
+    for ty in (0, 1):
+        variants.append(dict(product=M.DIGITAL, digital_style=0, type=ty))
+    pick = rng.integers(0, len(variants), n)
+    for i, v in enumerate(pick):
+        for k, val in variants[v].items():
+            c[k][i] = val
+    c["spot"] = 100.0
+    c["strike"] = rng.uniform(80, 120, n)
+    c["vol"] = rng.uniform(0.1, 0.5, n)
+    c["rate"] = rng.uniform(0.0, 0.06, n)
+    c["time"] = rng.uniform(0.25, 2.0, n)
+    c["monitoring_points"] = rng.integers(12, 253, n)
+    c["path_count"] = np.round(10.0 ** rng.uniform(4, 6, n)).astype(np.uint64)
+    h = rng.uniform(0.05, 0.3, n)
+    c["barrier"] = np.where(c["direction"] == 0, 100.0 * (1 + h), 100.0 * (1 - h))
+    c["rebate"] = 0.0
+    c["cash_amount"] = 1.0
+    c["seed"] = 42 + np.arange(n, dtype=np.uint64)
+    return c
+
+
+def path_steps(c):
+    steps = np.where(c["product"] == 1, 1, c["monitoring_points"]).astype(np.float64)
+    return float((steps * c["path_count"].astype(np.float64)).sum())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_baseline_sample(c, budget_s=12.0):
+    """Times the CPU port (bit-identical restatement of the reference) on a
+    stratified sample of the batch, each contract on all host threads over the
+    reference's fixed chunk partition (its own multithreaded path)."""
+    import oracle as O
+    orc = O.load()
+    threads = os.cpu_count() or 1
+    order = np.argsort(c["monitoring_points"] * c["path_count"].astype(np.float64))
+    # Grow a stratified sample (every k-th contract by cost) until ~budget_s of work.
+    for k in (512, 256, 128, 64):
+        idx = order[::k]
+        est = path_steps(c[idx]) / (threads * 1.2e7)
+        if est >= budget_s / 2 or k == 64:
+            break
+    sample = c[idx]
+    arr = (O.Contract * len(sample))()
+    for i, row in enumerate(sample):
+        for name in row.dtype.names:
+            setattr(arr[i], name, row[name].item())
+    out = (O.McResult * len(sample))()
+    t0 = time.perf_counter()
+    orc.orc_price_batch(arr, len(sample), threads, 0, out)
+    dt = time.perf_counter() - t0
+    paths = float(sample["path_count"].astype(np.float64).sum())
+    return {"value": paths / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(sample)} of 4096 contracts (every {k}th by cost), {paths:.3g} paths, "
+                      f"{path_steps(sample):.3g} path-steps, {dt:.2f} s",
+            "path_steps_per_s": path_steps(sample) / dt}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU algorithm (the oracle port,
+    bit-identical to the reference built from source) on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    c = make_batch()
+    for _ in range(max(args.warmup, 0)):
+        cpu_baseline_sample(c, budget_s=4.0)
+    vals = []
+    last = None
+    for _ in range(max(args.steps, 1)):
+        last = cpu_baseline_sample(c, budget_s=4.0)
+        vals.append(last["value"])
+    value = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": last["sample"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": last["cores"], "kind": "port",
+                             "sample": last["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--contracts", type=int, default=4096,
+                    help="batch size (the configuration is 4096; smaller only for profiling)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import mcd_gpu as M
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    # Replicas: every rank prices its own copy of the batch (the path does not
+    # need a collective, multi-GPU).
+    c = make_batch(args.contracts)
+    n = len(c)
+    total_paths = float(c["path_count"].astype(np.float64).sum())
+    total_steps = path_steps(c)
+
+    eng = M.Engine(local)
+    # Autotune the launch shape on a cost-stratified subset.
+    order = np.argsort(c["monitoring_points"] * c["path_count"].astype(np.float64))
+    tune = c[order[::16]]
+    if args.no_tune:
+        variant, ctas = eng.launch_shape("fp32")
+    else:
+        variant, ctas, _ = eng.autotune(tune, "fp32")
+
+    d_contracts = torch.from_numpy(c.view(np.uint8).copy()).cuda()
+    d_results = torch.zeros(n * M.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    # A dedicated stream: the library launches on it and the events below
+    # are recorded on it (the legacy default stream has handle 0, which the
+    # C ABI reads as "the context's own stream").
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    def step():
+        eng.price_batch_device(d_contracts.data_ptr(), n, d_results.data_ptr(), "fp32",
+                               stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    eng.kernel_timing(reset=True)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    kernel_ms, launches = eng.kernel_timing(reset=True)
+    if not kernel_ms > 0:
+        raise RuntimeError("no kernel timing was collected")
+    results = np.frombuffer(d_results.cpu().numpy().tobytes(), dtype=M.RESULT_DTYPE)
+    assert (results["path_count"] == c["path_count"]).all()
+
+    # End to end through the C ABI: host contracts in, host results out.
+    host_out = np.zeros(n, dtype=M.RESULT_DTYPE)
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_out = eng.price_batch(c, "fp32")
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_ms.append((t1 - t0) * 1e3)
+    e2e = sum(e2e_ms) / len(e2e_ms)
+    assert host_out.tobytes() == results.tobytes(), "device-resident and host paths disagree"
+
+    line = {
+        "metric": METRIC, "value": world * total_paths / (ms / 1e3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths / f64 accumulation",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "contracts": n, "total_paths": total_paths,
+                   "total_path_steps": total_steps, "parallelism": f"replicas x{world}",
+                   "l2": "flushed (256 MB write) between timed steps",
+                   "launch_shape": {"variant": variant, "ctas_per_sm": ctas}},
+        "contracts_per_second": world * n / (ms / 1e3),
+        "path_steps_per_second": world * total_steps / (ms / 1e3),
+        "gpu_launches": 2 * args.steps,
+        "e2e": {"value": world * total_paths / (e2e / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": n * 152 + (n + 1) * 4,
+                "d2h_bytes_per_step": n * M.RESULT_DTYPE.itemsize + 8},
+    }
+    # Roofline of the persistent path kernel: instruction issue (ALU-bound).
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    clk = clocks.summary()
+    mhz = clk["sm_mhz"] or peaks.get("sm_max_mhz", 2070.0)
+    ops_per_step = 118.0  # algorithmic thread-ops per FP32 GBM path-step (Philox + transform + step)
+    achieved = ops_per_step * total_steps / (kernel_ms / 1e3) / 1e12
+    peak = sm_count * 4 * 32 * mhz * 1e6 / 1e12
+    line["roofline"] = {"bound": "alu", "achieved": achieved, "peak": peak, "unit": "Tops/s",
+                        "frac": achieved / peak, "traffic": None,
+                        "kernel_ms": kernel_ms, "launches": launches,
+                        "note": "issue roofline: 4 SMSP x 32 lanes per SM at the sampled SM clock; "
+                                "118 algorithmic thread-ops per path-step"}
+    line["clocks"] = clk
+
+    if not args.no_fp64 and rank == 0:
+        sub = c[order[::64]]
+        r32 = eng.price_batch(sub, "fp32")
+        eng.kernel_timing(reset=True)
+        t0 = time.perf_counter()
+        r64 = eng.price_batch(sub, "fp64")
+        t64 = time.perf_counter() - t0
+        k64, _ = eng.kernel_timing(reset=True)
+        r32b = eng.price_batch(sub, "fp32")
+        k32, _ = eng.kernel_timing(reset=True)
+        se = np.maximum(r64["standard_error"], 1e-300)
+        err = np.abs(r32["price"] - r64["price"]) / se
+        line["fp64_gpu"] = {
+            "sample": f"{len(sub)} contracts (every 64th by cost)",
+            "fp64_kernel_ms": k64, "fp32_kernel_ms": k32, "speedup_fp32_over_fp64": k64 / k32,
+            "fp64_paths_per_second": float(sub["path_count"].astype(np.float64).sum()) / (k64 / 1e3),
+            "fp32_err_vs_fp64_max_se": float(err.max()), "fp32_err_vs_fp64_mean_se": float(err.mean()),
+            "fp64_wall_s": t64}
+        assert r32b.tobytes() == r32.tobytes()
+    if not args.no_cpu and rank == 0:
+        line["cpu_baseline"] = cpu_baseline_sample(c)
+    if rank == 0:
+        print(json.dumps(line))
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

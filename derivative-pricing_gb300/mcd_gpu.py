@@ -1,0 +1,276 @@
+"""Python access to libmcd_gpu.so through its C ABI (include/mcd_gpu.h).
+
+Function names and argument order follow the reference's Python module
+(bindings/python/src/module.cpp:64-293: ``monte_carlo_european``,
+``monte_carlo_asian``, ...), with one extra keyword, ``precision`` ("fp64" for
+the reference's arithmetic on the GPU, "fp32" for FP32 paths with FP64
+accumulation).  Every call goes to the GPU: there is no CPU fallback, and
+loading fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "build", "libmcd_gpu.so")
+
+u8, i32, u32, u64, dbl, vp = C.c_uint8, C.c_int, C.c_uint32, C.c_uint64, C.c_double, C.c_void_p
+P = C.POINTER
+
+CALL, PUT = 0, 1
+UP, DOWN = 0, 1
+IN, OUT = 0, 1
+FIXED, FLOATING = 0, 1
+CASH_OR_NOTHING, ASSET_OR_NOTHING = 0, 1
+ARITHMETIC, GEOMETRIC = 0, 1
+EUROPEAN, DIGITAL, ASIAN, BARRIER, LOOKBACK = 0, 1, 2, 3, 4
+FP64, FP32 = 0, 1
+SLAB_PATHS = 4096
+
+STATUS = {0: "ok", -1: "invalid argument", -2: "cuda error", -3: "out of memory", -4: "timeout",
+          -5: "unsupported", -6: "no device"}
+
+
+class McResult(C.Structure):
+    _fields_ = [("price", dbl), ("standard_error", dbl), ("path_count", u64)]
+
+    def __repr__(self):
+        return f"McResult(price={self.price!r}, standard_error={self.standard_error!r}, path_count={self.path_count})"
+
+
+class McOptions(C.Structure):
+    _fields_ = [("antithetic", u8), ("control_variate", u8), ("brownian_bridge", u8),
+                ("reserved", u8), ("num_threads", u32)]
+
+
+# numpy mirror of mcd_contract (include/mcd_gpu.h), 128 bytes.
+CONTRACT_DTYPE = np.dtype([
+    ("product", "<i4"), ("type", "<i4"), ("direction", "<i4"), ("knock", "<i4"),
+    ("strike_style", "<i4"), ("average_style", "<i4"), ("digital_style", "<i4"),
+    ("monitoring_points", "<i4"),
+    ("spot", "<f8"), ("strike", "<f8"), ("barrier", "<f8"), ("rebate", "<f8"), ("rate", "<f8"),
+    ("carry_yield", "<f8"), ("vol", "<f8"), ("time", "<f8"), ("cash_amount", "<f8"),
+    ("path_count", "<u8"), ("seed", "<u8"),
+    ("antithetic", "u1"), ("control_variate", "u1"), ("brownian_bridge", "u1"), ("reserved0", "u1"),
+    ("reserved1", "<u4"),
+])
+RESULT_DTYPE = np.dtype([("price", "<f8"), ("standard_error", "<f8"), ("path_count", "<u8")])
+assert CONTRACT_DTYPE.itemsize == 128 and RESULT_DTYPE.itemsize == 24
+
+
+class McdError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+def _prec(p) -> int:
+    if p in (0, "fp64", "FP64", "double"):
+        return FP64
+    if p in (1, "fp32", "FP32", "float"):
+        return FP32
+    raise ValueError(f"precision must be 'fp64' or 'fp32', got {p!r}")
+
+
+_lib = None
+
+
+def lib():
+    """Loads libmcd_gpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} not found: build it with derivative-pricing_gb300/build.py")
+    L = C.CDLL(LIB_PATH)
+
+    def sig(name, *args, res=i32):
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = list(args)
+
+    D6 = [dbl] * 6
+    sig("mcd_abi_version")
+    sig("mcd_create", i32, P(vp))
+    sig("mcd_destroy", vp, res=None)
+    sig("mcd_last_error", vp, res=C.c_char_p)
+    sig("mcd_synchronize", vp)
+    sig("mcd_price_european", vp, *D6, i32, u64, u64, P(McOptions), i32, P(McResult))
+    sig("mcd_price_digital", vp, *D6, i32, i32, dbl, u64, u64, P(McOptions), i32, P(McResult))
+    sig("mcd_price_asian", vp, *D6, i32, i32, i32, i32, u64, u64, P(McOptions), i32, P(McResult))
+    sig("mcd_price_barrier", vp, *([dbl] * 7), i32, i32, i32, dbl, i32, u64, u64, P(McOptions), i32,
+        P(McResult))
+    sig("mcd_price_lookback", vp, *D6, i32, i32, i32, u64, u64, P(McOptions), i32, P(McResult))
+    sig("mcd_price_batch", vp, vp, C.c_size_t, i32, vp)
+    sig("mcd_price_batch_device", vp, vp, C.c_size_t, i32, vp, vp)
+    sig("mcd_batch_invalidate", vp)
+    sig("mcd_set_launch_shape", vp, i32, i32, i32)
+    sig("mcd_get_launch_shape", vp, i32, P(i32), P(i32))
+    sig("mcd_autotune", vp, vp, C.c_size_t, i32, P(i32), P(i32), P(dbl))
+    sig("mcd_philox", vp, P(u32), P(u32), C.c_size_t, P(u32))
+    sig("mcd_draws", vp, u64, u64, u64, u32, u32, i32, i32, P(dbl))
+    sig("mcd_kernel_timing", vp, i32, P(dbl), P(u64))
+    _lib = L
+    return L
+
+
+class Engine:
+    """One mcd_ctx (device memory, stream, graphs) on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self._lib = lib()
+        h = vp()
+        rc = self._lib.mcd_create(device, C.byref(h))
+        if rc != 0:
+            raise McdError(rc, self._lib.mcd_last_error(None).decode())
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.mcd_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise McdError(rc, self._lib.mcd_last_error(self.handle).decode())
+
+    @staticmethod
+    def _opts(antithetic=False, control_variate=False, brownian_bridge=False):
+        return McOptions(int(bool(antithetic)), int(bool(control_variate)),
+                         int(bool(brownian_bridge)), 0, 1)
+
+    # -- reference pricer signatures (src/pricers/monte_carlo.cpp:233-338) ---------------
+    def monte_carlo_european(self, spot, strike, rate, carry_yield, vol, time, type, path_count,
+                             seed, antithetic=False, precision="fp64") -> McResult:
+        out = McResult()
+        o = self._opts(antithetic)
+        self._check(self._lib.mcd_price_european(self.handle, spot, strike, rate, carry_yield, vol,
+                                                 time, type, path_count, seed, C.byref(o),
+                                                 _prec(precision), C.byref(out)))
+        return out
+
+    def monte_carlo_digital(self, spot, strike, rate, carry_yield, vol, time, type, style,
+                            cash_amount, path_count, seed, antithetic=False,
+                            precision="fp64") -> McResult:
+        out = McResult()
+        o = self._opts(antithetic)
+        self._check(self._lib.mcd_price_digital(self.handle, spot, strike, rate, carry_yield, vol,
+                                                time, type, style, cash_amount, path_count, seed,
+                                                C.byref(o), _prec(precision), C.byref(out)))
+        return out
+
+    def monte_carlo_asian(self, spot, strike, rate, carry_yield, vol, time, type, strike_style,
+                          average_style, monitoring_points, path_count, seed, antithetic=False,
+                          control_variate=False, precision="fp64") -> McResult:
+        out = McResult()
+        o = self._opts(antithetic, control_variate)
+        self._check(self._lib.mcd_price_asian(self.handle, spot, strike, rate, carry_yield, vol,
+                                              time, type, strike_style, average_style,
+                                              monitoring_points, path_count, seed, C.byref(o),
+                                              _prec(precision), C.byref(out)))
+        return out
+
+    def monte_carlo_barrier(self, spot, strike, barrier, rate, carry_yield, vol, time, type,
+                            direction, knock, rebate, monitoring_points, path_count, seed,
+                            antithetic=False, brownian_bridge=False, precision="fp64") -> McResult:
+        out = McResult()
+        o = self._opts(antithetic, False, brownian_bridge)
+        self._check(self._lib.mcd_price_barrier(self.handle, spot, strike, barrier, rate,
+                                                carry_yield, vol, time, type, direction, knock,
+                                                rebate, monitoring_points, path_count, seed,
+                                                C.byref(o), _prec(precision), C.byref(out)))
+        return out
+
+    def monte_carlo_lookback(self, spot, strike, rate, carry_yield, vol, time, type, style,
+                             monitoring_points, path_count, seed, antithetic=False,
+                             precision="fp64") -> McResult:
+        out = McResult()
+        o = self._opts(antithetic)
+        self._check(self._lib.mcd_price_lookback(self.handle, spot, strike, rate, carry_yield, vol,
+                                                 time, type, style, monitoring_points, path_count,
+                                                 seed, C.byref(o), _prec(precision),
+                                                 C.byref(out)))
+        return out
+
+    # -- batch -----------------------------------------------------------------------------
+    def price_batch(self, contracts: np.ndarray, precision="fp64") -> np.ndarray:
+        contracts = np.ascontiguousarray(contracts, dtype=CONTRACT_DTYPE)
+        out = np.zeros(len(contracts), dtype=RESULT_DTYPE)
+        self._check(self._lib.mcd_price_batch(self.handle, contracts.ctypes.data, len(contracts),
+                                              _prec(precision), out.ctypes.data))
+        return out
+
+    def price_batch_device(self, contracts_ptr: int, n: int, results_ptr: int, precision="fp32",
+                           stream: int = 0) -> None:
+        self._check(self._lib.mcd_price_batch_device(self.handle, vp(contracts_ptr), n,
+                                                     _prec(precision), vp(results_ptr),
+                                                     vp(stream) if stream else None))
+
+    def invalidate(self):
+        self._check(self._lib.mcd_batch_invalidate(self.handle))
+
+    def set_launch_shape(self, precision, variant: int, ctas_per_sm: int):
+        self._check(self._lib.mcd_set_launch_shape(self.handle, _prec(precision), variant,
+                                                   ctas_per_sm))
+
+    def launch_shape(self, precision):
+        v, c = i32(), i32()
+        self._check(self._lib.mcd_get_launch_shape(self.handle, _prec(precision), C.byref(v),
+                                                   C.byref(c)))
+        return v.value, c.value
+
+    def autotune(self, contracts: np.ndarray, precision="fp32"):
+        contracts = np.ascontiguousarray(contracts, dtype=CONTRACT_DTYPE)
+        v, c, ms = i32(), i32(), dbl()
+        self._check(self._lib.mcd_autotune(self.handle, contracts.ctypes.data, len(contracts),
+                                           _prec(precision), C.byref(v), C.byref(c), C.byref(ms)))
+        return v.value, c.value, ms.value
+
+    def synchronize(self):
+        self._check(self._lib.mcd_synchronize(self.handle))
+
+    def kernel_timing(self, reset=False):
+        ms, n = dbl(), u64()
+        self._check(self._lib.mcd_kernel_timing(self.handle, int(reset), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    # -- draws -----------------------------------------------------------------------------
+    def philox(self, counters: np.ndarray, keys: np.ndarray) -> np.ndarray:
+        counters = np.ascontiguousarray(counters, dtype=np.uint32).reshape(-1, 4)
+        keys = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 2)
+        out = np.zeros_like(counters)
+        self._check(self._lib.mcd_philox(self.handle, counters.ctypes.data_as(P(u32)),
+                                         keys.ctypes.data_as(P(u32)), len(counters),
+                                         out.ctypes.data_as(P(u32))))
+        return out
+
+    def draws(self, seed, path_begin, n_paths, draw_begin, n_draws, stream_id=0,
+              precision="fp64") -> np.ndarray:
+        out = np.zeros((n_paths, n_draws), dtype=np.float64)
+        self._check(self._lib.mcd_draws(self.handle, seed, path_begin, n_paths, draw_begin, n_draws,
+                                        stream_id, _prec(precision), out.ctypes.data_as(P(dbl))))
+        return out
+
+
+def contracts(n: int) -> np.ndarray:
+    """A zeroed contract array (cash_amount 1, monitoring_points 1)."""
+    a = np.zeros(n, dtype=CONTRACT_DTYPE)
+    a["cash_amount"] = 1.0
+    a["monitoring_points"] = 1
+    return a

@@ -1,0 +1,196 @@
+/*
+ * mcd_gpu.h -- C ABI of the GB300 (sm_103a) Monte Carlo engine for mcd.
+ *
+ * One shared library (libmcd_gpu.so) with plain C types: no C++ or torch types
+ * cross this boundary.  Every entry point returns an mcd_status (0 = success,
+ * negative = error); mcd_last_error() gives the message.  The caller owns every
+ * host array passed in or out; an mcd_ctx owns its device memory, stream and
+ * captured CUDA graphs.  Use one context per host thread (calls on a context
+ * are stream-ordered and not thread-safe).
+ *
+ * Each pricing entry point replaces one reference function (cited per
+ * declaration; paths are within FredTheMay/derivative-pricing).  The reference
+ * functions are noexcept and "trust the caller"; this ABI validates arguments
+ * instead and reports MCD_ERR_INVALID_ARGUMENT.
+ *
+ * Precision (mcd_precision):
+ *   MCD_PRECISION_FP64  the reference's arithmetic in FP64 on the GPU (Acklam
+ *                       inverse CDF with its Halley step, multiplicative GBM
+ *                       steps); identical draws; prices agree with the CPU
+ *                       reference to ~1e-12 relative.
+ *   MCD_PRECISION_FP32  the same Philox draws (same counters, word 0) turned
+ *                       into FP32 normals; paths evolve in FP32 (log space);
+ *                       payoffs are accumulated and merged in FP64.
+ *
+ * Results are bitwise identical for a given precision regardless of launch
+ * configuration (grid size, kernel variant): paths are grouped into fixed
+ * slabs of MCD_SLAB_PATHS and every reduction tree is fixed by slab index.
+ */
+#ifndef MCD_GPU_H
+#define MCD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCD_GPU_ABI_VERSION 1
+#define MCD_SLAB_PATHS 4096
+
+typedef struct mcd_ctx mcd_ctx;
+
+typedef enum {
+    MCD_OK = 0,
+    MCD_ERR_INVALID_ARGUMENT = -1,
+    MCD_ERR_CUDA = -2,
+    MCD_ERR_OUT_OF_MEMORY = -3,
+    MCD_ERR_TIMEOUT = -4,
+    MCD_ERR_UNSUPPORTED = -5,
+    MCD_ERR_NO_DEVICE = -6
+} mcd_status;
+
+typedef enum { MCD_PRECISION_FP64 = 0, MCD_PRECISION_FP32 = 1 } mcd_precision;
+
+/* Same values as mcd's enums (include/mcd/core/types.hpp:12-17). */
+typedef enum { MCD_CALL = 0, MCD_PUT = 1 } mcd_option_type;
+typedef enum { MCD_UP = 0, MCD_DOWN = 1 } mcd_barrier_direction;
+typedef enum { MCD_IN = 0, MCD_OUT = 1 } mcd_barrier_knock;
+typedef enum { MCD_FIXED = 0, MCD_FLOATING = 1 } mcd_strike_style;
+typedef enum { MCD_CASH_OR_NOTHING = 0, MCD_ASSET_OR_NOTHING = 1 } mcd_digital_style;
+typedef enum { MCD_ARITHMETIC = 0, MCD_GEOMETRIC = 1 } mcd_average_style;
+
+typedef enum {
+    MCD_PRODUCT_EUROPEAN = 0,
+    MCD_PRODUCT_DIGITAL = 1,
+    MCD_PRODUCT_ASIAN = 2,
+    MCD_PRODUCT_BARRIER = 3,
+    MCD_PRODUCT_LOOKBACK = 4
+} mcd_product;
+
+/* mcd::pricers::McResult (include/mcd/pricers/monte_carlo.hpp:9-13). */
+typedef struct {
+    double price;
+    double standard_error;
+    uint64_t path_count;
+} mcd_mc_result;
+
+/* mcd::pricers::McOptions (include/mcd/pricers/monte_carlo.hpp:18-33).
+ * num_threads is accepted and ignored: the GPU result does not depend on it,
+ * just as the reference's does not. */
+typedef struct {
+    uint8_t antithetic;
+    uint8_t control_variate;
+    uint8_t brownian_bridge;
+    uint8_t reserved;
+    uint32_t num_threads;
+} mcd_mc_options;
+
+/* One contract of a batch: the argument list of the reference pricer for
+ * `product` (monte_carlo.hpp:38-80) flattened into one record.  Fields a
+ * product does not use are ignored.  Draws are keyed on (seed, path, step)
+ * exactly as in the reference, so a contract priced alone and inside a batch
+ * gives the same result. */
+typedef struct {
+    int32_t product;           /* mcd_product */
+    int32_t type;              /* mcd_option_type */
+    int32_t direction;         /* barrier: mcd_barrier_direction */
+    int32_t knock;             /* barrier: mcd_barrier_knock */
+    int32_t strike_style;      /* asian, lookback: mcd_strike_style */
+    int32_t average_style;     /* asian: mcd_average_style */
+    int32_t digital_style;     /* digital: mcd_digital_style */
+    int32_t monitoring_points; /* asian, barrier, lookback (>= 1) */
+    double spot, strike, barrier, rebate, rate, carry_yield, vol, time, cash_amount;
+    uint64_t path_count;
+    uint64_t seed;
+    uint8_t antithetic, control_variate, brownian_bridge, reserved0;
+    uint32_t reserved1;
+} mcd_contract;
+
+/* ---- context ------------------------------------------------------------ */
+int mcd_abi_version(void);
+/* Creates a context on CUDA device `device` (its own non-blocking stream). */
+int mcd_create(int device, mcd_ctx** out);
+void mcd_destroy(mcd_ctx* ctx);
+/* Message of the last failed call on ctx (or of the last failed mcd_create
+ * when ctx is NULL).  Valid until the next call on the same context. */
+const char* mcd_last_error(const mcd_ctx* ctx);
+/* Blocks until all work queued on the context's stream has finished. */
+int mcd_synchronize(mcd_ctx* ctx);
+
+/* ---- single-contract pricers (one GPU launch each) ---------------------- */
+/* replaces mcd::pricers::monte_carlo_european (src/pricers/monte_carlo.cpp:233-249) */
+int mcd_price_european(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                       double vol, double time, int type, uint64_t path_count, uint64_t seed,
+                       const mcd_mc_options* options, int precision, mcd_mc_result* out);
+/* replaces mcd::pricers::monte_carlo_digital (src/pricers/monte_carlo.cpp:251-260) */
+int mcd_price_digital(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                      double vol, double time, int type, int digital_style, double cash_amount,
+                      uint64_t path_count, uint64_t seed, const mcd_mc_options* options,
+                      int precision, mcd_mc_result* out);
+/* replaces mcd::pricers::monte_carlo_asian (src/pricers/monte_carlo.cpp:262-308) */
+int mcd_price_asian(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                    double vol, double time, int type, int strike_style, int average_style,
+                    int monitoring_points, uint64_t path_count, uint64_t seed,
+                    const mcd_mc_options* options, int precision, mcd_mc_result* out);
+/* replaces mcd::pricers::monte_carlo_barrier (src/pricers/monte_carlo.cpp:310-324) */
+int mcd_price_barrier(mcd_ctx* ctx, double spot, double strike, double barrier, double rate,
+                      double carry_yield, double vol, double time, int type, int direction,
+                      int knock, double rebate, int monitoring_points, uint64_t path_count,
+                      uint64_t seed, const mcd_mc_options* options, int precision,
+                      mcd_mc_result* out);
+/* replaces mcd::pricers::monte_carlo_lookback (src/pricers/monte_carlo.cpp:326-338) */
+int mcd_price_lookback(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                       double vol, double time, int type, int strike_style, int monitoring_points,
+                       uint64_t path_count, uint64_t seed, const mcd_mc_options* options,
+                       int precision, mcd_mc_result* out);
+
+/* ---- batched pricing: one persistent-kernel launch in a CUDA graph ------ */
+/* Host arrays in and out (copies included).  Equivalent to calling the
+ * reference pricer once per contract (monte_carlo.cpp:233-338). */
+int mcd_price_batch(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, int precision,
+                    mcd_mc_result* results);
+/* Device-resident variant: `contracts` and `results` are device pointers; the
+ * work is queued on `stream` (a cudaStream_t, or NULL for the context's
+ * stream) and the call returns without synchronising.  The contract list is
+ * read from the device once to plan the launch; replanning happens only when
+ * the pointer, count or precision changes (mcd_batch_invalidate forces it). */
+int mcd_price_batch_device(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, int precision,
+                           mcd_mc_result* results, void* stream);
+int mcd_batch_invalidate(mcd_ctx* ctx);
+
+/* Launch shape of the persistent path kernel.  variant 0..3 selects the
+ * register budget (__launch_bounds__ min blocks 4/8/12/16), ctas_per_sm the
+ * grid (SM count x ctas_per_sm).  0 restores the autotuned/default choice.
+ * Results do not depend on either. */
+int mcd_set_launch_shape(mcd_ctx* ctx, int precision, int variant, int ctas_per_sm);
+int mcd_get_launch_shape(mcd_ctx* ctx, int precision, int* variant, int* ctas_per_sm);
+/* Autotuner: times every launch shape on `contracts` (host array) and keeps
+ * the fastest for `precision`.  Writes the chosen shape and its time. */
+int mcd_autotune(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, int precision,
+                 int* variant, int* ctas_per_sm, double* best_ms);
+
+/* ---- draws (parity and diagnostics) ------------------------------------- */
+/* Philox4x32-10 of n (counter, key) pairs; replaces mcd::philox4x32_10
+ * (src/core/rng.cpp:41-47).  counters: n x 4, keys: n x 2, out: n x 4. */
+int mcd_philox(mcd_ctx* ctx, const uint32_t* counters, const uint32_t* keys, size_t n,
+               uint32_t* out);
+/* Draws for paths [path_begin, path_begin+n_paths) x draws
+ * [draw_begin, draw_begin+n_draws), row-major by path.  stream_id 0 gives the
+ * standard normal of mcd::standard_normal_variate (src/core/rng.cpp:59-66),
+ * stream_id 1 the uniform of mcd::uniform_variate (:68-74); precision picks the
+ * FP64 or FP32 transform (FP32 values are widened to double). */
+int mcd_draws(mcd_ctx* ctx, uint64_t seed, uint64_t path_begin, uint64_t n_paths,
+              uint32_t draw_begin, uint32_t n_draws, int stream_id, int precision, double* out);
+
+/* ---- timing helper for benchmarks ---------------------------------------- */
+/* Average device time (ms) of the persistent path kernel over the calls made
+ * since the last reset, measured with CUDA events on the launching stream. */
+int mcd_kernel_timing(mcd_ctx* ctx, int reset, double* avg_ms, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCD_GPU_H */
