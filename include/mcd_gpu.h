@@ -160,6 +160,36 @@ int mcd_price_batch_device(mcd_ctx* ctx, const mcd_contract* contracts, size_t n
                            mcd_mc_result* results, void* stream);
 int mcd_batch_invalidate(mcd_ctx* ctx);
 
+/* Batched pricing that allocates no memory.  No counterpart in the reference
+ * (the reference has no GPU and no device memory).
+ *
+ * For callers that cannot call cudaMalloc: services that reserve all device
+ * memory when they start and must not allocate afterwards, and code where an
+ * allocation's implicit device synchronisation is not acceptable.  It needs
+ * no mcd_ctx.  It runs the same kernels as mcd_price_batch and returns bitwise
+ * the same results; its scratch (contract records, slab partials, device
+ * results, ticket and error word) lives in one fixed __device__ array of
+ * about 7 MB.  Every GPU that loads the library holds that array until the
+ * process exits.
+ *
+ * Limits: at most 4096 contracts and 262144 slabs of MCD_SLAB_PATHS paths
+ * (about 1.07e9 paths in total) per call.  Larger requests fail with
+ * MCD_ERR_INVALID_ARGUMENT and a message saying which limit was hit.
+ * Inputs and outputs are host arrays; `stream` is a cudaStream_t (NULL: the
+ * legacy default stream) on the current device.  The call returns when the
+ * results are in `results`.  On failure, a message is written to
+ * error_message (if error_capacity > 0).
+ *
+ * The first call on a device does the set-up for that device: it resolves the
+ * array's device address with that device current.  Make that first call
+ * before any stream capture.  All calls share the one array, and it keeps
+ * the last call's contents.  Calls that overlapped on the GPU would race on
+ * it; this entry point serialises its calls with a process-wide lock and
+ * waits for its GPU work before returning, so its own calls never overlap. */
+int mcd_price_batch_static(const mcd_contract* contracts, size_t n, int precision,
+                           mcd_mc_result* results, void* stream, char* error_message,
+                           size_t error_capacity);
+
 /* Launch shape of the persistent path kernel.  variant 0..3 selects the
  * register budget (__launch_bounds__ min blocks 4/8/12/16), ctas_per_sm the
  * grid (SM count x ctas_per_sm).  0 restores the autotuned/default choice.
