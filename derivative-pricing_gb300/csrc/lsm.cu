@@ -1,0 +1,514 @@
+// lsm.cu -- batched Longstaff-Schwartz American pricing (QR regression).
+//
+// Reference: monte_carlo_lsm_american (src/pricers/lsm.cpp:62-149) and
+// reprice_against_frozen_policy (:151-213): forward-simulated GBM paths, cash
+// flows seeded with the terminal intrinsic, backward over dates n-1..1 (discount
+// the cash flows, regress them on the weighted Laguerre basis of S/K over the
+// in-the-money paths -- skipped below 4 such paths --, exercise where
+// intrinsic > continuation), a final discount, Welford, and the inception check.
+//
+// Layout.  Every contract's paths live in HBM for the whole backward pass,
+// date-major (S[d-1][i], coalesced per date for the forward stores and the
+// backward column reads), FP32 or FP64; cash flows are FP64.  Paths are cut
+// into fixed chunks of 1024 (the reduction unit); a chunk is one CTA of 256
+// threads (4 paths per thread, stride 256).
+//
+// Backward pass.  All contracts of a batch step back in lockstep: iteration k
+// handles date e = n_c - k of contract c.  Per iteration:
+//   lsm_exercise  exercise at date e with that date's coefficients, discount,
+//                 and either the Gram sums of date e-1 (pass A) or, when e = 1,
+//                 the final Welford partial;
+//   lsm_solve_a   per contract: fixed-order reduction, Cholesky G = R^T R,
+//                 T = R^{-1};
+//   lsm_gram_b    Gram sums and right-hand side in the preconditioned basis
+//                 b' = b T (pass B);
+//   lsm_solve_b   per contract: reduction, 4x4 Householder solve of
+//                 G' beta' = h', gamma = T beta' (coefficients in the
+//                 Laguerre basis, as the reference's policy stores them).
+// This is Cholesky-QR2 applied to the least-squares problem: the first pass
+// removes the conditioning (cond(X) reaches ~2e6 for these bases, cond(G)
+// ~4e12), the second is solved at QR accuracy, so the coefficients agree with
+// the reference's Householder QR to ~1e-10 relative and exercise decisions
+// essentially never differ.  All sums are FP64 and every reduction tree is
+// fixed by chunk index.
+//
+// nvcc-flags: --fmad=false
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+#include "lsm.hpp"
+
+namespace mcdg {
+
+namespace {
+
+__device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
+
+__device__ __forceinline__ double intrinsic(double s, double k, int type) {
+    return dmax((type == 0 ? 1.0 : -1.0) * (s - k), 0.0);
+}
+
+// Weighted Laguerre basis on x = S/K (src/pricers/lsm.cpp:21-25).  FP64 path:
+// the reference's expressions.  FP32 path: the common factor exp(-x/2) in
+// FP32 (a relative error there scales the continuation value, it is not
+// amplified by the large coefficients), the polynomials in FP64.
+template <int PREC>
+__device__ __forceinline__ void basis(double s, double strike, double inv_strike, double b[4]) {
+    double x, e;
+    if (PREC == 0) {
+        x = s / strike;
+        e = exp(-x / 2.0);
+    } else {
+        x = s * inv_strike;
+        e = static_cast<double>(__expf(-0.5f * static_cast<float>(x)));
+    }
+    b[0] = e;
+    b[1] = e * (1.0 - x);
+    b[2] = e * (1.0 - 2.0 * x + 0.5 * x * x);
+    b[3] = e * (1.0 - 3.0 * x + 1.5 * x * x - x * x * x / 6.0);
+}
+
+template <int PREC>
+__device__ __forceinline__ double load_s(const void* store, uint64_t idx) {
+    if (PREC == 0) return static_cast<const double*>(store)[idx];
+    return static_cast<double>(static_cast<const float*>(store)[idx]);
+}
+
+// Fixed-shape block reduction of N doubles (256 threads): warp trees, then
+// warp 0 folds the 8 warp results in order.  Result valid in thread 0.
+template <int N>
+__device__ void block_sum(double (&v)[N], double (*smem)[N]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        double x = v[i];
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+        v[i] = x;
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) smem[warp][i] = v[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            double x = smem[0][i];
+            for (int w = 1; w < kLsmThreads / 32; ++w) x += smem[w][i];
+            v[i] = x;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// forward simulation (src/pricers/lsm.cpp:35-58), date-major stores
+// ---------------------------------------------------------------------------
+template <int PREC>
+__global__ void __launch_bounds__(kLsmThreads)
+    lsm_forward(const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
+                uint32_t total_chunks, void* __restrict__ store) {
+    const uint32_t chunk = blockIdx.x;
+    if (chunk >= total_chunks) return;
+    const LsmDev c = cs[chunk_contract[chunk]];
+    const uint32_t local = chunk - c.chunk_begin;
+    const PhiloxKeys k = philox_keys(c.seed);
+    const float mu = static_cast<float>(c.drift), sg = static_cast<float>(c.vs);
+    const float s0 = static_cast<float>(c.spot);
+    for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+        const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
+        if (i >= c.path_count) break;
+        const PhiloxPath pp = philox_path(i, 0u, k);
+        if (PREC == 0) {
+            double* S = static_cast<double*>(store) + c.s_offset;
+            double s = c.spot;
+            for (int d = 0; d < c.n_steps; ++d) {
+                const double z = normal_from_bits_f64(philox_word0(pp, static_cast<uint32_t>(d), k));
+                s = s * exp(c.drift + c.vs * z);
+                S[static_cast<uint64_t>(d) * c.path_count + i] = s;
+            }
+        } else {
+            float* S = static_cast<float*>(store) + c.s_offset;
+            float x = 0.0f;
+            for (int d = 0; d < c.n_steps; ++d) {
+                const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(d), k));
+                x = __fmaf_rn(sg, z, x + mu);
+                S[static_cast<uint64_t>(d) * c.path_count + i] = s0 * __expf(x);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// iteration k: exercise at date e, discount, pass A for date e-1 (or final)
+// ---------------------------------------------------------------------------
+template <int PREC>
+__global__ void __launch_bounds__(kLsmThreads)
+    lsm_exercise(int k, int frozen, const LsmDev* __restrict__ cs,
+                 const uint32_t* __restrict__ chunk_contract, uint32_t total_chunks,
+                 const void* __restrict__ store, double* __restrict__ cf,
+                 const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_a,
+                 Welford* __restrict__ final_part) {
+    __shared__ double smem[kLsmThreads / 32][11];
+    __shared__ Welford swf[kLsmThreads / 32];
+    const uint32_t chunk = blockIdx.x;
+    if (chunk >= total_chunks) return;
+    const LsmDev c = cs[chunk_contract[chunk]];
+    const int n = c.n_steps;
+    const int e = n - k;
+    if (e < 1) return;  // this contract has finished (uniform per CTA)
+    const bool init = (k == 0);
+    const bool last = (e == 1);
+    const bool gram = !frozen && !last;
+    const LsmReg* re = (!init && e <= n - 1) ? &reg[c.reg_offset + e] : nullptr;
+    const bool exercise = re != nullptr && re->has == 1;
+    double g0 = 0, g1 = 0, g2 = 0, g3 = 0;
+    if (exercise) {
+        g0 = re->gamma[0];
+        g1 = re->gamma[1];
+        g2 = re->gamma[2];
+        g3 = re->gamma[3];
+    }
+    const double inv_k = 1.0 / c.strike;
+    double acc[11];
+#pragma unroll
+    for (int q = 0; q < 11; ++q) acc[q] = 0.0;
+    Welford w{0ull, 0.0, 0.0};
+    const uint32_t local = chunk - c.chunk_begin;
+    for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+        const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
+        if (i >= c.path_count) break;
+        double v;
+        if (init) {
+            v = intrinsic(load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(n - 1) * c.path_count + i),
+                          c.strike, c.type);
+        } else {
+            v = cf[c.cf_offset + i];
+            if (exercise) {
+                const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 1) * c.path_count + i);
+                const double ex = intrinsic(s, c.strike, c.type);
+                if (ex > 0.0) {
+                    double b[4];
+                    basis<PREC>(s, c.strike, inv_k, b);
+                    double cont = 0.0;
+                    cont += g0 * b[0];
+                    cont += g1 * b[1];
+                    cont += g2 * b[2];
+                    cont += g3 * b[3];
+                    if (ex > cont) v = ex;
+                }
+            }
+        }
+        v *= c.disc;
+        if (last) {
+            welford_add(w, v);
+        } else {
+            cf[c.cf_offset + i] = v;
+            if (gram) {
+                const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 2) * c.path_count + i);
+                if (intrinsic(s, c.strike, c.type) > 0.0) {
+                    double b[4];
+                    basis<PREC>(s, c.strike, inv_k, b);
+                    acc[0] += 1.0;
+                    acc[1] += b[0] * b[0];
+                    acc[2] += b[0] * b[1];
+                    acc[3] += b[0] * b[2];
+                    acc[4] += b[0] * b[3];
+                    acc[5] += b[1] * b[1];
+                    acc[6] += b[1] * b[2];
+                    acc[7] += b[1] * b[3];
+                    acc[8] += b[2] * b[2];
+                    acc[9] += b[2] * b[3];
+                    acc[10] += b[3] * b[3];
+                }
+            }
+        }
+    }
+    if (last) {
+        w = welford_warp_reduce(w);
+        if ((threadIdx.x & 31) == 0) swf[threadIdx.x >> 5] = w;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            Welford m = swf[0];
+            for (int q = 1; q < kLsmThreads / 32; ++q) m = welford_merge(m, swf[q]);
+            final_part[chunk] = m;
+        }
+    } else if (gram) {
+        block_sum<11>(acc, smem);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int q = 0; q < 11; ++q) part_a[chunk].v[q] = acc[q];
+        }
+    }
+}
+
+// Upper-triangular index of (r, c), r <= c, in the packed 10-entry layout.
+__device__ __forceinline__ int tri(int r, int col) {
+    const int base[4] = {0, 4, 7, 9};
+    return base[r] + (col - r);
+}
+
+// Per contract: fold pass-A partials in chunk order, Cholesky, T = R^{-1}.
+__global__ void lsm_solve_a(int k, const LsmDev* __restrict__ cs, int n_contracts,
+                            const LsmPartial* __restrict__ part_a, LsmReg* __restrict__ reg) {
+    const int ci = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (ci >= n_contracts) return;
+    const LsmDev c = cs[ci];
+    const int date = c.n_steps - k - 1;  // regression date of this iteration
+    if (date < 1) return;
+    double s[11];
+#pragma unroll
+    for (int q = 0; q < 11; ++q) s[q] = 0.0;
+    for (uint32_t ch = lane; ch < c.n_chunks; ch += 32)
+#pragma unroll
+        for (int q = 0; q < 11; ++q) s[q] += part_a[c.chunk_begin + ch].v[q];
+#pragma unroll
+    for (int q = 0; q < 11; ++q)
+        for (int off = 16; off >= 1; off >>= 1) s[q] += __shfl_down_sync(0xffffffffu, s[q], off);
+    if (lane != 0) return;
+    LsmReg& r = reg[c.reg_offset + date];
+    r.has = 0;
+    r.degenerate = 0;
+    if (s[0] < 4.0) {  // too few in-the-money paths (src/pricers/lsm.cpp:102-104)
+        r.has = -1;
+        return;
+    }
+    double G[4][4];
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = a; b2 < 4; ++b2) G[a][b2] = G[b2][a] = s[1 + tri(a, b2)];
+    double R[4][4] = {};
+    bool ok = true;
+    for (int j = 0; j < 4 && ok; ++j) {
+        double d = G[j][j];
+        for (int p = 0; p < j; ++p) d -= R[p][j] * R[p][j];
+        if (!(d > 0.0)) {
+            ok = false;
+            break;
+        }
+        R[j][j] = sqrt(d);
+        for (int l = j + 1; l < 4; ++l) {
+            double x = G[j][l];
+            for (int p = 0; p < j; ++p) x -= R[p][j] * R[p][l];
+            R[j][l] = x / R[j][j];
+        }
+    }
+    double T[4][4] = {};
+    if (ok) {
+        for (int j = 3; j >= 0; --j) {
+            T[j][j] = 1.0 / R[j][j];
+            for (int l = j + 1; l < 4; ++l) {
+                double x = 0.0;
+                for (int p = j; p < l; ++p) x += T[j][p] * R[p][l];
+                T[j][l] = -x / R[l][l];
+            }
+        }
+    } else {
+        for (int j = 0; j < 4; ++j) T[j][j] = 1.0;
+        r.degenerate = 1;
+    }
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = a; b2 < 4; ++b2) r.T[tri(a, b2)] = T[a][b2];
+}
+
+// Pass B: Gram sums and right-hand side in the preconditioned basis b' = b T.
+template <int PREC>
+__global__ void __launch_bounds__(kLsmThreads)
+    lsm_gram_b(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
+               uint32_t total_chunks, const void* __restrict__ store, const double* __restrict__ cf,
+               const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_b) {
+    __shared__ double smem[kLsmThreads / 32][15];
+    const uint32_t chunk = blockIdx.x;
+    if (chunk >= total_chunks) return;
+    const LsmDev c = cs[chunk_contract[chunk]];
+    const int date = c.n_steps - k - 1;
+    if (date < 1) return;
+    const LsmReg& r = reg[c.reg_offset + date];
+    if (r.has == -1) return;  // no regression at this date
+    double T[10];
+#pragma unroll
+    for (int q = 0; q < 10; ++q) T[q] = r.T[q];
+    const double inv_k = 1.0 / c.strike;
+    double acc[15];
+#pragma unroll
+    for (int q = 0; q < 15; ++q) acc[q] = 0.0;
+    const uint32_t local = chunk - c.chunk_begin;
+    for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+        const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
+        if (i >= c.path_count) break;
+        const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(date - 1) * c.path_count + i);
+        if (!(intrinsic(s, c.strike, c.type) > 0.0)) continue;
+        double b[4];
+        basis<PREC>(s, c.strike, inv_k, b);
+        // b'_l = sum_{j <= l} b_j T[j][l]
+        double q0 = b[0] * T[0];
+        double q1 = b[0] * T[1] + b[1] * T[4];
+        double q2 = b[0] * T[2] + b[1] * T[5] + b[2] * T[7];
+        double q3 = b[0] * T[3] + b[1] * T[6] + b[2] * T[8] + b[3] * T[9];
+        const double y = cf[c.cf_offset + i];
+        acc[0] += 1.0;
+        acc[1] += q0 * q0;
+        acc[2] += q0 * q1;
+        acc[3] += q0 * q2;
+        acc[4] += q0 * q3;
+        acc[5] += q1 * q1;
+        acc[6] += q1 * q2;
+        acc[7] += q1 * q3;
+        acc[8] += q2 * q2;
+        acc[9] += q2 * q3;
+        acc[10] += q3 * q3;
+        acc[11] += q0 * y;
+        acc[12] += q1 * y;
+        acc[13] += q2 * y;
+        acc[14] += q3 * y;
+    }
+    block_sum<15>(acc, smem);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < 15; ++q) part_b[chunk].v[q] = acc[q];
+    }
+}
+
+// 4x4 Householder least squares (the reference's algorithm, src/core/linalg.cpp:7-71,
+// on a square system): A is overwritten, y too.
+__device__ void householder4(double A[4][4], double y[4], double beta[4]) {
+    for (int kk = 0; kk < 4; ++kk) {
+        double norm_sq = 0.0;
+        for (int i = kk; i < 4; ++i) norm_sq += A[i][kk] * A[i][kk];
+        const double norm = sqrt(norm_sq);
+        if (norm == 0.0) continue;
+        const double akk = A[kk][kk];
+        const double alpha = akk >= 0.0 ? -norm : norm;
+        double v[4] = {0, 0, 0, 0};
+        v[kk] = akk - alpha;
+        for (int i = kk + 1; i < 4; ++i) v[i] = A[i][kk];
+        double vn = 0.0;
+        for (int i = kk; i < 4; ++i) vn += v[i] * v[i];
+        if (vn == 0.0) continue;
+        for (int jj = kk; jj < 4; ++jj) {
+            double dot = 0.0;
+            for (int i = kk; i < 4; ++i) dot += v[i] * A[i][jj];
+            const double f = 2.0 * dot / vn;
+            for (int i = kk; i < 4; ++i) A[i][jj] -= f * v[i];
+        }
+        double dy = 0.0;
+        for (int i = kk; i < 4; ++i) dy += v[i] * y[i];
+        const double fy = 2.0 * dy / vn;
+        for (int i = kk; i < 4; ++i) y[i] -= fy * v[i];
+    }
+    for (int i = 3; i >= 0; --i) {
+        double sum = y[i];
+        for (int jj = i + 1; jj < 4; ++jj) sum -= A[i][jj] * beta[jj];
+        const double diag = A[i][i];
+        beta[i] = diag != 0.0 ? sum / diag : 0.0;
+    }
+}
+
+__global__ void lsm_solve_b(int k, const LsmDev* __restrict__ cs, int n_contracts,
+                            const LsmPartial* __restrict__ part_b, LsmReg* __restrict__ reg) {
+    const int ci = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (ci >= n_contracts) return;
+    const LsmDev c = cs[ci];
+    const int date = c.n_steps - k - 1;
+    if (date < 1) return;
+    LsmReg& r = reg[c.reg_offset + date];
+    if (r.has == -1) return;
+    double s[15];
+#pragma unroll
+    for (int q = 0; q < 15; ++q) s[q] = 0.0;
+    for (uint32_t ch = lane; ch < c.n_chunks; ch += 32)
+#pragma unroll
+        for (int q = 0; q < 15; ++q) s[q] += part_b[c.chunk_begin + ch].v[q];
+#pragma unroll
+    for (int q = 0; q < 15; ++q)
+        for (int off = 16; off >= 1; off >>= 1) s[q] += __shfl_down_sync(0xffffffffu, s[q], off);
+    if (lane != 0) return;
+    double G[4][4], y[4], beta[4] = {0, 0, 0, 0};
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = a; b2 < 4; ++b2) G[a][b2] = G[b2][a] = s[1 + tri(a, b2)];
+    for (int a = 0; a < 4; ++a) y[a] = s[11 + a];
+    householder4(G, y, beta);
+    // gamma = T beta
+    for (int a = 0; a < 4; ++a) {
+        double x = 0.0;
+        for (int b2 = a; b2 < 4; ++b2) x += r.T[tri(a, b2)] * beta[b2];
+        r.gamma[a] = x;
+    }
+    r.has = 1;
+}
+
+__global__ void lsm_finish(const LsmDev* __restrict__ cs, int n_contracts,
+                           const Welford* __restrict__ final_part, double* __restrict__ out) {
+    const int ci = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (ci >= n_contracts) return;
+    const LsmDev c = cs[ci];
+    Welford w{0ull, 0.0, 0.0};
+    for (uint32_t ch = lane; ch < c.n_chunks; ch += 32) w = welford_merge(w, final_part[c.chunk_begin + ch]);
+    w = welford_warp_reduce(w);
+    if (lane != 0) return;
+    const double var = w.count < 2 ? 0.0 : w.m2 / static_cast<double>(w.count - 1);
+    const double se = w.count == 0 ? 0.0 : sqrt(var / static_cast<double>(w.count));
+    // inception decision (src/pricers/lsm.cpp:141-148)
+    const bool ex0 = c.inception > w.mean;
+    out[6 * ci + 0] = ex0 ? c.inception : w.mean;
+    out[6 * ci + 1] = ex0 ? 0.0 : se;
+    out[6 * ci + 2] = static_cast<double>(w.count);
+    out[6 * ci + 3] = ex0 ? 1.0 : 0.0;
+    out[6 * ci + 4] = w.mean;  // path average before the inception test
+    out[6 * ci + 5] = se;
+}
+
+}  // namespace
+
+cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
+                               const uint32_t* chunk_contract, uint32_t total_chunks, void* s_store,
+                               cudaStream_t stream) {
+    (void)n_contracts;
+    cudaGetLastError();
+    if (total_chunks == 0) return cudaSuccess;
+    if (precision == 0)
+        lsm_forward<0><<<total_chunks, kLsmThreads, 0, stream>>>(c, chunk_contract, total_chunks, s_store);
+    else
+        lsm_forward<1><<<total_chunks, kLsmThreads, 0, stream>>>(c, chunk_contract, total_chunks, s_store);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lsm_iteration(int precision, int k, bool frozen, const LsmDev* c,
+                                 int n_contracts, const uint32_t* chunk_contract,
+                                 uint32_t total_chunks, const void* s_store, double* cf,
+                                 LsmReg* reg, LsmPartial* part_a, LsmPartial* part_b,
+                                 Welford* final_part, cudaStream_t stream) {
+    cudaGetLastError();
+    if (total_chunks == 0) return cudaSuccess;
+    const int solve_blocks = (n_contracts * 32 + 127) / 128;
+    if (precision == 0)
+        lsm_exercise<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, frozen ? 1 : 0, c, chunk_contract,
+                                                                  total_chunks, s_store, cf, reg,
+                                                                  part_a, final_part);
+    else
+        lsm_exercise<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, frozen ? 1 : 0, c, chunk_contract,
+                                                                  total_chunks, s_store, cf, reg,
+                                                                  part_a, final_part);
+    if (!frozen) {
+        lsm_solve_a<<<solve_blocks, 128, 0, stream>>>(k, c, n_contracts, part_a, reg);
+        if (precision == 0)
+            lsm_gram_b<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks,
+                                                                    s_store, cf, reg, part_b);
+        else
+            lsm_gram_b<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks,
+                                                                    s_store, cf, reg, part_b);
+        lsm_solve_b<<<solve_blocks, 128, 0, stream>>>(k, c, n_contracts, part_b, reg);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lsm_finish(const LsmDev* c, int n_contracts, const Welford* final_part,
+                              double* out, cudaStream_t stream) {
+    cudaGetLastError();
+    lsm_finish<<<(n_contracts * 32 + 127) / 128, 128, 0, stream>>>(c, n_contracts, final_part, out);
+    return cudaGetLastError();
+}
+
+}  // namespace mcdg

@@ -1,0 +1,59 @@
+// lsm.hpp -- batched Longstaff-Schwartz: layouts shared by host and kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "engine.hpp"
+
+namespace mcdg {
+
+constexpr int kLsmChunk = 1024;      // paths per chunk (fixed reduction unit)
+constexpr int kLsmThreads = 256;     // 4 paths per thread per chunk
+constexpr int kLsmBasis = 4;         // weighted Laguerre, degree 3 (src/pricers/lsm.cpp:16-25)
+
+// One American contract.  Paths are stored date-major: S[d-1][i] for dates
+// d = 1..n at s_offset + (d-1)*path_count + i (elements of the path
+// precision); cashflows are FP64 at cf_offset + i.
+struct LsmDev {
+    double spot, strike;
+    double disc;          // exp(-r dt) (src/pricers/lsm.cpp:67)
+    double drift;         // (r - q - vol^2/2) dt  (src/models/gbm.cpp:8-9)
+    double vs;            // vol sqrt(dt)          (src/models/gbm.cpp:10)
+    double inception;     // intrinsic at t = 0    (src/pricers/lsm.cpp:141)
+    uint64_t seed, path_count;
+    uint64_t s_offset, cf_offset;
+    uint32_t chunk_begin, n_chunks;
+    uint32_t reg_offset;  // row of date 0 in the per-date regression table
+    int32_t n_steps, type;
+};
+
+// Regression state of one (contract, date): T = R1^{-1} (upper triangular,
+// packed row-major: (0,0) (0,1) (0,2) (0,3) (1,1) (1,2) (1,3) (2,2) (2,3) (3,3)),
+// the Laguerre coefficients gamma, and flags.
+struct LsmReg {
+    double T[10];
+    double gamma[4];
+    int32_t has;          // coefficients valid at this date (>= 4 ITM paths)
+    int32_t degenerate;   // Cholesky of the first pass failed; solved without preconditioning
+};
+
+// Per-chunk partial sums.  Pass A: count + 10 Gram entries.  Pass B: count +
+// 10 preconditioned Gram entries + 4 right-hand side entries.  Final: Welford.
+struct LsmPartial {
+    double v[16];
+};
+
+cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
+                               const uint32_t* chunk_contract, uint32_t total_chunks, void* s_store,
+                               cudaStream_t stream);
+cudaError_t launch_lsm_iteration(int precision, int k, bool frozen, const LsmDev* c,
+                                 int n_contracts, const uint32_t* chunk_contract,
+                                 uint32_t total_chunks, const void* s_store, double* cf,
+                                 LsmReg* reg, LsmPartial* part_a, LsmPartial* part_b,
+                                 Welford* final_part, cudaStream_t stream);
+cudaError_t launch_lsm_finish(const LsmDev* c, int n_contracts, const Welford* final_part,
+                              double* out /* n x 6: price, se, count, inception, mean, se */,
+                              cudaStream_t stream);
+
+}  // namespace mcdg

@@ -42,6 +42,39 @@ class McResult(C.Structure):
         return f"McResult(price={self.price!r}, standard_error={self.standard_error!r}, path_count={self.path_count})"
 
 
+class HestonParams(C.Structure):
+    """mcd_heston_params (= mcd::models::HestonParams, include/mcd/models/heston.hpp:8-18)."""
+    _fields_ = [(n, dbl) for n in ("spot", "rate", "carry_yield", "v0", "kappa", "theta", "xi",
+                                   "rho", "time")]
+
+
+class LsmResult(C.Structure):
+    """mcd_lsm_result (LsmResult without the policy vectors, plus the inception flag)."""
+    _fields_ = [("price", dbl), ("standard_error", dbl), ("path_count", u64),
+                ("exercise_at_inception", C.c_int32), ("reserved", C.c_int32)]
+
+
+LSM_CONTRACT_DTYPE = np.dtype([(n, "<f8") for n in ("spot", "strike", "rate", "carry_yield", "vol",
+                                                   "time")] +
+                              [("type", "<i4"), ("monitoring_points", "<i4"), ("path_count", "<u8"),
+                               ("seed", "<u8")])
+LSM_RESULT_DTYPE = np.dtype([("price", "<f8"), ("standard_error", "<f8"), ("path_count", "<u8"),
+                             ("exercise_at_inception", "<i4"), ("reserved", "<i4")])
+LSM_QR, LSM_MLP = 0, 1
+
+
+def _regression(r) -> int:
+    if r in (0, "qr", "QR", "laguerre"):
+        return LSM_QR
+    if r in (1, "mlp", "MLP", "learned"):
+        return LSM_MLP
+    raise ValueError(f"regression must be 'qr' or 'mlp', got {r!r}")
+
+
+HESTON_DTYPE = np.dtype([(n, "<f8") for n in ("spot", "rate", "carry_yield", "v0", "kappa",
+                                              "theta", "xi", "rho", "time")])
+
+
 class McOptions(C.Structure):
     _fields_ = [("antithetic", u8), ("control_variate", u8), ("brownian_bridge", u8),
                 ("reserved", u8), ("num_threads", u32)]
@@ -111,6 +144,11 @@ def lib():
     sig("mcd_set_launch_shape", vp, i32, i32, i32)
     sig("mcd_get_launch_shape", vp, i32, P(i32), P(i32))
     sig("mcd_autotune", vp, vp, C.c_size_t, i32, P(i32), P(i32), P(dbl))
+    sig("mcd_heston_qe_european", vp, P(HestonParams), dbl, i32, i32, u64, u64, i32, P(McResult))
+    sig("mcd_heston_qe_batch", vp, vp, C.c_size_t, P(dbl), C.c_size_t, i32, i32, u64, u64, i32, vp)
+    sig("mcd_lsm_american", vp, *D6, i32, i32, u64, u64, i32, i32, P(LsmResult), P(dbl), P(u8))
+    sig("mcd_lsm_reprice_frozen", vp, *D6, i32, i32, u64, u64, P(dbl), P(u8), i32, i32, P(dbl))
+    sig("mcd_lsm_batch", vp, vp, C.c_size_t, i32, i32, vp)
     sig("mcd_philox", vp, P(u32), P(u32), C.c_size_t, P(u32))
     sig("mcd_draws", vp, u64, u64, u64, u32, u32, i32, i32, P(dbl))
     sig("mcd_kernel_timing", vp, i32, P(dbl), P(u64))
@@ -206,6 +244,66 @@ class Engine:
                                                  time, type, style, monitoring_points, path_count,
                                                  seed, C.byref(o), _prec(precision),
                                                  C.byref(out)))
+        return out
+
+    # -- Heston QE (src/pricers/heston.cpp:120-156) -----------------------------------------
+    def heston_qe_european(self, params, strike, type, monitoring_points, path_count, seed,
+                           precision="fp64") -> McResult:
+        p = params if isinstance(params, HestonParams) else HestonParams(*params)
+        out = McResult()
+        self._check(self._lib.mcd_heston_qe_european(self.handle, C.byref(p), strike, type,
+                                                     monitoring_points, path_count, seed,
+                                                     _prec(precision), C.byref(out)))
+        return out
+
+    def heston_qe_batch(self, sets, strikes, type, monitoring_points, path_count, seed,
+                        precision="fp32") -> np.ndarray:
+        """sets: array of HESTON_DTYPE records (or n x 9 floats); returns n_sets x n_strikes."""
+        sets = np.ascontiguousarray(sets, dtype=np.float64).reshape(-1, 9) \
+            if not (isinstance(sets, np.ndarray) and sets.dtype == HESTON_DTYPE) \
+            else np.ascontiguousarray(sets)
+        strikes = np.ascontiguousarray(strikes, dtype=np.float64)
+        out = np.zeros((len(sets), len(strikes)), dtype=RESULT_DTYPE)
+        self._check(self._lib.mcd_heston_qe_batch(self.handle, sets.ctypes.data, len(sets),
+                                                  strikes.ctypes.data_as(P(dbl)), len(strikes),
+                                                  type, monitoring_points, path_count, seed,
+                                                  _prec(precision), out.ctypes.data))
+        return out
+
+    # -- Longstaff-Schwartz (src/pricers/lsm.cpp:62-213) -------------------------------------
+    def monte_carlo_lsm_american(self, spot, strike, rate, carry_yield, vol, time, type,
+                                 monitoring_points, path_count, seed, precision="fp64",
+                                 regression="qr", policy=False):
+        """Returns an LsmResult, or (LsmResult, coefficients[(n+1), 4], has[n+1]) with policy=True."""
+        out = LsmResult()
+        n1 = monitoring_points + 1
+        co = np.zeros((n1, 4), dtype=np.float64) if policy else None
+        ha = np.zeros(n1, dtype=np.uint8) if policy else None
+        self._check(self._lib.mcd_lsm_american(
+            self.handle, spot, strike, rate, carry_yield, vol, time, type, monitoring_points,
+            path_count, seed, _prec(precision), _regression(regression), C.byref(out),
+            co.ctypes.data_as(P(dbl)) if policy else None,
+            ha.ctypes.data_as(P(u8)) if policy else None))
+        return (out, co, ha) if policy else out
+
+    def reprice_against_frozen_policy(self, spot, strike, rate, carry_yield, vol, time, type,
+                                      monitoring_points, path_count, seed, coefficients, has,
+                                      exercise_at_inception=False, precision="fp64") -> float:
+        co = np.ascontiguousarray(coefficients, dtype=np.float64)
+        ha = np.ascontiguousarray(has, dtype=np.uint8)
+        price = dbl()
+        self._check(self._lib.mcd_lsm_reprice_frozen(
+            self.handle, spot, strike, rate, carry_yield, vol, time, type, monitoring_points,
+            path_count, seed, co.ctypes.data_as(P(dbl)), ha.ctypes.data_as(P(u8)),
+            int(bool(exercise_at_inception)), _prec(precision), C.byref(price)))
+        return price.value
+
+    def lsm_batch(self, contracts, precision="fp32", regression="qr") -> np.ndarray:
+        contracts = np.ascontiguousarray(contracts, dtype=LSM_CONTRACT_DTYPE)
+        out = np.zeros(len(contracts), dtype=LSM_RESULT_DTYPE)
+        self._check(self._lib.mcd_lsm_batch(self.handle, contracts.ctypes.data, len(contracts),
+                                            _prec(precision), _regression(regression),
+                                            out.ctypes.data))
         return out
 
     # -- batch -----------------------------------------------------------------------------

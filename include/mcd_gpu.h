@@ -201,6 +201,73 @@ int mcd_get_launch_shape(mcd_ctx* ctx, int precision, int* variant, int* ctas_pe
 int mcd_autotune(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, int precision,
                  int* variant, int* ctas_per_sm, double* best_ms);
 
+/* ---- Heston QE ------------------------------------------------------------ */
+/* mcd::models::HestonParams (include/mcd/models/heston.hpp:8-18). */
+typedef struct {
+    double spot, rate, carry_yield, v0, kappa, theta, xi, rho, time;
+} mcd_heston_params;
+
+/* replaces mcd::pricers::heston_qe_european (src/pricers/heston.cpp:120-156):
+ * Andersen QE variance step (psi_c = 1.5) and the K0..K4 log-spot update;
+ * stream-0 normal for the spot and stream-1 uniform for the variance per
+ * (path, step). */
+int mcd_heston_qe_european(mcd_ctx* ctx, const mcd_heston_params* params, double strike, int type,
+                           int monitoring_points, uint64_t path_count, uint64_t seed,
+                           int precision, mcd_mc_result* out);
+/* Many parameter sets x many strikes in one launch.  Equivalent to calling
+ * heston_qe_european (src/pricers/heston.cpp:120-156) once per (set, strike)
+ * with the same seed, path count and steps: each set's paths are simulated
+ * once and paid out against every strike.  results: n_sets x n_strikes,
+ * row-major.  1 <= n_strikes <= 256. */
+int mcd_heston_qe_batch(mcd_ctx* ctx, const mcd_heston_params* sets, size_t n_sets,
+                        const double* strikes, size_t n_strikes, int type, int monitoring_points,
+                        uint64_t path_count, uint64_t seed, int precision, mcd_mc_result* results);
+
+/* ---- Longstaff-Schwartz American options ---------------------------------- */
+typedef enum { MCD_LSM_QR = 0, MCD_LSM_MLP = 1 } mcd_lsm_regression;
+
+/* mcd::pricers::LsmResult (include/mcd/pricers/lsm.hpp:26-30) without the
+ * policy vectors (returned separately), plus LsmPolicy::exercise_at_inception. */
+typedef struct {
+    double price;
+    double standard_error;
+    uint64_t path_count;
+    int32_t exercise_at_inception;
+    int32_t reserved;
+} mcd_lsm_result;
+
+/* One contract of an LSM batch: monte_carlo_lsm_american's argument list. */
+typedef struct {
+    double spot, strike, rate, carry_yield, vol, time;
+    int32_t type;
+    int32_t monitoring_points;
+    uint64_t path_count;
+    uint64_t seed;
+} mcd_lsm_contract;
+
+/* replaces mcd::pricers::monte_carlo_lsm_american (src/pricers/lsm.cpp:62-149):
+ * weighted Laguerre basis of degree 3 on S/K, in-the-money regression (skipped
+ * below 4 paths), exercise where intrinsic > continuation, inception check.
+ * The regression is solved by two FP64 Gram passes (Cholesky-QR2) and a 4x4
+ * Householder solve.  coefficients ((monitoring_points+1) x 4) and
+ * has_coefficients (monitoring_points+1) receive the policy
+ * (LsmPolicy::coefficients_by_date, lsm.hpp:16-24); either may be NULL.
+ * regression selects MCD_LSM_QR or the learned MCD_LSM_MLP. */
+int mcd_lsm_american(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                     double vol, double time, int type, int monitoring_points,
+                     uint64_t path_count, uint64_t seed, int precision, int regression,
+                     mcd_lsm_result* out, double* coefficients, uint8_t* has_coefficients);
+/* replaces mcd::pricers::reprice_against_frozen_policy (src/pricers/lsm.cpp:151-213). */
+int mcd_lsm_reprice_frozen(mcd_ctx* ctx, double spot, double strike, double rate,
+                           double carry_yield, double vol, double time, int type,
+                           int monitoring_points, uint64_t path_count, uint64_t seed,
+                           const double* coefficients, const uint8_t* has_coefficients,
+                           int exercise_at_inception, int precision, double* price);
+/* Many American contracts (uneven date counts allowed) in one graph launch:
+ * all paths stay resident and the contracts step back in lockstep. */
+int mcd_lsm_batch(mcd_ctx* ctx, const mcd_lsm_contract* contracts, size_t n, int precision,
+                  int regression, mcd_lsm_result* results);
+
 /* ---- draws (parity and diagnostics) ------------------------------------- */
 /* Philox4x32-10 of n (counter, key) pairs; replaces mcd::philox4x32_10
  * (src/core/rng.cpp:41-47).  counters: n x 4, keys: n x 2, out: n x 4. */
