@@ -92,7 +92,16 @@ struct Ctx {
 
     // State owned by the other modules (Heston, LSM, QMC, Greeks); freed by
     // release_extensions().
-    DeviceBuffer ext[16];
+    DeviceBuffer ext[24];
+
+    // Training schedule of the learned LSM regression (mcd_lsm_set_mlp_config).
+    int mlp_steps_first = 1000;
+    int mlp_steps = 200;
+    float mlp_lr_first = 3e-3f;
+    float mlp_lr = 1e-3f;
+    // Networks of the last learned-LSM run (for mcd_lsm_mlp_policy).
+    std::vector<uint32_t> mlp_reg_offset;
+    std::vector<int32_t> mlp_steps_of;
 
     int fail(int code, const std::string& msg);
     int cuda_fail(cudaError_t e, const char* where);

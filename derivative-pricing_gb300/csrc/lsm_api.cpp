@@ -8,8 +8,9 @@
 #include <vector>
 
 #include "context.hpp"
+#include "mlp_layout.hpp"
 #include "lsm.hpp"
-#include "lsm_mlp.hpp"
+#include "lsm_mlp_dev.hpp"
 #include "mcd_gpu.h"
 
 using namespace mcdg;
@@ -18,7 +19,7 @@ namespace {
 
 // Extension slots of Ctx::ext used by this module (Heston uses 0..3).
 enum { kDev = 4, kChunkMap = 5, kStore = 6, kCf = 7, kReg = 8, kPartA = 9, kPartB = 10,
-       kFinal = 11, kOut = 12 };
+       kFinal = 11, kOut = 12, kNets = 13, kSnaps = 14, kSnapOk = 15, kAdamT = 16, kErr = 17 };
 
 struct LsmPlan {
     std::vector<LsmDev> dev;
@@ -74,8 +75,12 @@ int plan_lsm(Ctx& ctx, const mcd_lsm_contract* cs, size_t n, LsmPlan& p) {
     return MCD_OK;
 }
 
+// Runs a planned batch.  mlp = false: Laguerre QR regression (frozen: replay
+// frozen_reg).  mlp = true: learned regression (frozen: replay the networks in
+// frozen_nets, one kParamStride block per (contract, date) row).
 int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
-                   const std::vector<LsmReg>* frozen_reg, std::vector<double>& out) {
+                   const std::vector<LsmReg>* frozen_reg, std::vector<double>& out, bool mlp = false,
+                   const std::vector<float>* frozen_nets = nullptr, const std::vector<int>* frozen_ok = nullptr) {
     const size_t n = p.dev.size();
     const size_t elem = precision == 0 ? sizeof(double) : sizeof(float);
     int rc = ctx.reserve(ctx.ext[kDev], sizeof(LsmDev) * n, "lsm contracts");
@@ -87,6 +92,17 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
     if (!rc) rc = ctx.reserve(ctx.ext[kPartB], sizeof(LsmPartial) * std::max<size_t>(p.total_chunks, 1), "lsm partials");
     if (!rc) rc = ctx.reserve(ctx.ext[kFinal], sizeof(Welford) * std::max<size_t>(p.total_chunks, 1), "lsm final partials");
     if (!rc) rc = ctx.reserve(ctx.ext[kOut], sizeof(double) * 6 * n, "lsm results");
+    if (!rc && mlp) {
+        rc = ctx.reserve(ctx.ext[kNets], sizeof(float) * 3 * mlp::kParamStride * n, "mlp networks");
+        if (!rc) rc = ctx.reserve(ctx.ext[kSnaps], sizeof(float) * mlp::kParamStride * p.reg_rows, "mlp snapshots");
+        if (!rc) rc = ctx.reserve(ctx.ext[kSnapOk], sizeof(int) * p.reg_rows, "mlp snapshot flags");
+        if (!rc) rc = ctx.reserve(ctx.ext[kAdamT], sizeof(int) * n, "mlp adam steps");
+        if (!rc) rc = ctx.reserve(ctx.ext[kErr], 256, "mlp error word");
+        if (!rc) {
+            cudaError_t pe = mlp_prepare();
+            if (pe != cudaSuccess) rc = ctx.cuda_fail(pe, "mlp shared memory opt-in");
+        }
+    }
     if (rc) return rc;
     cudaError_t e = cudaMemcpyAsync(ctx.ext[kDev].ptr, p.dev.data(), sizeof(LsmDev) * n, cudaMemcpyHostToDevice, ctx.stream);
     if (e == cudaSuccess && p.total_chunks)
@@ -99,7 +115,22 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
         else
             e = cudaMemsetAsync(ctx.ext[kReg].ptr, 0, sizeof(LsmReg) * p.reg_rows, ctx.stream);
     }
+    if (e == cudaSuccess && mlp) {
+        e = cudaMemsetAsync(ctx.ext[kErr].ptr, 0, 256, ctx.stream);
+        if (e == cudaSuccess) {
+            if (frozen_nets && frozen_ok) {
+                e = cudaMemcpyAsync(ctx.ext[kSnaps].ptr, frozen_nets->data(), sizeof(float) * frozen_nets->size(),
+                                    cudaMemcpyHostToDevice, ctx.stream);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(ctx.ext[kSnapOk].ptr, frozen_ok->data(), sizeof(int) * frozen_ok->size(),
+                                        cudaMemcpyHostToDevice, ctx.stream);
+            } else {
+                e = cudaMemsetAsync(ctx.ext[kSnapOk].ptr, 0, sizeof(int) * p.reg_rows, ctx.stream);
+            }
+        }
+    }
     if (e != cudaSuccess) return ctx.cuda_fail(e, "lsm upload");
+    const MlpConfig cfg{ctx.mlp_steps_first, ctx.mlp_steps, ctx.mlp_lr_first, ctx.mlp_lr};
 
     // Capture forward pass + every backward iteration + finish into one graph.
     cudaGetLastError();
@@ -110,13 +141,24 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
     const uint32_t* d_map = static_cast<const uint32_t*>(ctx.ext[kChunkMap].ptr);
     cudaError_t le = launch_lsm_forward(precision, d_dev, static_cast<int>(n), d_map, p.total_chunks,
                                         ctx.ext[kStore].ptr, ctx.stream);
-    for (int k = 0; k < p.max_steps && le == cudaSuccess; ++k)
-        le = launch_lsm_iteration(precision, k, frozen, d_dev, static_cast<int>(n), d_map, p.total_chunks,
-                                  ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
-                                  static_cast<LsmReg*>(ctx.ext[kReg].ptr),
-                                  static_cast<LsmPartial*>(ctx.ext[kPartA].ptr),
-                                  static_cast<LsmPartial*>(ctx.ext[kPartB].ptr),
-                                  static_cast<Welford*>(ctx.ext[kFinal].ptr), ctx.stream);
+    for (int k = 0; k < p.max_steps && le == cudaSuccess; ++k) {
+        if (mlp)
+            le = launch_lsm_mlp_iteration(precision, k, !frozen, d_dev, static_cast<int>(n), d_map, p.total_chunks,
+                                          ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
+                                          static_cast<float*>(ctx.ext[kNets].ptr),
+                                          static_cast<float*>(ctx.ext[kSnaps].ptr),
+                                          static_cast<int*>(ctx.ext[kSnapOk].ptr),
+                                          static_cast<int*>(ctx.ext[kAdamT].ptr), cfg,
+                                          static_cast<Welford*>(ctx.ext[kFinal].ptr),
+                                          static_cast<uint32_t*>(ctx.ext[kErr].ptr), ctx.stream);
+        else
+            le = launch_lsm_iteration(precision, k, frozen, d_dev, static_cast<int>(n), d_map, p.total_chunks,
+                                      ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
+                                      static_cast<LsmReg*>(ctx.ext[kReg].ptr),
+                                      static_cast<LsmPartial*>(ctx.ext[kPartA].ptr),
+                                      static_cast<LsmPartial*>(ctx.ext[kPartB].ptr),
+                                      static_cast<Welford*>(ctx.ext[kFinal].ptr), ctx.stream);
+    }
     if (le == cudaSuccess)
         le = launch_lsm_finish(d_dev, static_cast<int>(n), static_cast<const Welford*>(ctx.ext[kFinal].ptr),
                                static_cast<double*>(ctx.ext[kOut].ptr), ctx.stream);
@@ -146,30 +188,68 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
     }
     cudaGraphExecDestroy(exec);
     ctx.collect_timing(false);
+    if (!rc && mlp) {
+        uint32_t werr = 0;
+        e = cudaMemcpy(&werr, ctx.ext[kErr].ptr, sizeof werr, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return ctx.cuda_fail(e, "mlp error word");
+        if (werr != 0)
+            return ctx.fail(MCD_ERR_TIMEOUT, "tensor-core wait gave up (code " + std::to_string(werr) + ")");
+    }
     return rc;
 }
 
 int lsm_batch(Ctx& ctx, const mcd_lsm_contract* cs, size_t n, int precision, int regression,
               mcd_lsm_result* results, std::vector<LsmReg>* reg_out) {
     if (precision != 0 && precision != 1) return ctx.fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
-    if (regression == MCD_LSM_MLP) return lsm_mlp_batch(ctx, cs, n, precision, results);
-    if (regression != MCD_LSM_QR) return ctx.fail(MCD_ERR_INVALID_ARGUMENT, "regression must be MCD_LSM_QR or MCD_LSM_MLP");
+    if (regression != MCD_LSM_QR && regression != MCD_LSM_MLP)
+        return ctx.fail(MCD_ERR_INVALID_ARGUMENT, "regression must be MCD_LSM_QR or MCD_LSM_MLP");
     if (n == 0) return MCD_OK;
     if (!cs || !results) return ctx.fail(MCD_ERR_INVALID_ARGUMENT, "null array");
     LsmPlan p;
     int rc = plan_lsm(ctx, cs, n, p);
     if (rc) return rc;
     std::vector<double> out;
-    rc = upload_and_run(ctx, p, precision, false, nullptr, out);
+    const bool mlp = regression == MCD_LSM_MLP;
+    rc = upload_and_run(ctx, p, precision, false, nullptr, out, mlp);
     if (rc) return rc;
+    std::vector<int> ok;
+    if (mlp) {
+        ok.resize(p.reg_rows);
+        cudaError_t e = cudaMemcpy(ok.data(), ctx.ext[kSnapOk].ptr, sizeof(int) * p.reg_rows, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return ctx.cuda_fail(e, "mlp snapshot flags");
+        ctx.mlp_reg_offset.resize(n);
+        ctx.mlp_steps_of.resize(n);
+        for (size_t i = 0; i < n; ++i) {
+            ctx.mlp_reg_offset[i] = p.dev[i].reg_offset;
+            ctx.mlp_steps_of[i] = p.dev[i].n_steps;
+        }
+    }
+    std::vector<size_t> fallback;
     for (size_t i = 0; i < n; ++i) {
         results[i].price = out[6 * i];
         results[i].standard_error = out[6 * i + 1];
         results[i].path_count = static_cast<uint64_t>(out[6 * i + 2]);
         results[i].exercise_at_inception = out[6 * i + 3] != 0.0 ? 1 : 0;
         results[i].reserved = 0;
+        if (mlp) {
+            // A date whose training ended with non-finite weights: the network
+            // is not trusted and the contract is priced by the QR regression.
+            const int nd = p.dev[i].n_steps;
+            for (int d = 1; d < nd; ++d)
+                if (ok[p.dev[i].reg_offset + d] != 1) {
+                    fallback.push_back(i);
+                    break;
+                }
+        }
     }
-    if (reg_out) {
+    for (size_t i : fallback) {
+        mcd_lsm_result r{};
+        rc = lsm_batch(ctx, &cs[i], 1, precision, MCD_LSM_QR, &r, nullptr);
+        if (rc) return rc;
+        r.reserved = 1;  // priced by the QR fallback
+        results[i] = r;
+    }
+    if (reg_out && !mlp) {
         reg_out->resize(p.reg_rows);
         cudaError_t e = cudaMemcpy(reg_out->data(), ctx.ext[kReg].ptr, sizeof(LsmReg) * p.reg_rows,
                                    cudaMemcpyDeviceToHost);
@@ -245,6 +325,155 @@ int mcd_lsm_batch(mcd_ctx* handle, const mcd_lsm_contract* contracts, size_t n, 
                   int regression, mcd_lsm_result* results) {
     MCD_CTX_OR_FAIL(handle, ctx);
     return lsm_batch(*ctx, contracts, n, precision, regression, results, nullptr);
+}
+
+int mcd_lsm_set_mlp_config(mcd_ctx* handle, int steps_first, int steps, double lr_first, double lr) {
+    MCD_CTX_OR_FAIL(handle, ctx);
+    if (steps_first < 0 || steps < 0 || steps_first > 1000000 || steps > 1000000 || !(lr_first > 0) || !(lr > 0))
+        return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "steps must be 0..1e6 and learning rates > 0");
+    ctx->mlp_steps_first = steps_first;
+    ctx->mlp_steps = steps;
+    ctx->mlp_lr_first = static_cast<float>(lr_first);
+    ctx->mlp_lr = static_cast<float>(lr);
+    return MCD_OK;
+}
+
+int mcd_lsm_mlp_policy(mcd_ctx* handle, size_t contract, float* weights, uint8_t* has) {
+    MCD_CTX_OR_FAIL(handle, ctx);
+    if (contract >= ctx->mlp_reg_offset.size()) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "no such contract in the last learned run");
+    const uint32_t off = ctx->mlp_reg_offset[contract];
+    const int nd = ctx->mlp_steps_of[contract];
+    std::vector<float> buf(static_cast<size_t>(nd + 1) * mlp::kParamStride);
+    std::vector<int> ok(nd + 1);
+    cudaError_t e = cudaMemcpy(buf.data(), static_cast<float*>(ctx->ext[kSnaps].ptr) + static_cast<size_t>(off) * mlp::kParamStride,
+                               sizeof(float) * buf.size(), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(ok.data(), static_cast<int*>(ctx->ext[kSnapOk].ptr) + off, sizeof(int) * ok.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "mlp policy copy");
+    for (int d = 0; d <= nd; ++d) {
+        if (has) has[d] = ok[d] == 1 ? 1 : 0;
+        if (weights)
+            for (int q = 0; q < mlp::kParams; ++q)
+                weights[static_cast<size_t>(d) * mlp::kParams + q] = ok[d] == 1 ? buf[static_cast<size_t>(d) * mlp::kParamStride + q] : 0.0f;
+    }
+    return MCD_OK;
+}
+
+int mcd_lsm_reprice_mlp(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield,
+                        double vol, double time, int type, int monitoring_points, uint64_t path_count,
+                        uint64_t seed, const float* weights, const uint8_t* has, int precision,
+                        mcd_lsm_result* out) {
+    MCD_CTX_OR_FAIL(handle, ctx);
+    if (!weights || !has || !out) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
+    if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
+    const mcd_lsm_contract c{spot, strike, rate, carry_yield, vol, time, type, monitoring_points, path_count, seed};
+    LsmPlan p;
+    int rc = plan_lsm(*ctx, &c, 1, p);
+    if (rc) return rc;
+    std::vector<float> nets(p.reg_rows * mlp::kParamStride, 0.0f);
+    std::vector<int> ok(p.reg_rows, 0);
+    for (int d = 1; d < monitoring_points; ++d) {
+        if (!has[d]) continue;
+        ok[d] = 1;
+        for (int q = 0; q < mlp::kParams; ++q)
+            nets[static_cast<size_t>(d) * mlp::kParamStride + q] = weights[static_cast<size_t>(d) * mlp::kParams + q];
+    }
+    std::vector<double> res;
+    rc = upload_and_run(*ctx, p, precision, true, nullptr, res, true, &nets, &ok);
+    if (rc) return rc;
+    out->price = res[0];
+    out->standard_error = res[1];
+    out->path_count = static_cast<uint64_t>(res[2]);
+    out->exercise_at_inception = res[3] != 0.0 ? 1 : 0;
+    out->reserved = 0;
+    return MCD_OK;
+}
+
+int mcd_umma_selftest(mcd_ctx* handle, const float* a, const float* b, float* d) {
+    MCD_CTX_OR_FAIL(handle, ctx);
+    if (!a || !b || !d) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
+    int rc = ctx->reserve(ctx->ext[kErr], 256, "error word");
+    if (!rc) rc = ctx->reserve(ctx->d_scratch2, sizeof(float) * (128 * 64 * 2 + 64 * 64), "selftest buffers");
+    if (rc) return rc;
+    float* da = static_cast<float*>(ctx->d_scratch2.ptr);
+    float* db = da + 128 * 64;
+    float* dd = db + 64 * 64;
+    uint32_t werr = 0;
+    cudaError_t e = cudaMemcpyAsync(da, a, sizeof(float) * 128 * 64, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(db, b, sizeof(float) * 64 * 64, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->ext[kErr].ptr, 0, 256, ctx->stream);
+    if (e == cudaSuccess) e = launch_umma_selftest(da, db, dd, static_cast<uint32_t*>(ctx->ext[kErr].ptr), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, dd, sizeof(float) * 128 * 64, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&werr, ctx->ext[kErr].ptr, sizeof werr, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "umma selftest");
+    if (werr) return ctx->fail(MCD_ERR_TIMEOUT, "tensor-core wait gave up");
+    return MCD_OK;
+}
+
+int mcd_mlp_gradients(mcd_ctx* handle, const float* params, const float* x0, const float* x1, const float* y,
+                      const float* w, int n, float* grad, float* loss) {
+    MCD_CTX_OR_FAIL(handle, ctx);
+    if (n < 1 || n > 128) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "n must be 1..128");
+    if (!params || !x0 || !x1 || !y || !w || !grad || !loss) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
+    int rc = ctx->reserve(ctx->ext[kErr], 256, "error word");
+    const size_t floats = mlp::kParamStride * 2 + 128 * 4 + 4;
+    if (!rc) rc = ctx->reserve(ctx->d_scratch2, sizeof(float) * floats, "gradient buffers");
+    if (rc) return rc;
+    cudaError_t e = mlp_prepare();
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "mlp shared memory opt-in");
+    float* dp = static_cast<float*>(ctx->d_scratch2.ptr);
+    float* dg = dp + mlp::kParamStride;
+    float* dx0 = dg + mlp::kParamStride;
+    float* dx1 = dx0 + 128;
+    float* dy = dx1 + 128;
+    float* dw = dy + 128;
+    float* dl = dw + 128;
+    uint32_t werr = 0;
+    e = cudaMemcpyAsync(dp, params, sizeof(float) * mlp::kParams, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx0, x0, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx1, x1, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dw, w, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->ext[kErr].ptr, 0, 256, ctx->stream);
+    if (e == cudaSuccess)
+        e = launch_mlp_grad(dp, dx0, dx1, dy, dw, n, dg, dl, static_cast<uint32_t*>(ctx->ext[kErr].ptr), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(grad, dg, sizeof(float) * mlp::kParams, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(loss, dl, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&werr, ctx->ext[kErr].ptr, sizeof werr, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "mlp gradients");
+    if (werr) return ctx->fail(MCD_ERR_TIMEOUT, "tensor-core wait gave up");
+    return MCD_OK;
+}
+
+int mcd_mlp_forward(mcd_ctx* handle, const float* params, const float* x0, const float* x1, size_t n, float* out) {
+    MCD_CTX_OR_FAIL(handle, ctx);
+    if (n == 0) return MCD_OK;
+    if (n > (1u << 26)) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "at most 2^26 inputs per call");
+    if (!params || !x0 || !x1 || !out) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
+    int rc = ctx->reserve(ctx->ext[kErr], 256, "error word");
+    if (!rc) rc = ctx->reserve(ctx->d_scratch2, sizeof(float) * (mlp::kParamStride + 3 * n), "forward buffers");
+    if (rc) return rc;
+    cudaError_t e = mlp_prepare();
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "mlp shared memory opt-in");
+    float* dp = static_cast<float*>(ctx->d_scratch2.ptr);
+    float* dx0 = dp + mlp::kParamStride;
+    float* dx1 = dx0 + n;
+    float* dout = dx1 + n;
+    uint32_t werr = 0;
+    e = cudaMemcpyAsync(dp, params, sizeof(float) * mlp::kParams, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx0, x0, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx1, x1, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->ext[kErr].ptr, 0, 256, ctx->stream);
+    if (e == cudaSuccess)
+        e = launch_mlp_forward(dp, dx0, dx1, static_cast<int>(n), dout, static_cast<uint32_t*>(ctx->ext[kErr].ptr), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&werr, ctx->ext[kErr].ptr, sizeof werr, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "mlp forward");
+    if (werr) return ctx->fail(MCD_ERR_TIMEOUT, "tensor-core wait gave up");
+    return MCD_OK;
 }
 
 }  // extern "C"

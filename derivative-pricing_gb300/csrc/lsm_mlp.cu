@@ -1,0 +1,722 @@
+// lsm_mlp.cu -- learned continuation values for Longstaff-Schwartz.
+//
+// In place of the Laguerre least-squares fit of src/pricers/lsm.cpp:88-108, a
+// 2 -> 64 -> 64 -> 1 GELU network (mlp.cuh) is trained at every exercise date
+// on in-the-money paths from the simulator (targets: the discounted cash flows,
+// as in the reference), warm-started from the previous (later) date, and used
+// for the exercise decisions at that date.
+//
+// Kernels (all operands K-major BF16 in shared memory, FP32 accumulators in
+// tensor memory; umma.cuh):
+//   lsm_mlp_train     one CTA per contract: `steps` Adam steps on 128-sample
+//                     tiles.  Per step the 64x64 layer runs three tcgen05 MMA
+//                     groups -- forward Z2 = H1 W2^T (4 x K16), input gradient
+//                     dH1 = dZ2 W2 (4 x K16) and weight gradient
+//                     dW2 = dZ2^T H1 (8 x K16, M padded to 128 with zero rows)
+//                     -- and the CUDA cores do layer 1, layer 3, the GELUs and
+//                     the fixed-order reductions of the small gradients.
+//   lsm_mlp_exercise  one CTA per 1024-path chunk: inference (the forward MMA
+//                     per 128-path tile), exercise, discount, final Welford.
+//   mlp_grad_kernel   one step without update, for gradient checks.
+//   mlp_forward_kernel / umma_selftest_kernel   inference and GEMM checks.
+//
+// Every mbarrier wait is bounded (umma.cuh); on a timeout the kernel records
+// an error code, waits once more (bounded) for its MMAs, frees its tensor
+// memory and returns.
+//
+// nvcc-flags: --fmad=false
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+#include "lsm.hpp"
+#include "lsm_mlp_dev.hpp"
+#include "mlp.cuh"
+#include "umma.cuh"
+
+namespace mcdg {
+
+using namespace mlp;
+
+namespace {
+
+constexpr uint32_t kIdesc = umma::idesc_bf16(128, 64);
+constexpr int kRow = 65;  // scratch row stride in floats (65: bank-conflict free)
+
+struct __align__(1024) TrainSmem {
+    __nv_bfloat16 h1[128 * 64];     // A [sample][in]    K = 64
+    __nv_bfloat16 h1t[64 * 128];    // B [in][sample]    K = 128
+    __nv_bfloat16 dz2[128 * 64];    // A [sample][out]   K = 64
+    __nv_bfloat16 dz2t[128 * 128];  // A [out][sample]   K = 128, rows 64..127 zero
+    __nv_bfloat16 w2[64 * 64];      // B [out][in]       K = 64
+    __nv_bfloat16 w2t[64 * 64];     // B [in][out]       K = 64
+    float scratch[128 * kRow];      // per-sample FP32 rows (padded: conflict-free)
+    float p[kParamStride];          // master parameters
+    float m[kParamStride];          // Adam first moment
+    float v[kParamStride];          // Adam second moment
+    float g[384];                   // reduced gradients: W1 0..127, b1 128..191, b2 192..255, W3 256..319, b3 320
+    float x0[128], x1[128], y[128], w[128], dy[128];
+    uint64_t mbar;
+    uint32_t tmem_base;
+    float loss;
+};
+
+struct __align__(1024) InferSmem {
+    __nv_bfloat16 h1[128 * 64];
+    __nv_bfloat16 w2[64 * 64];
+    float p[kParamStride];
+    uint64_t mbar;
+    uint32_t tmem_base;
+};
+
+__device__ __forceinline__ __nv_bfloat16* at(__nv_bfloat16* base, int r, int k, int kcols) {
+    return reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(base) + umma::kmajor_offset(r, k, kcols));
+}
+
+__device__ __forceinline__ uint64_t desc(const void* p, uint32_t sbo, int kstep) {
+    return umma::smem_desc(umma::smem_u32(p) + static_cast<uint32_t>(kstep) * 256u, 128u, sbo);
+}
+
+// Refreshes the BF16 copies of W2 (row `r` of W2 and column `r` of W2^T).
+__device__ __forceinline__ void refresh_w2_row(TrainSmem& S, int r) {
+    for (int j = 0; j < 64; j += 2) {
+        const __nv_bfloat162 pr = __floats2bfloat162_rn(S.p[kW2 + r * 64 + j], S.p[kW2 + r * 64 + j + 1]);
+        *reinterpret_cast<__nv_bfloat162*>(at(S.w2, r, j, 64)) = pr;
+        *at(S.w2t, j, r, 64) = pr.x;
+        *at(S.w2t, j + 1, r, 64) = pr.y;
+    }
+}
+
+__device__ __forceinline__ float adam(float& p, float& m, float& v, float g, float lr, float c1, float c2) {
+    m = 0.9f * m + 0.1f * g;
+    v = 0.999f * v + 0.001f * g * g;
+    const float mh = m / c1, vh = v / c2;
+    p -= lr * mh / (sqrtf(vh) + 1e-8f);
+    return p;
+}
+
+// One forward/backward pass over the 128-sample tile staged in S.x0/x1/y/w
+// (n_eff = number of samples with weight > 0), then (optionally) an Adam
+// update.  grad_out, when given, receives the full gradient in parameter
+// layout.  Returns false on an MMA timeout.
+__device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff, bool update, float lr,
+                           int t_adam, float* grad_out, uint32_t* err) {
+    const int s = threadIdx.x;
+    const int warp = s >> 5;
+    const float inv_n = 1.0f / static_cast<float>(n_eff > 0 ? n_eff : 1);
+    // ---- layer 1 (CUDA cores) -> H1 (BF16, both layouts)
+    {
+        const float x0 = S.x0[s], x1 = S.x1[s];
+        for (int j = 0; j < 64; j += 2) {
+            float t;
+            const float za = __fmaf_rn(S.p[kW1 + 2 * j], x0, __fmaf_rn(S.p[kW1 + 2 * j + 1], x1, S.p[kB1 + j]));
+            const float zb = __fmaf_rn(S.p[kW1 + 2 * j + 2], x0, __fmaf_rn(S.p[kW1 + 2 * j + 3], x1, S.p[kB1 + j + 1]));
+            const __nv_bfloat162 hp = __floats2bfloat162_rn(gelu(za, t), gelu(zb, t));
+            *reinterpret_cast<__nv_bfloat162*>(at(S.h1, s, j, 64)) = hp;
+            *at(S.h1t, j, s, 128) = hp.x;
+            *at(S.h1t, j + 1, s, 128) = hp.y;
+        }
+    }
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    if (s == 0) {
+        umma::fence_after_sync();
+        for (int kk = 0; kk < 4; ++kk)
+            umma::mma_bf16(tm, desc(S.h1, 1024, kk), desc(S.w2, 1024, kk), kIdesc, kk > 0);
+        umma::mma_commit(&S.mbar);
+    }
+    const bool ok2 = __syncthreads_and(umma::mbar_wait(&S.mbar, phase, err, 2));
+    if (!ok2) return false;
+    phase ^= 1u;
+    umma::fence_after_sync();
+    // ---- layer 2 epilogue, layer 3, loss
+    float yhat = S.p[kB3];
+    for (int c = 0; c < 4; ++c) {
+        float zz[16];
+        umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, c * 16), zz);
+        for (int q = 0; q < 16; ++q) {
+            const int j = c * 16 + q;
+            float t;
+            const float h = gelu(zz[q] + S.p[kB2 + j], t);
+            yhat = __fmaf_rn(S.p[kW3 + j], h, yhat);
+            S.scratch[s * kRow + j] = h;
+        }
+    }
+    const float diff = yhat - S.y[s];
+    const float dy = S.w[s] > 0.0f ? 2.0f * diff * inv_n : 0.0f;
+    S.dy[s] = dy;
+    __syncthreads();
+    if (s < 64) {
+        float acc = 0.0f;
+        for (int q = 0; q < 128; ++q) acc = __fmaf_rn(S.dy[q], S.scratch[q * kRow + s], acc);
+        S.g[256 + s] = acc;  // dW3
+    } else if (s == 64) {
+        float acc = 0.0f;
+        for (int q = 0; q < 128; ++q) acc += S.dy[q];
+        S.g[320] = acc;  // db3
+    }
+    __syncthreads();
+    // ---- back through GELU to dZ2 (BF16, both layouts) and its FP32 rows
+    for (int c = 0; c < 4; ++c) {
+        float zz[16];
+        umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, c * 16), zz);
+        for (int q = 0; q < 16; q += 2) {
+            const int j = c * 16 + q;
+            float ta, tb;
+            const float za = zz[q] + S.p[kB2 + j], zb = zz[q + 1] + S.p[kB2 + j + 1];
+            gelu(za, ta);
+            gelu(zb, tb);
+            const float da = dy * S.p[kW3 + j] * gelu_grad(za, ta);
+            const float db = dy * S.p[kW3 + j + 1] * gelu_grad(zb, tb);
+            S.scratch[s * kRow + j] = da;
+            S.scratch[s * kRow + j + 1] = db;
+            const __nv_bfloat162 dp = __floats2bfloat162_rn(da, db);
+            *reinterpret_cast<__nv_bfloat162*>(at(S.dz2, s, j, 64)) = dp;
+            *at(S.dz2t, j, s, 128) = dp.x;
+            *at(S.dz2t, j + 1, s, 128) = dp.y;
+        }
+    }
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    if (s == 0) {
+        umma::fence_after_sync();
+        for (int kk = 0; kk < 4; ++kk)  // dH1 = dZ2 W2
+            umma::mma_bf16(tm + 64, desc(S.dz2, 1024, kk), desc(S.w2t, 1024, kk), kIdesc, kk > 0);
+        for (int kk = 0; kk < 8; ++kk)  // dW2 = dZ2^T H1 (rows 64..127 of A are zero)
+            umma::mma_bf16(tm + 128, desc(S.dz2t, 2048, kk), desc(S.h1t, 2048, kk), kIdesc, kk > 0);
+        umma::mma_commit(&S.mbar);
+    }
+    if (s < 64) {  // db2 while the tensor core runs
+        float acc = 0.0f;
+        for (int q = 0; q < 128; ++q) acc += S.scratch[q * kRow + s];
+        S.g[192 + s] = acc;
+    }
+    const bool ok3 = __syncthreads_and(umma::mbar_wait(&S.mbar, phase, err, 3));
+    if (!ok3) return false;
+    phase ^= 1u;
+    umma::fence_after_sync();
+    __syncthreads();
+    // ---- dH1 -> dZ1 (through GELU), FP32 rows
+    {
+        const float x0 = S.x0[s], x1 = S.x1[s];
+        for (int c = 0; c < 4; ++c) {
+            float dd[16];
+            umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 64 + c * 16), dd);
+            for (int q = 0; q < 16; ++q) {
+                const int j = c * 16 + q;
+                float t;
+                const float z = __fmaf_rn(S.p[kW1 + 2 * j], x0, __fmaf_rn(S.p[kW1 + 2 * j + 1], x1, S.p[kB1 + j]));
+                gelu(z, t);
+                S.scratch[s * kRow + j] = dd[q] * gelu_grad(z, t);
+            }
+        }
+    }
+    __syncthreads();
+    if (s < 64) {
+        float gb = 0.0f, g0 = 0.0f, g1 = 0.0f;
+        for (int q = 0; q < 128; ++q) {
+            const float d = S.scratch[q * kRow + s];
+            gb += d;
+            g0 = __fmaf_rn(d, S.x0[q], g0);
+            g1 = __fmaf_rn(d, S.x1[q], g1);
+        }
+        S.g[128 + s] = gb;
+        S.g[2 * s] = g0;
+        S.g[2 * s + 1] = g1;
+    }
+    const float c1 = 1.0f - powf(0.9f, static_cast<float>(t_adam));
+    const float c2 = 1.0f - powf(0.999f, static_cast<float>(t_adam));
+    // ---- dW2 rows from tensor memory (lanes 0..63 = output neurons)
+    if (warp < 2) {
+        for (int c = 0; c < 4; ++c) {
+            float dw[16];
+            umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 128 + c * 16), dw);
+            for (int q = 0; q < 16; ++q) {
+                const int idx = kW2 + s * 64 + c * 16 + q;
+                if (grad_out) grad_out[idx] = dw[q];
+                if (update) adam(S.p[idx], S.m[idx], S.v[idx], dw[q], lr, c1, c2);
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    // ---- the small parameters
+    for (int q = s; q < 321; q += 128) {
+        int idx;
+        if (q < 128) idx = kW1 + q;
+        else if (q < 192) idx = kB1 + (q - 128);
+        else if (q < 256) idx = kB2 + (q - 192);
+        else if (q < 320) idx = kW3 + (q - 256);
+        else idx = kB3;
+        if (grad_out) grad_out[idx] = S.g[q];
+        if (update) adam(S.p[idx], S.m[idx], S.v[idx], S.g[q], lr, c1, c2);
+    }
+    __syncthreads();
+    if (update && s < 64) refresh_w2_row(S, s);
+    // loss of the tile (before the update)
+    {
+        const float l = S.w[s] > 0.0f ? diff * diff * inv_n : 0.0f;
+        S.scratch[s] = l;  // scratch rows are free again
+    }
+    __syncthreads();
+    if (s == 0) {
+        float l = 0.0f;
+        for (int q = 0; q < 128; ++q) l += S.scratch[q];
+        S.loss = l;
+    }
+    __syncthreads();
+    return true;
+}
+
+__device__ void train_setup(TrainSmem& S) {
+    const int s = threadIdx.x;
+    if (s == 0) umma::mbar_init(&S.mbar, 1);
+    // dZ2^T rows 64..127 stay zero (M padding of the weight-gradient MMA)
+    for (int i = s; i < 128 * 128 / 2; i += 128) reinterpret_cast<uint32_t*>(S.dz2t)[i] = 0u;
+    if ((s >> 5) == 0) umma::tmem_alloc(&S.tmem_base, 256);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+}
+
+__device__ void train_teardown(TrainSmem& S, uint32_t phase, bool ok, uint32_t* err) {
+    if (!ok) {
+        // bounded second wait for any MMA still in flight, then release TMEM
+        umma::mbar_wait(&S.mbar, phase, err, 4);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) umma::tmem_dealloc(S.tmem_base, 256);
+}
+
+// Deterministic initial weights: He-scaled normals from Philox (stream 7).
+__device__ void init_params(float* p, uint64_t seed) {
+    const PhiloxKeys k = philox_keys(seed ^ 0x6a09e667f3bcc909ull);
+    for (int i = threadIdx.x; i < kParamStride; i += blockDim.x) {
+        float scale = 0.0f;
+        if (i < kB1) scale = 1.0f;                 // W1: fan-in 2
+        else if (i >= kW2 && i < kB2) scale = 0.1767767f;  // W2: sqrt(2/64)
+        else if (i >= kW3 && i < kB3) scale = 0.125f;      // W3
+        float val = 0.0f;
+        if (scale != 0.0f) {
+            const PhiloxPath pp = philox_path(static_cast<uint64_t>(i), 7u, k);
+            val = scale * normal_from_bits_f32(philox_word0(pp, 0u, k));
+        }
+        p[i] = val;
+    }
+}
+
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352dU;
+    x ^= x >> 15;
+    x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+
+template <int PREC>
+__device__ __forceinline__ double path_s(const void* store, uint64_t idx) {
+    if (PREC == 0) return static_cast<const double*>(store)[idx];
+    return static_cast<double>(static_cast<const float*>(store)[idx]);
+}
+
+// ---------------------------------------------------------------------------
+// per-contract trainer for date n - k - 1
+// ---------------------------------------------------------------------------
+template <int PREC>
+__global__ void __launch_bounds__(128, 1)
+    lsm_mlp_train(int k, const LsmDev* __restrict__ cs, int n_contracts, const void* __restrict__ store,
+                  const double* __restrict__ cf, float* __restrict__ nets, float* __restrict__ snaps,
+                  int* __restrict__ snap_ok, int* __restrict__ adam_t, MlpConfig cfg,
+                  uint32_t* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
+    const int ci = blockIdx.x;
+    if (ci >= n_contracts) return;
+    const LsmDev c = cs[ci];
+    const int n = c.n_steps;
+    const int date = n - k - 1;
+    if (date < 1) return;
+    const int s = threadIdx.x;
+    float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
+    if (k == 0) {
+        init_params(S.p, c.seed);
+        for (int i = s; i < kParamStride; i += 128) {
+            S.m[i] = 0.0f;
+            S.v[i] = 0.0f;
+        }
+    } else {
+        for (int i = s; i < kParamStride; i += 128) {
+            S.p[i] = net[i];
+            S.m[i] = net[kParamStride + i];
+            S.v[i] = net[2 * kParamStride + i];
+        }
+    }
+    train_setup(S);
+    if (s < 64) refresh_w2_row(S, s);
+    __syncthreads();
+    const uint32_t tm = S.tmem_base;
+    uint32_t phase = 0;
+    int t = k == 0 ? 0 : adam_t[ci];
+    const int steps = k == 0 ? cfg.steps_first : cfg.steps;
+    const float lr = k == 0 ? cfg.lr_first : cfg.lr;
+    const double inv_k = 1.0 / c.strike;
+    const float x1 = static_cast<float>(n - date) / static_cast<float>(n);
+    bool ok = true;
+    for (int st = 0; st < steps && ok; ++st) {
+        const uint32_t h = mix32(static_cast<uint32_t>(c.seed) * 0x9E3779B1u ^ mix32((static_cast<uint32_t>(date) << 20) ^
+                                                                                     (static_cast<uint32_t>(st) << 7) ^ s));
+        const uint64_t i = static_cast<uint64_t>(h) % c.path_count;
+        const double sv = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(date - 1) * c.path_count + i);
+        const double ex = (c.type == 0 ? 1.0 : -1.0) * (sv - c.strike);
+        const bool itm = ex > 0.0;
+        S.x0[s] = static_cast<float>(4.0 * (sv * inv_k - 1.0));
+        S.x1[s] = x1;
+        // Target: time value (continuation minus exercise value) over K.  The
+        // decision only needs its sign, and it is an order of magnitude
+        // smaller than the continuation value itself, so the network's
+        // relative error costs far fewer wrong decisions.
+        S.y[s] = itm ? static_cast<float>((cf[c.cf_offset + i] - ex) * inv_k) : 0.0f;
+        S.w[s] = itm ? 1.0f : 0.0f;
+        const int n_eff = __syncthreads_count(itm);
+        ++t;
+        ok = train_step(S, tm, phase, n_eff, true, lr, t, nullptr, err);
+    }
+    // persist the network and snapshot it for this date
+    bool finite = true;
+    for (int i = s; i < kParamStride; i += 128) {
+        const float pv = S.p[i];
+        if (!(pv == pv) || fabsf(pv) > 1e30f) finite = false;
+        net[i] = pv;
+        net[kParamStride + i] = S.m[i];
+        net[2 * kParamStride + i] = S.v[i];
+        snaps[(static_cast<size_t>(c.reg_offset) + date) * kParamStride + i] = pv;
+    }
+    const int all_finite = __syncthreads_and(finite);
+    if (s == 0) {
+        adam_t[ci] = t;
+        snap_ok[c.reg_offset + date] = (ok && all_finite) ? 1 : 0;
+    }
+    train_teardown(S, phase, ok, err);
+}
+
+// ---------------------------------------------------------------------------
+// exercise with the network of date e, discount, final Welford
+// ---------------------------------------------------------------------------
+template <int PREC>
+__global__ void __launch_bounds__(128)
+    lsm_mlp_exercise(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
+                     uint32_t total_chunks, const void* __restrict__ store, double* __restrict__ cf,
+                     const float* __restrict__ snaps, const int* __restrict__ snap_ok,
+                     Welford* __restrict__ final_part, uint32_t* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+    __shared__ Welford swf[4];
+    const uint32_t chunk = blockIdx.x;
+    if (chunk >= total_chunks) return;
+    const LsmDev c = cs[chunk_contract[chunk]];
+    const int n = c.n_steps;
+    const int e = n - k;
+    if (e < 1) return;
+    const int s = threadIdx.x;
+    const int warp = s >> 5;
+    const bool init = (k == 0);
+    const bool last = (e == 1);
+    const bool exercise = !init && e <= n - 1 && snap_ok[c.reg_offset + e] == 1;
+    const double inv_k = 1.0 / c.strike;
+    const double phi = c.type == 0 ? 1.0 : -1.0;
+    uint32_t tm = 0, phase = 0;
+    bool ok = true;
+    if (exercise) {
+        const float* net = snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride;
+        for (int i = s; i < kParamStride; i += 128) S.p[i] = net[i];
+        __syncthreads();
+        if (s < 64)
+            for (int j = 0; j < 64; j += 2)
+                *reinterpret_cast<__nv_bfloat162*>(at(S.w2, s, j, 64)) =
+                    __floats2bfloat162_rn(S.p[kW2 + s * 64 + j], S.p[kW2 + s * 64 + j + 1]);
+        if (s == 0) umma::mbar_init(&S.mbar, 1);
+        if (warp == 0) umma::tmem_alloc(&S.tmem_base, 64);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+        tm = S.tmem_base;
+    }
+    const float x1 = static_cast<float>(n - e) / static_cast<float>(n);
+    Welford w{0ull, 0.0, 0.0};
+    const uint32_t local = chunk - c.chunk_begin;
+    for (int tile = 0; tile < kLsmChunk / 128; ++tile) {
+        const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + tile * 128 + s;
+        const bool live = i < c.path_count;
+        double v = 0.0, ex = 0.0;
+        if (live) {
+            if (init) {
+                const double sT = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(n - 1) * c.path_count + i);
+                const double x = phi * (sT - c.strike);
+                v = x > 0.0 ? x : 0.0;
+            } else {
+                v = cf[c.cf_offset + i];
+            }
+        }
+        if (exercise) {
+            float x0 = 0.0f;
+            if (live) {
+                const double sv = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 1) * c.path_count + i);
+                const double xx = phi * (sv - c.strike);
+                ex = xx > 0.0 ? xx : 0.0;
+                x0 = static_cast<float>(4.0 * (sv * inv_k - 1.0));
+            }
+            for (int j = 0; j < 64; j += 2) {
+                float t;
+                const float za = __fmaf_rn(S.p[kW1 + 2 * j], x0, __fmaf_rn(S.p[kW1 + 2 * j + 1], x1, S.p[kB1 + j]));
+                const float zb = __fmaf_rn(S.p[kW1 + 2 * j + 2], x0, __fmaf_rn(S.p[kW1 + 2 * j + 3], x1, S.p[kB1 + j + 1]));
+                *reinterpret_cast<__nv_bfloat162*>(at(S.h1, s, j, 64)) = __floats2bfloat162_rn(gelu(za, t), gelu(zb, t));
+            }
+            umma::fence_smem_to_async();
+            umma::fence_before_sync();
+            __syncthreads();
+            if (s == 0) {
+                umma::fence_after_sync();
+                for (int kk = 0; kk < 4; ++kk)
+                    umma::mma_bf16(tm, desc(S.h1, 1024, kk), desc(S.w2, 1024, kk), kIdesc, kk > 0);
+                umma::mma_commit(&S.mbar);
+            }
+            ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 5));
+            phase ^= 1u;
+            umma::fence_after_sync();
+            float yhat = S.p[kB3];
+            for (int cc = 0; cc < 4; ++cc) {
+                float zz[16];
+                umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, cc * 16), zz);
+                for (int q = 0; q < 16; ++q) {
+                    float t;
+                    yhat = __fmaf_rn(S.p[kW3 + cc * 16 + q], gelu(zz[q] + S.p[kB2 + cc * 16 + q], t), yhat);
+                }
+            }
+            umma::fence_before_sync();
+            __syncthreads();  // h1 and the accumulator are reused by the next tile
+            // The network predicts (continuation - exercise)/K: exercise where negative.
+            if (live && ok && ex > 0.0 && yhat < 0.0f) v = ex;
+        }
+        if (!live) continue;
+        v *= c.disc;
+        if (last) welford_add(w, v);
+        else cf[c.cf_offset + i] = v;
+    }
+    if (exercise) {
+        if (!ok) umma::mbar_wait(&S.mbar, phase, err, 6);
+        umma::fence_before_sync();
+        __syncthreads();
+        if (warp == 0) umma::tmem_dealloc(tm, 64);
+    }
+    if (last) {
+        w = welford_warp_reduce(w);
+        if ((s & 31) == 0) swf[warp] = w;
+        __syncthreads();
+        if (s == 0) final_part[chunk] = welford_merge(welford_merge(swf[0], swf[1]), welford_merge(swf[2], swf[3]));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// checks: one gradient step, inference, a single GEMM
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128, 1)
+    mlp_grad_kernel(const float* __restrict__ params, const float* __restrict__ x0, const float* __restrict__ x1,
+                    const float* __restrict__ y, const float* __restrict__ wt, int n, float* __restrict__ grad,
+                    float* __restrict__ loss, uint32_t* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
+    const int s = threadIdx.x;
+    for (int i = s; i < kParamStride; i += 128) {
+        S.p[i] = i < kParams ? params[i] : 0.0f;
+        S.m[i] = 0.0f;
+        S.v[i] = 0.0f;
+    }
+    train_setup(S);
+    if (s < 64) refresh_w2_row(S, s);
+    const bool live = s < n;
+    S.x0[s] = live ? x0[s] : 0.0f;
+    S.x1[s] = live ? x1[s] : 0.0f;
+    S.y[s] = live ? y[s] : 0.0f;
+    S.w[s] = live ? wt[s] : 0.0f;
+    const int n_eff = __syncthreads_count(live && wt[s] > 0.0f);
+    uint32_t phase = 0;
+    const bool ok = train_step(S, S.tmem_base, phase, n_eff, false, 0.0f, 1, grad, err);
+    if (s == 0) *loss = S.loss;
+    train_teardown(S, phase, ok, err);
+}
+
+__global__ void __launch_bounds__(128)
+    mlp_forward_kernel(const float* __restrict__ params, const float* __restrict__ x0, const float* __restrict__ x1,
+                       int n, float* __restrict__ out, uint32_t* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+    const int s = threadIdx.x, warp = s >> 5;
+    for (int i = s; i < kParamStride; i += 128) S.p[i] = i < kParams ? params[i] : 0.0f;
+    __syncthreads();
+    if (s < 64)
+        for (int j = 0; j < 64; j += 2)
+            *reinterpret_cast<__nv_bfloat162*>(at(S.w2, s, j, 64)) =
+                __floats2bfloat162_rn(S.p[kW2 + s * 64 + j], S.p[kW2 + s * 64 + j + 1]);
+    if (s == 0) umma::mbar_init(&S.mbar, 1);
+    if (warp == 0) umma::tmem_alloc(&S.tmem_base, 64);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tm = S.tmem_base;
+    uint32_t phase = 0;
+    bool ok = true;
+    const int tiles = (n + 127) / 128;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int i = tile * 128 + s;
+        const float a = i < n ? x0[i] : 0.0f, b = i < n ? x1[i] : 0.0f;
+        for (int j = 0; j < 64; j += 2) {
+            float t;
+            const float za = __fmaf_rn(S.p[kW1 + 2 * j], a, __fmaf_rn(S.p[kW1 + 2 * j + 1], b, S.p[kB1 + j]));
+            const float zb = __fmaf_rn(S.p[kW1 + 2 * j + 2], a, __fmaf_rn(S.p[kW1 + 2 * j + 3], b, S.p[kB1 + j + 1]));
+            *reinterpret_cast<__nv_bfloat162*>(at(S.h1, s, j, 64)) = __floats2bfloat162_rn(gelu(za, t), gelu(zb, t));
+        }
+        umma::fence_smem_to_async();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (s == 0) {
+            umma::fence_after_sync();
+            for (int kk = 0; kk < 4; ++kk)
+                umma::mma_bf16(tm, desc(S.h1, 1024, kk), desc(S.w2, 1024, kk), kIdesc, kk > 0);
+            umma::mma_commit(&S.mbar);
+        }
+        ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 7));
+        phase ^= 1u;
+        umma::fence_after_sync();
+        float yhat = S.p[kB3];
+        for (int cc = 0; cc < 4; ++cc) {
+            float zz[16];
+            umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, cc * 16), zz);
+            for (int q = 0; q < 16; ++q) {
+                float t;
+                yhat = __fmaf_rn(S.p[kW3 + cc * 16 + q], gelu(zz[q] + S.p[kB2 + cc * 16 + q], t), yhat);
+            }
+        }
+        if (i < n) out[i] = ok ? yhat : 0.0f;
+        umma::fence_before_sync();
+        __syncthreads();
+    }
+    if (!ok) umma::mbar_wait(&S.mbar, phase, err, 8);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tm, 64);
+}
+
+// D (128 x 64) = A (128 x 64) B^T (B: 64 x 64), BF16 inputs, FP32 accumulate.
+__global__ void __launch_bounds__(128, 1)
+    umma_selftest_kernel(const float* __restrict__ A, const float* __restrict__ B, float* __restrict__ D,
+                         uint32_t* __restrict__ err) {
+    __shared__ __align__(1024) __nv_bfloat16 a_s[128 * 64];
+    __shared__ __align__(1024) __nv_bfloat16 b_s[64 * 64];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tbase;
+    const int s = threadIdx.x, warp = s >> 5;
+    for (int k = 0; k < 64; ++k) *at(a_s, s, k, 64) = __float2bfloat16_rn(A[s * 64 + k]);
+    if (s < 64)
+        for (int k = 0; k < 64; ++k) *at(b_s, s, k, 64) = __float2bfloat16_rn(B[s * 64 + k]);
+    if (s == 0) umma::mbar_init(&mbar, 1);
+    if (warp == 0) umma::tmem_alloc(&tbase, 64);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tm = tbase;
+    if (s == 0) {
+        for (int kk = 0; kk < 4; ++kk) umma::mma_bf16(tm, desc(a_s, 1024, kk), desc(b_s, 1024, kk), kIdesc, kk > 0);
+        umma::mma_commit(&mbar);
+    }
+    const bool ok = __syncthreads_and(umma::mbar_wait(&mbar, 0, err, 9));
+    umma::fence_after_sync();
+    if (ok) {
+        for (int c = 0; c < 4; ++c) {
+            float v[16];
+            umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, c * 16), v);
+            for (int q = 0; q < 16; ++q) D[s * 64 + c * 16 + q] = v[q];
+        }
+    } else {
+        umma::mbar_wait(&mbar, 0, err, 10);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tm, 64);
+}
+
+template <typename K>
+cudaError_t set_smem(K kernel, size_t bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+
+}  // namespace
+
+size_t mlp_train_smem_bytes() { return sizeof(TrainSmem); }
+size_t mlp_infer_smem_bytes() { return sizeof(InferSmem); }
+
+cudaError_t mlp_prepare() {
+    cudaError_t e = set_smem(lsm_mlp_train<0>, sizeof(TrainSmem));
+    if (e == cudaSuccess) e = set_smem(lsm_mlp_train<1>, sizeof(TrainSmem));
+    if (e == cudaSuccess) e = set_smem(mlp_grad_kernel, sizeof(TrainSmem));
+    if (e == cudaSuccess) e = set_smem(lsm_mlp_exercise<0>, sizeof(InferSmem));
+    if (e == cudaSuccess) e = set_smem(lsm_mlp_exercise<1>, sizeof(InferSmem));
+    if (e == cudaSuccess) e = set_smem(mlp_forward_kernel, sizeof(InferSmem));
+    return e;
+}
+
+cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int n_contracts,
+                                     const uint32_t* chunk_contract, uint32_t total_chunks, const void* store,
+                                     double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
+                                     const MlpConfig& cfg, Welford* final_part, uint32_t* err,
+                                     cudaStream_t stream) {
+    cudaGetLastError();
+    if (total_chunks == 0) return cudaSuccess;
+    if (precision == 0)
+        lsm_mlp_exercise<0><<<total_chunks, 128, sizeof(InferSmem), stream>>>(k, c, chunk_contract, total_chunks,
+                                                                             store, cf, snaps, snap_ok, final_part, err);
+    else
+        lsm_mlp_exercise<1><<<total_chunks, 128, sizeof(InferSmem), stream>>>(k, c, chunk_contract, total_chunks,
+                                                                             store, cf, snaps, snap_ok, final_part, err);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !train) return e;
+    if (precision == 0)
+        lsm_mlp_train<0><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, n_contracts, store, cf, nets, snaps,
+                                                                          snap_ok, adam_t, cfg, err);
+    else
+        lsm_mlp_train<1><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, n_contracts, store, cf, nets, snaps,
+                                                                          snap_ok, adam_t, cfg, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_grad(const float* params, const float* x0, const float* x1, const float* y, const float* w,
+                            int n, float* grad, float* loss, uint32_t* err, cudaStream_t stream) {
+    cudaGetLastError();
+    mlp_grad_kernel<<<1, 128, sizeof(TrainSmem), stream>>>(params, x0, x1, y, w, n, grad, loss, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_forward(const float* params, const float* x0, const float* x1, int n, float* out,
+                               uint32_t* err, cudaStream_t stream) {
+    cudaGetLastError();
+    const int tiles = (n + 127) / 128;
+    const int grid = tiles < 1024 ? (tiles > 0 ? tiles : 1) : 1024;
+    mlp_forward_kernel<<<grid, 128, sizeof(InferSmem), stream>>>(params, x0, x1, n, out, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_umma_selftest(const float* A, const float* B, float* D, uint32_t* err, cudaStream_t stream) {
+    cudaGetLastError();
+    umma_selftest_kernel<<<1, 128, 0, stream>>>(A, B, D, err);
+    return cudaGetLastError();
+}
+
+}  // namespace mcdg

@@ -1,0 +1,37 @@
+// lsm_mlp_dev.hpp -- launch interface of the learned-regression kernels.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "engine.hpp"
+#include "lsm.hpp"
+
+namespace mcdg {
+
+// Training schedule of the continuation network (per contract, per date).
+struct MlpConfig {
+    int steps_first;  // Adam steps at the first (latest) exercise date, from the initial weights
+    int steps;        // Adam steps at every earlier date, warm-started from the later date
+    float lr_first;
+    float lr;
+};
+
+size_t mlp_train_smem_bytes();
+size_t mlp_infer_smem_bytes();
+cudaError_t mlp_prepare();  // opts the kernels into their dynamic shared memory
+// One backward iteration: exercise with the network of date n-k, discount,
+// then (train = true) train the network of date n-k-1 (one CTA per contract).
+cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int n_contracts,
+                                     const uint32_t* chunk_contract, uint32_t total_chunks, const void* store,
+                                     double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
+                                     const MlpConfig& cfg, Welford* final_part, uint32_t* err,
+                                     cudaStream_t stream);
+cudaError_t launch_mlp_grad(const float* params, const float* x0, const float* x1, const float* y, const float* w,
+                            int n, float* grad, float* loss, uint32_t* err, cudaStream_t stream);
+cudaError_t launch_mlp_forward(const float* params, const float* x0, const float* x1, int n, float* out,
+                               uint32_t* err, cudaStream_t stream);
+cudaError_t launch_umma_selftest(const float* A, const float* B, float* D, uint32_t* err, cudaStream_t stream);
+
+}  // namespace mcdg

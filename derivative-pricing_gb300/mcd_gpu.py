@@ -61,6 +61,11 @@ LSM_CONTRACT_DTYPE = np.dtype([(n, "<f8") for n in ("spot", "strike", "rate", "c
 LSM_RESULT_DTYPE = np.dtype([("price", "<f8"), ("standard_error", "<f8"), ("path_count", "<u8"),
                              ("exercise_at_inception", "<i4"), ("reserved", "<i4")])
 LSM_QR, LSM_MLP = 0, 1
+MLP_PARAMS = 4417  # W1[64][2], b1[64], W2[64][64], b2[64], W3[64], b3
+
+
+def _fptr(a):
+    return a.ctypes.data_as(P(C.c_float))
 
 
 def _regression(r) -> int:
@@ -149,6 +154,13 @@ def lib():
     sig("mcd_lsm_american", vp, *D6, i32, i32, u64, u64, i32, i32, P(LsmResult), P(dbl), P(u8))
     sig("mcd_lsm_reprice_frozen", vp, *D6, i32, i32, u64, u64, P(dbl), P(u8), i32, i32, P(dbl))
     sig("mcd_lsm_batch", vp, vp, C.c_size_t, i32, i32, vp)
+    F = P(C.c_float)
+    sig("mcd_lsm_set_mlp_config", vp, i32, i32, dbl, dbl)
+    sig("mcd_lsm_mlp_policy", vp, C.c_size_t, F, P(u8))
+    sig("mcd_lsm_reprice_mlp", vp, *D6, i32, i32, u64, u64, F, P(u8), i32, P(LsmResult))
+    sig("mcd_umma_selftest", vp, F, F, F)
+    sig("mcd_mlp_gradients", vp, F, F, F, F, F, i32, F, F)
+    sig("mcd_mlp_forward", vp, F, F, F, C.c_size_t, F)
     sig("mcd_philox", vp, P(u32), P(u32), C.c_size_t, P(u32))
     sig("mcd_draws", vp, u64, u64, u64, u32, u32, i32, i32, P(dbl))
     sig("mcd_kernel_timing", vp, i32, P(dbl), P(u64))
@@ -304,6 +316,53 @@ class Engine:
         self._check(self._lib.mcd_lsm_batch(self.handle, contracts.ctypes.data, len(contracts),
                                             _prec(precision), _regression(regression),
                                             out.ctypes.data))
+        return out
+
+    # -- learned regression ----------------------------------------------------------------
+    def set_mlp_config(self, steps_first=1000, steps=200, lr_first=3e-3, lr=1e-3):
+        self._check(self._lib.mcd_lsm_set_mlp_config(self.handle, steps_first, steps, lr_first, lr))
+
+    def mlp_policy(self, contract: int, monitoring_points: int):
+        w = np.zeros((monitoring_points + 1, MLP_PARAMS), dtype=np.float32)
+        has = np.zeros(monitoring_points + 1, dtype=np.uint8)
+        self._check(self._lib.mcd_lsm_mlp_policy(self.handle, contract, _fptr(w),
+                                                 has.ctypes.data_as(P(u8))))
+        return w, has
+
+    def reprice_mlp(self, spot, strike, rate, carry_yield, vol, time, type, monitoring_points,
+                    path_count, seed, weights, has, precision="fp32") -> LsmResult:
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        h = np.ascontiguousarray(has, dtype=np.uint8)
+        out = LsmResult()
+        self._check(self._lib.mcd_lsm_reprice_mlp(self.handle, spot, strike, rate, carry_yield, vol,
+                                                  time, type, monitoring_points, path_count, seed,
+                                                  _fptr(w), h.ctypes.data_as(P(u8)),
+                                                  _prec(precision), C.byref(out)))
+        return out
+
+    def umma_selftest(self, a, b):
+        a = np.ascontiguousarray(a, dtype=np.float32).reshape(128, 64)
+        b = np.ascontiguousarray(b, dtype=np.float32).reshape(64, 64)
+        d = np.zeros((128, 64), dtype=np.float32)
+        self._check(self._lib.mcd_umma_selftest(self.handle, _fptr(a), _fptr(b), _fptr(d)))
+        return d
+
+    def mlp_gradients(self, params, x0, x1, y, w):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        arrs = [np.ascontiguousarray(v, dtype=np.float32) for v in (x0, x1, y, w)]
+        g = np.zeros(MLP_PARAMS, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        self._check(self._lib.mcd_mlp_gradients(self.handle, _fptr(params), *[_fptr(a) for a in arrs],
+                                                len(arrs[0]), _fptr(g), _fptr(loss)))
+        return g, float(loss[0])
+
+    def mlp_forward(self, params, x0, x1):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        x0 = np.ascontiguousarray(x0, dtype=np.float32)
+        x1 = np.ascontiguousarray(x1, dtype=np.float32)
+        out = np.zeros(len(x0), dtype=np.float32)
+        self._check(self._lib.mcd_mlp_forward(self.handle, _fptr(params), _fptr(x0), _fptr(x1),
+                                              len(x0), _fptr(out)))
         return out
 
     # -- batch -----------------------------------------------------------------------------

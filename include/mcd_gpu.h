@@ -268,6 +268,36 @@ int mcd_lsm_reprice_frozen(mcd_ctx* ctx, double spot, double strike, double rate
 int mcd_lsm_batch(mcd_ctx* ctx, const mcd_lsm_contract* contracts, size_t n, int precision,
                   int regression, mcd_lsm_result* results);
 
+/* Learned regression (MCD_LSM_MLP).  No counterpart in the reference: it
+ * replaces the Laguerre least-squares fit of src/pricers/lsm.cpp:88-108 by a
+ * 2 -> 64 -> 64 -> 1 GELU network of (4 (S/K - 1), tau/T) trained at every
+ * exercise date on in-the-money paths (Adam, BF16 tensor-core GEMMs with FP32
+ * accumulation), warm-started from the later date.  A contract whose training
+ * produced non-finite weights is priced by the QR regression instead
+ * (mcd_lsm_result.reserved = 1).  Schedule: steps_first Adam steps of 128
+ * samples at the latest date, steps at each earlier date. */
+int mcd_lsm_set_mlp_config(mcd_ctx* ctx, int steps_first, int steps, double lr_first, double lr);
+/* Networks of contract `contract` of the last learned run:
+ * weights (monitoring_points+1) x 4417 floats (layout: W1[64][2], b1[64],
+ * W2[64][64], b2[64], W3[64], b3), has (monitoring_points+1). */
+int mcd_lsm_mlp_policy(mcd_ctx* ctx, size_t contract, float* weights, uint8_t* has);
+/* Frozen learned policy replayed on the paths of `seed` (out-of-sample
+ * evaluation); counterpart of reprice_against_frozen_policy for networks. */
+int mcd_lsm_reprice_mlp(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                        double vol, double time, int type, int monitoring_points, uint64_t path_count,
+                        uint64_t seed, const float* weights, const uint8_t* has, int precision,
+                        mcd_lsm_result* out);
+/* Checks of the tensor-core kernels (no counterpart in the reference):
+ * D (128x64) = A (128x64) B^T (B 64x64) with BF16 inputs and FP32
+ * accumulation; one forward/backward pass of the network on n <= 128 samples
+ * (gradient of sum_i w_i (f(x_i) - y_i)^2 / #{w_i > 0}, parameter layout as
+ * above); inference on n inputs. */
+int mcd_umma_selftest(mcd_ctx* ctx, const float* a, const float* b, float* d);
+int mcd_mlp_gradients(mcd_ctx* ctx, const float* params, const float* x0, const float* x1,
+                      const float* y, const float* w, int n, float* grad, float* loss);
+int mcd_mlp_forward(mcd_ctx* ctx, const float* params, const float* x0, const float* x1, size_t n,
+                    float* out);
+
 /* ---- draws (parity and diagnostics) ------------------------------------- */
 /* Philox4x32-10 of n (counter, key) pairs; replaces mcd::philox4x32_10
  * (src/core/rng.cpp:41-47).  counters: n x 4, keys: n x 2, out: n x 4. */

@@ -1,0 +1,101 @@
+"""GPU checks of the tensor-core network kernels and the learned LSM regression.
+
+Bars:
+  * tcgen05 GEMM (BF16 in, FP32 accumulate) equals the BF16-rounded product to FP32
+    summation accuracy.
+  * One forward/backward pass: every gradient block within 2 % (relative L2) of
+    the oracle evaluated with the same BF16 rounding points (the remainder is
+    tanh.approx and FP32 summation order); inference within 1 % of the oracle.
+  * Learned LSM: within 3 SE (+ the 50-date Bermudan gap allowance 0.02) of the
+    CRR American tree, and its frozen policy replayed out of sample agrees with
+    the in-sample price within 3 SE.
+  * Gain over the method without it: on held-out paths (a fresh seed, same paths
+    for both policies) the learned exercise policy is worth at least as much as
+    the Laguerre QR policy, and its in-sample regression loss is lower.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def test_umma_gemm_matches_bf16_product(engine):
+    rng = np.random.default_rng(11)
+    a = rng.standard_normal((128, 64)).astype(np.float32)
+    b = rng.standard_normal((64, 64)).astype(np.float32)
+    d = engine.umma_selftest(a, b)
+    ref = M.bf16(a) @ M.bf16(b).T
+    assert np.abs(d - ref).max() <= 1e-4 * np.abs(ref).max(), np.abs(d - ref).max()
+
+
+@pytest.mark.parametrize("n", [128, 77])
+def test_gradients_match_oracle(engine, n):
+    rng = np.random.default_rng(n)
+    p = M.init_params(rng)
+    p[M.B1:M.W2] = rng.standard_normal(64) * 0.1
+    p[M.B2:M.W3] = rng.standard_normal(64) * 0.1
+    p = p.astype(np.float32).astype(np.float64)
+    x0 = rng.uniform(-2, 0.5, n).astype(np.float32)
+    x1 = rng.uniform(0, 1, n).astype(np.float32)
+    y = rng.uniform(0, 0.3, n).astype(np.float32)
+    w = (rng.uniform(size=n) > 0.3).astype(np.float32)
+    g, loss = engine.mlp_gradients(p, x0, x1, y, w)
+    ref_loss, ref = M.loss_and_grad(p, x0, x1, y, w, bf16_tc=True)
+    assert abs(loss - ref_loss) <= 1e-2 * ref_loss
+    for name, lo, hi in [("W1", M.W1, M.B1), ("b1", M.B1, M.W2), ("W2", M.W2, M.B2), ("b2", M.B2, M.W3),
+                         ("W3", M.W3, M.B3), ("b3", M.B3, M.B3 + 1)]:
+        err = rel_l2(g[lo:hi], ref[lo:hi])
+        assert err <= 2e-2, (name, err)
+
+
+def test_forward_matches_oracle(engine):
+    rng = np.random.default_rng(5)
+    p = M.init_params(rng).astype(np.float32)
+    n = 1000
+    x0 = rng.uniform(-2, 0.5, n).astype(np.float32)
+    x1 = rng.uniform(0, 1, n).astype(np.float32)
+    out = engine.mlp_forward(p, x0, x1)
+    ref = M.forward(p.astype(np.float64), x0, x1, bf16_tc=True)
+    assert rel_l2(out, ref) <= 1e-2
+
+
+CASES = [(36, 40, .06, 0, .2, 1.0, 1), (40, 40, .06, 0, .4, 2.0, 1)]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_learned_lsm_against_tree_and_out_of_sample(engine, orc, case):
+    s, k, r, q, v, t, ty = case
+    paths, n = 1 << 17, 50
+    res = engine.monte_carlo_lsm_american(s, k, r, q, v, t, ty, n, paths, 42, precision="fp32",
+                                          regression="mlp")
+    assert res.reserved == 0  # no QR fallback was needed
+    tree = orc.orc_crr_binomial_american(s, k, r, q, v, t, 2000, ty)
+    assert abs(res.price - tree) < 3 * res.standard_error + 0.02, (res.price, res.standard_error, tree)
+    w, has = engine.mlp_policy(0, n)
+    assert has[1:n].all()
+    oos = engine.reprice_mlp(s, k, r, q, v, t, ty, n, paths, 4242, w, has, "fp32")
+    assert abs(oos.price - res.price) < 3 * np.hypot(oos.standard_error, res.standard_error) + 0.01
+
+
+def test_learned_policy_gains_over_qr_out_of_sample(engine, orc):
+    # Held-out evaluation: both policies trained on seed 42, replayed on seed 777.
+    s, k, r, q, v, t, ty = 40, 40, .06, 0, .4, 2.0, 1
+    paths, n = 1 << 17, 50
+    engine.monte_carlo_lsm_american(s, k, r, q, v, t, ty, n, paths, 42, precision="fp32", regression="mlp")
+    w, has = engine.mlp_policy(0, n)
+    qr, co, hq = engine.monte_carlo_lsm_american(s, k, r, q, v, t, ty, n, paths, 42, precision="fp32",
+                                                 policy=True)
+    mlp_oos = engine.reprice_mlp(s, k, r, q, v, t, ty, n, paths, 777, w, has, "fp32").price
+    qr_oos = engine.reprice_against_frozen_policy(s, k, r, q, v, t, ty, n, paths, 777, co, hq, False, "fp32")
+    tree = orc.orc_crr_binomial_american(s, k, r, q, v, t, 2000, ty)
+    print(f"out-of-sample: learned {mlp_oos:.5f}  QR {qr_oos:.5f}  tree {tree:.5f}  SE {qr.standard_error:.5f}")
+    # Same evaluation paths for both: the difference has far less noise than either price.
+    assert mlp_oos >= qr_oos - 1.0 * qr.standard_error
