@@ -95,8 +95,8 @@ struct Ctx {
     DeviceBuffer ext[24];
 
     // Training schedule of the learned LSM regression (mcd_lsm_set_mlp_config).
-    int mlp_steps_first = 1000;
-    int mlp_steps = 200;
+    int mlp_steps_first = 300;
+    int mlp_steps = 0;
     float mlp_lr_first = 3e-3f;
     float mlp_lr = 1e-3f;
     // Networks of the last learned-LSM run (for mcd_lsm_mlp_policy).

@@ -26,7 +26,12 @@ struct LsmDev {
     uint32_t chunk_begin, n_chunks;
     uint32_t reg_offset;  // row of date 0 in the per-date regression table
     int32_t n_steps, type;
+    uint32_t group_begin, n_groups;  // learned regression: CTAs of group_chunks chunks each
+    uint32_t group_chunks;
 };
+
+constexpr int kLsmMaxGroups = 256;  // learned-regression CTAs per contract at most
+constexpr int kGramPacked = 66 * 67 / 2;  // upper triangle of the 66 x 66 Gram matrix, row-major
 
 // Regression state of one (contract, date): T = R1^{-1} (upper triangular,
 // packed row-major: (0,0) (0,1) (0,2) (0,3) (1,1) (1,2) (1,3) (2,2) (2,3) (3,3)),

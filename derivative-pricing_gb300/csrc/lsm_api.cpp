@@ -19,13 +19,15 @@ namespace {
 
 // Extension slots of Ctx::ext used by this module (Heston uses 0..3).
 enum { kDev = 4, kChunkMap = 5, kStore = 6, kCf = 7, kReg = 8, kPartA = 9, kPartB = 10,
-       kFinal = 11, kOut = 12, kNets = 13, kSnaps = 14, kSnapOk = 15, kAdamT = 16, kErr = 17 };
+       kFinal = 11, kOut = 12, kNets = 13, kSnaps = 14, kSnapOk = 15, kAdamT = 16, kErr = 17,
+       kGroupMap = 18, kGramPart = 19, kGramSum = 20 };
 
 struct LsmPlan {
     std::vector<LsmDev> dev;
     std::vector<uint32_t> chunk_contract;
+    std::vector<uint32_t> group_contract;  // learned regression: group -> contract
     uint64_t store_elems = 0, cf_elems = 0, reg_rows = 0;
-    uint32_t total_chunks = 0;
+    uint32_t total_chunks = 0, total_groups = 0;
     int max_steps = 0;
 };
 
@@ -70,6 +72,16 @@ int plan_lsm(Ctx& ctx, const mcd_lsm_contract* cs, size_t n, LsmPlan& p) {
         p.store_elems += static_cast<uint64_t>(c.monitoring_points) * c.path_count;
         p.cf_elems += c.path_count;
         p.reg_rows += static_cast<uint64_t>(c.monitoring_points) + 1;
+        // learned regression: at most kLsmMaxGroups CTAs per contract; the
+        // split depends on this contract alone, so its Gram sums (and hence
+        // its price) do not depend on the rest of the batch
+        const uint64_t per_group = (chunks + kLsmMaxGroups - 1) / kLsmMaxGroups;
+        const uint32_t groups = static_cast<uint32_t>((chunks + per_group - 1) / per_group);
+        d.group_chunks = static_cast<uint32_t>(per_group);
+        d.group_begin = p.total_groups;
+        d.n_groups = groups;
+        for (uint32_t g = 0; g < groups; ++g) p.group_contract.push_back(static_cast<uint32_t>(i));
+        p.total_groups += groups;
         p.max_steps = std::max(p.max_steps, c.monitoring_points);
     }
     return MCD_OK;
@@ -98,6 +110,9 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
         if (!rc) rc = ctx.reserve(ctx.ext[kSnapOk], sizeof(int) * p.reg_rows, "mlp snapshot flags");
         if (!rc) rc = ctx.reserve(ctx.ext[kAdamT], sizeof(int) * n, "mlp adam steps");
         if (!rc) rc = ctx.reserve(ctx.ext[kErr], 256, "mlp error word");
+        if (!rc) rc = ctx.reserve(ctx.ext[kGroupMap], sizeof(uint32_t) * std::max<uint32_t>(p.total_groups, 1), "mlp group map");
+        if (!rc) rc = ctx.reserve(ctx.ext[kGramPart], sizeof(float) * kGramPacked * std::max<uint32_t>(p.total_groups, 1), "mlp gram partials");
+        if (!rc) rc = ctx.reserve(ctx.ext[kGramSum], sizeof(double) * kGramPacked * n, "mlp gram sums");
         if (!rc) {
             cudaError_t pe = mlp_prepare();
             if (pe != cudaSuccess) rc = ctx.cuda_fail(pe, "mlp shared memory opt-in");
@@ -117,6 +132,9 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
     }
     if (e == cudaSuccess && mlp) {
         e = cudaMemsetAsync(ctx.ext[kErr].ptr, 0, 256, ctx.stream);
+        if (e == cudaSuccess && p.total_groups)
+            e = cudaMemcpyAsync(ctx.ext[kGroupMap].ptr, p.group_contract.data(), sizeof(uint32_t) * p.total_groups,
+                                cudaMemcpyHostToDevice, ctx.stream);
         if (e == cudaSuccess) {
             if (frozen_nets && frozen_ok) {
                 e = cudaMemcpyAsync(ctx.ext[kSnaps].ptr, frozen_nets->data(), sizeof(float) * frozen_nets->size(),
@@ -143,12 +161,15 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
                                         ctx.ext[kStore].ptr, ctx.stream);
     for (int k = 0; k < p.max_steps && le == cudaSuccess; ++k) {
         if (mlp)
-            le = launch_lsm_mlp_iteration(precision, k, !frozen, d_dev, static_cast<int>(n), d_map, p.total_chunks,
+            le = launch_lsm_mlp_iteration(precision, k, !frozen, d_dev, static_cast<int>(n),
+                                          static_cast<const uint32_t*>(ctx.ext[kGroupMap].ptr), p.total_groups,
                                           ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
                                           static_cast<float*>(ctx.ext[kNets].ptr),
                                           static_cast<float*>(ctx.ext[kSnaps].ptr),
                                           static_cast<int*>(ctx.ext[kSnapOk].ptr),
-                                          static_cast<int*>(ctx.ext[kAdamT].ptr), cfg,
+                                          static_cast<int*>(ctx.ext[kAdamT].ptr),
+                                          static_cast<float*>(ctx.ext[kGramPart].ptr),
+                                          static_cast<double*>(ctx.ext[kGramSum].ptr), cfg,
                                           static_cast<Welford*>(ctx.ext[kFinal].ptr),
                                           static_cast<uint32_t*>(ctx.ext[kErr].ptr), ctx.stream);
         else
@@ -236,7 +257,7 @@ int lsm_batch(Ctx& ctx, const mcd_lsm_contract* cs, size_t n, int precision, int
             // is not trusted and the contract is priced by the QR regression.
             const int nd = p.dev[i].n_steps;
             for (int d = 1; d < nd; ++d)
-                if (ok[p.dev[i].reg_offset + d] != 1) {
+                if (ok[p.dev[i].reg_offset + d] == 0) {
                     fallback.push_back(i);
                     break;
                 }

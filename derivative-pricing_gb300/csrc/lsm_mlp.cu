@@ -1,24 +1,34 @@
 // lsm_mlp.cu -- learned continuation values for Longstaff-Schwartz.
 //
-// In place of the Laguerre least-squares fit of src/pricers/lsm.cpp:88-108, a
-// 2 -> 64 -> 64 -> 1 GELU network (mlp.cuh) is trained at every exercise date
-// on in-the-money paths from the simulator (targets: the discounted cash flows,
-// as in the reference), warm-started from the previous (later) date, and used
-// for the exercise decisions at that date.
+// In place of the Laguerre least-squares fit of src/pricers/lsm.cpp:88-108,
+// the regression basis is *learned*: a 2 -> 64 -> 64 -> 1 GELU network
+// (mlp.cuh) of (4 (S/K - 1), tau/T) is trained with Adam on in-the-money paths
+// from the simulator (target: time value = (discounted cash flow - exercise
+// value)/K), and its 64 last-layer features plus a bias become the regression
+// basis.  At every exercise date the output layer is then fitted exactly, by
+// ridge least squares over *all* in-the-money paths of that date (like the
+// reference's QR fit, but on 65 learned functions instead of 4 Laguerre
+// ones); exercise where the predicted time value is negative.
 //
-// Kernels (all operands K-major BF16 in shared memory, FP32 accumulators in
+// Kernels (BF16 operands K-major in shared memory, FP32 accumulators in
 // tensor memory; umma.cuh):
-//   lsm_mlp_train     one CTA per contract: `steps` Adam steps on 128-sample
-//                     tiles.  Per step the 64x64 layer runs three tcgen05 MMA
-//                     groups -- forward Z2 = H1 W2^T (4 x K16), input gradient
-//                     dH1 = dZ2 W2 (4 x K16) and weight gradient
-//                     dW2 = dZ2^T H1 (8 x K16, M padded to 128 with zero rows)
-//                     -- and the CUDA cores do layer 1, layer 3, the GELUs and
-//                     the fixed-order reductions of the small gradients.
-//   lsm_mlp_exercise  one CTA per 1024-path chunk: inference (the forward MMA
-//                     per 128-path tile), exercise, discount, final Welford.
-//   mlp_grad_kernel   one step without update, for gradient checks.
-//   mlp_forward_kernel / umma_selftest_kernel   inference and GEMM checks.
+//   lsm_mlp_train   one CTA per contract: Adam steps on 128-sample tiles.  Per
+//                   step the 64x64 layer runs three tcgen05 MMA groups --
+//                   forward Z2 = H1 W2^T (4 x K16), input gradient dH1 = dZ2 W2
+//                   (4 x K16), weight gradient dW2 = dZ2^T H1 (8 x K16, M padded
+//                   to 128 with zero rows) -- and the CUDA cores do layers 1 and
+//                   3, the GELUs and the fixed-order reductions.
+//   lsm_mlp_pass    one CTA per group of chunks: exercise with the network
+//                   of date e, discount, and the Gram matrix of date e-1 on the
+//                   tensor core -- per 128-path tile an MMA with M = 128 (66
+//                   rows used), N = 80, K = 128 paths over
+//                   [features | 1 | target], accumulated in tensor memory.
+//   lsm_mlp_gram_reduce  one thread per Gram entry and contract: fixed-order
+//                   compensated sum of the group Gram matrices.
+//   lsm_mlp_solve   one CTA per contract: scaled ridge Cholesky solve (65 x 65,
+//                   FP32 factor, FP64-residual refinement) for the output
+//                   layer of that date.
+//   mlp_grad_kernel / mlp_forward_kernel / umma_selftest_kernel   checks.
 //
 // Every mbarrier wait is bounded (umma.cuh); on a timeout the kernel records
 // an error code, waits once more (bounded) for its MMAs, frees its tensor
@@ -386,140 +396,445 @@ __global__ void __launch_bounds__(128, 1)
         ++t;
         ok = train_step(S, tm, phase, n_eff, true, lr, t, nullptr, err);
     }
-    // persist the network and snapshot it for this date
-    bool finite = true;
+    // persist the network (features and output layer) for the next dates
     for (int i = s; i < kParamStride; i += 128) {
-        const float pv = S.p[i];
-        if (!(pv == pv) || fabsf(pv) > 1e30f) finite = false;
-        net[i] = pv;
+        net[i] = S.p[i];
         net[kParamStride + i] = S.m[i];
         net[2 * kParamStride + i] = S.v[i];
-        snaps[(static_cast<size_t>(c.reg_offset) + date) * kParamStride + i] = pv;
     }
-    const int all_finite = __syncthreads_and(finite);
-    if (s == 0) {
-        adam_t[ci] = t;
-        snap_ok[c.reg_offset + date] = (ok && all_finite) ? 1 : 0;
-    }
+    if (s == 0) adam_t[ci] = t;
     train_teardown(S, phase, ok, err);
 }
 
 // ---------------------------------------------------------------------------
-// exercise with the network of date e, discount, final Welford
+// pass over a group of chunks: exercise at date e with the network of that
+// date, discount, final Welford (e = 1) and/or the tensor-core Gram matrix of
+// date e - 1 over [features(S_{e-1}) | 1 | time-value target]
 // ---------------------------------------------------------------------------
+constexpr int kGramN = 80;    // MMA N of the Gram product (66 used)
+constexpr int kGramDim = 66;  // 64 features, bias, target
+constexpr int kSmall = 321;   // W1, b1 (as layout), then b2, W3, b3 copied below
+
+struct __align__(1024) PassSmem {
+    __nv_bfloat16 h1d[128 * 64];   // decision network input tile (S at date e)
+    __nv_bfloat16 h1c[128 * 64];   // current network input tile (S at date e-1)
+    __nv_bfloat16 xt[128 * 128];   // Gram operand [row][path]; rows 66..127 stay zero
+    __nv_bfloat16 w2d[64 * 64];
+    __nv_bfloat16 w2c[64 * 64];
+    float pd[kParamStride - 4096];  // decision network without W2: W1 b1 | b2 W3 b3
+    float pc[kParamStride - 4096];
+    uint64_t mbar;
+    uint32_t tmem_base;
+};
+
+// Copies a network into shared memory: the small parameters as FP32 (W2's
+// slot removed) and W2 as the BF16 K-major MMA operand.
+__device__ void load_net(const float* __restrict__ net, float* small, __nv_bfloat16* w2) {
+    const int s = threadIdx.x;
+    for (int i = s; i < kW2; i += 128) small[i] = net[i];
+    for (int i = s; i < kParams - kB2; i += 128) small[kW2 + i] = net[kB2 + i];
+    if (s < 64)
+        for (int j = 0; j < 64; j += 2)
+            *reinterpret_cast<__nv_bfloat162*>(at(w2, s, j, 64)) =
+                __floats2bfloat162_rn(net[kW2 + s * 64 + j], net[kW2 + s * 64 + j + 1]);
+}
+
+// Small-parameter offsets inside PassSmem::pd / pc.
+constexpr int sW1 = kW1, sB1 = kB1, sB2 = kW2, sW3 = kW2 + (kW3 - kB2), sB3 = kW2 + (kB3 - kB2);
+
+__device__ __forceinline__ void layer1_row(const float* small, float x0, float x1, __nv_bfloat16* h1, int s) {
+    for (int j = 0; j < 64; j += 2) {
+        float t;
+        const float za = __fmaf_rn(small[sW1 + 2 * j], x0, __fmaf_rn(small[sW1 + 2 * j + 1], x1, small[sB1 + j]));
+        const float zb = __fmaf_rn(small[sW1 + 2 * j + 2], x0, __fmaf_rn(small[sW1 + 2 * j + 3], x1, small[sB1 + j + 1]));
+        *reinterpret_cast<__nv_bfloat162*>(at(h1, s, j, 64)) = __floats2bfloat162_rn(gelu(za, t), gelu(zb, t));
+    }
+}
+
+enum PassMode { kStep = 1, kGram = 2 };
+
 template <int PREC>
 __global__ void __launch_bounds__(128)
-    lsm_mlp_exercise(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
-                     uint32_t total_chunks, const void* __restrict__ store, double* __restrict__ cf,
-                     const float* __restrict__ snaps, const int* __restrict__ snap_ok,
-                     Welford* __restrict__ final_part, uint32_t* __restrict__ err) {
+    lsm_mlp_pass(int k, int mode, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
+                 uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
+                 const float* __restrict__ nets, const float* __restrict__ snaps, const int* __restrict__ snap_ok,
+                 float* __restrict__ gram_part, Welford* __restrict__ final_part, uint32_t* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+    PassSmem& S = *reinterpret_cast<PassSmem*>(smem_raw);
     __shared__ Welford swf[4];
-    const uint32_t chunk = blockIdx.x;
-    if (chunk >= total_chunks) return;
-    const LsmDev c = cs[chunk_contract[chunk]];
+    const uint32_t g = blockIdx.x;
+    if (g >= total_groups) return;
+    const uint32_t ci = group_contract[g];
+    const LsmDev c = cs[ci];
     const int n = c.n_steps;
     const int e = n - k;
     if (e < 1) return;
-    const int s = threadIdx.x;
-    const int warp = s >> 5;
-    const bool init = (k == 0);
-    const bool last = (e == 1);
-    const bool exercise = !init && e <= n - 1 && snap_ok[c.reg_offset + e] == 1;
-    const double inv_k = 1.0 / c.strike;
+    const bool step = (mode & kStep) != 0;
+    const bool init = step && k == 0;
+    const bool last = step && e == 1;
+    const bool exercise = step && k > 0 && e <= n - 1 && snap_ok[c.reg_offset + e] == 1;
+    const bool gram = (mode & kGram) != 0 && e - 1 >= 1;
+    if (!step && !gram) return;
+    const int s = threadIdx.x, warp = s >> 5;
     const double phi = c.type == 0 ? 1.0 : -1.0;
-    uint32_t tm = 0, phase = 0;
-    bool ok = true;
-    if (exercise) {
-        const float* net = snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride;
-        for (int i = s; i < kParamStride; i += 128) S.p[i] = net[i];
-        __syncthreads();
-        if (s < 64)
-            for (int j = 0; j < 64; j += 2)
-                *reinterpret_cast<__nv_bfloat162*>(at(S.w2, s, j, 64)) =
-                    __floats2bfloat162_rn(S.p[kW2 + s * 64 + j], S.p[kW2 + s * 64 + j + 1]);
+    const double inv_k = 1.0 / c.strike;
+    const bool mma = exercise || gram;
+    if (mma) {
+        if (exercise) load_net(snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride, S.pd, S.w2d);
+        if (gram) load_net(nets + static_cast<size_t>(ci) * 3 * kParamStride, S.pc, S.w2c);
+        for (int i = s; i < 128 * 128 / 2; i += 128) reinterpret_cast<uint32_t*>(S.xt)[i] = 0u;
         if (s == 0) umma::mbar_init(&S.mbar, 1);
-        if (warp == 0) umma::tmem_alloc(&S.tmem_base, 64);
+        if (warp == 0) umma::tmem_alloc(&S.tmem_base, 256);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         umma::fence_before_sync();
         __syncthreads();
         umma::fence_after_sync();
-        tm = S.tmem_base;
     }
-    const float x1 = static_cast<float>(n - e) / static_cast<float>(n);
+    const uint32_t tm = mma ? S.tmem_base : 0u;
+    uint32_t phase = 0;
+    bool ok = true;
+    bool gram_pending = false, gram_started = false;
+    const float x1e = static_cast<float>(n - e) / static_cast<float>(n);
+    const float x1d = static_cast<float>(n - (e - 1)) / static_cast<float>(n);
+    const uint32_t gl = g - c.group_begin;
+    const uint32_t chunk0 = gl * c.group_chunks;
+    const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
     Welford w{0ull, 0.0, 0.0};
-    const uint32_t local = chunk - c.chunk_begin;
-    for (int tile = 0; tile < kLsmChunk / 128; ++tile) {
-        const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + tile * 128 + s;
-        const bool live = i < c.path_count;
-        double v = 0.0, ex = 0.0;
-        if (live) {
-            if (init) {
-                const double sT = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(n - 1) * c.path_count + i);
-                const double x = phi * (sT - c.strike);
-                v = x > 0.0 ? x : 0.0;
-            } else {
-                v = cf[c.cf_offset + i];
-            }
-        }
-        if (exercise) {
-            float x0 = 0.0f;
+    for (uint32_t ch = chunk0; ch < chunk1; ++ch) {
+        for (int tile = 0; tile < kLsmChunk / 128; ++tile) {
+            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + tile * 128 + s;
+            const bool live = i < c.path_count;
+            double v = 0.0, ex_e = 0.0, ex_d = 0.0, s_d = 0.0;
             if (live) {
-                const double sv = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 1) * c.path_count + i);
-                const double xx = phi * (sv - c.strike);
-                ex = xx > 0.0 ? xx : 0.0;
-                x0 = static_cast<float>(4.0 * (sv * inv_k - 1.0));
-            }
-            for (int j = 0; j < 64; j += 2) {
-                float t;
-                const float za = __fmaf_rn(S.p[kW1 + 2 * j], x0, __fmaf_rn(S.p[kW1 + 2 * j + 1], x1, S.p[kB1 + j]));
-                const float zb = __fmaf_rn(S.p[kW1 + 2 * j + 2], x0, __fmaf_rn(S.p[kW1 + 2 * j + 3], x1, S.p[kB1 + j + 1]));
-                *reinterpret_cast<__nv_bfloat162*>(at(S.h1, s, j, 64)) = __floats2bfloat162_rn(gelu(za, t), gelu(zb, t));
-            }
-            umma::fence_smem_to_async();
-            umma::fence_before_sync();
-            __syncthreads();
-            if (s == 0) {
-                umma::fence_after_sync();
-                for (int kk = 0; kk < 4; ++kk)
-                    umma::mma_bf16(tm, desc(S.h1, 1024, kk), desc(S.w2, 1024, kk), kIdesc, kk > 0);
-                umma::mma_commit(&S.mbar);
-            }
-            ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 5));
-            phase ^= 1u;
-            umma::fence_after_sync();
-            float yhat = S.p[kB3];
-            for (int cc = 0; cc < 4; ++cc) {
-                float zz[16];
-                umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, cc * 16), zz);
-                for (int q = 0; q < 16; ++q) {
-                    float t;
-                    yhat = __fmaf_rn(S.p[kW3 + cc * 16 + q], gelu(zz[q] + S.p[kB2 + cc * 16 + q], t), yhat);
+                if (init) {
+                    const double sT = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(n - 1) * c.path_count + i);
+                    const double x = phi * (sT - c.strike);
+                    v = x > 0.0 ? x : 0.0;
+                } else {
+                    v = cf[c.cf_offset + i];
                 }
             }
-            umma::fence_before_sync();
-            __syncthreads();  // h1 and the accumulator are reused by the next tile
-            // The network predicts (continuation - exercise)/K: exercise where negative.
-            if (live && ok && ex > 0.0 && yhat < 0.0f) v = ex;
+            if (exercise) {
+                float x0 = 0.0f;
+                if (live) {
+                    const double se = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 1) * c.path_count + i);
+                    const double xx = phi * (se - c.strike);
+                    ex_e = xx > 0.0 ? xx : 0.0;
+                    x0 = static_cast<float>(4.0 * (se * inv_k - 1.0));
+                }
+                layer1_row(S.pd, x0, x1e, S.h1d, s);
+            }
+            if (gram) {
+                float x0 = 0.0f;
+                if (live) {
+                    s_d = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 2) * c.path_count + i);
+                    const double xx = phi * (s_d - c.strike);
+                    ex_d = xx > 0.0 ? xx : 0.0;
+                    x0 = static_cast<float>(4.0 * (s_d * inv_k - 1.0));
+                }
+                layer1_row(S.pc, x0, x1d, S.h1c, s);
+            }
+            if (mma) {
+                umma::fence_smem_to_async();
+                umma::fence_before_sync();
+                __syncthreads();
+                if (s == 0) {
+                    umma::fence_after_sync();
+                    if (exercise)
+                        for (int kk = 0; kk < 4; ++kk)
+                            umma::mma_bf16(tm, desc(S.h1d, 1024, kk), desc(S.w2d, 1024, kk), kIdesc, kk > 0);
+                    if (gram)
+                        for (int kk = 0; kk < 4; ++kk)
+                            umma::mma_bf16(tm + 64, desc(S.h1c, 1024, kk), desc(S.w2c, 1024, kk), kIdesc, kk > 0);
+                    umma::mma_commit(&S.mbar);  // also covers the previous tile's Gram MMA
+                }
+                ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 11));
+                phase ^= 1u;
+                gram_pending = false;
+                umma::fence_after_sync();
+            }
+            if (exercise) {
+                float yhat = S.pd[sB3];
+                for (int cc = 0; cc < 4; ++cc) {
+                    float zz[16];
+                    umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, cc * 16), zz);
+                    for (int q = 0; q < 16; ++q) {
+                        float t;
+                        yhat = __fmaf_rn(S.pd[sW3 + cc * 16 + q], gelu(zz[q] + S.pd[sB2 + cc * 16 + q], t), yhat);
+                    }
+                }
+                // predicted time value < 0: exercise
+                if (live && ok && ex_e > 0.0 && yhat < 0.0f) v = ex_e;
+            }
+            if (live && step) {
+                v *= c.disc;
+                if (last) welford_add(w, v);
+                else cf[c.cf_offset + i] = v;
+            }
+            if (gram) {
+                const bool itm = live && ex_d > 0.0;
+                const float y = itm ? static_cast<float>((v - ex_d) * inv_k) : 0.0f;
+                for (int cc = 0; cc < 4; ++cc) {
+                    float zz[16];
+                    umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 64 + cc * 16), zz);
+                    for (int q = 0; q < 16; ++q) {
+                        float t;
+                        const float h = itm ? gelu(zz[q] + S.pc[sB2 + cc * 16 + q], t) : 0.0f;
+                        *at(S.xt, cc * 16 + q, s, 128) = __float2bfloat16_rn(h);
+                    }
+                }
+                *at(S.xt, 64, s, 128) = __float2bfloat16_rn(itm ? 1.0f : 0.0f);
+                *at(S.xt, 65, s, 128) = __float2bfloat16_rn(y);
+                umma::fence_smem_to_async();
+                umma::fence_before_sync();
+                __syncthreads();
+                if (s == 0) {
+                    umma::fence_after_sync();
+                    // D[i][j] += sum_paths xt[i][p] xt[j][p]  (M = 128 rows, N = 80)
+                    for (int kk = 0; kk < 8; ++kk)
+                        umma::mma_bf16(tm + 128, desc(S.xt, 2048, kk), desc(S.xt, 2048, kk),
+                                       umma::idesc_bf16(128, kGramN), gram_started || kk > 0);
+                }
+                gram_started = true;
+                gram_pending = true;
+            } else if (mma) {
+                umma::fence_before_sync();
+                __syncthreads();  // h1 tiles and accumulators are reused by the next tile
+            }
         }
-        if (!live) continue;
-        v *= c.disc;
-        if (last) welford_add(w, v);
-        else cf[c.cf_offset + i] = v;
+        if (last) {  // one final partial per chunk, fixed tree
+            Welford r = welford_warp_reduce(w);
+            if ((s & 31) == 0) swf[warp] = r;
+            __syncthreads();
+            if (s == 0) final_part[c.chunk_begin + ch] = welford_merge(welford_merge(swf[0], swf[1]), welford_merge(swf[2], swf[3]));
+            __syncthreads();
+            w = Welford{0ull, 0.0, 0.0};
+        }
     }
-    if (exercise) {
-        if (!ok) umma::mbar_wait(&S.mbar, phase, err, 6);
+    if (mma) {
+        if (gram_pending) {
+            if (s == 0) umma::mma_commit(&S.mbar);
+            ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 12));
+            phase ^= 1u;
+            umma::fence_after_sync();
+        }
+        if (gram) {
+            float* out = gram_part + static_cast<size_t>(g) * kGramPacked;
+            if (warp < 3) {  // lanes 0..95 hold rows 0..95; the upper triangle of rows 0..65 is kept
+                const int row0 = s * kGramDim - s * (s - 1) / 2;  // packed index of (s, s)
+                for (int cc = 0; cc < 5; ++cc) {
+                    float dd[16];
+                    umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 128 + cc * 16), dd);
+                    if (s < kGramDim)
+                        for (int q = 0; q < 16; ++q) {
+                            const int col = cc * 16 + q;
+                            if (col >= s && col < kGramDim) out[row0 + col - s] = ok ? dd[q] : 0.0f;
+                        }
+                }
+            }
+        }
+        if (!ok) umma::mbar_wait(&S.mbar, phase, err, 13);
         umma::fence_before_sync();
         __syncthreads();
-        if (warp == 0) umma::tmem_dealloc(tm, 64);
+        if (warp == 0) umma::tmem_dealloc(tm, 256);
     }
-    if (last) {
-        w = welford_warp_reduce(w);
-        if ((s & 31) == 0) swf[warp] = w;
+}
+
+// ---------------------------------------------------------------------------
+// output layer of date d = n - k - 1: ridge least squares on the Gram matrix
+//
+// The 64 GELU features are smooth functions of one state variable and are
+// strongly collinear, and the Gram matrix is accumulated in FP32 by the
+// tensor cores, so it is only positive semi-definite to a small fraction of
+// its diagonal.  The regressors are therefore scaled to unit diagonal and a
+// ridge of kRidge is added in those units; a pivot that still falls below
+// half the ridge drops its regressor (coefficient 0) instead of failing the
+// date.  FP64 is slow on this part, so the group partials are summed in FP32
+// with compensation (lsm_mlp_gram_reduce), the 65 x 65 Cholesky factor is
+// computed in FP32 (every thread keeps its share of the triangle in
+// registers; one barrier per column), and two steps of iterative refinement
+// with FP64 residuals bring the solution to FP64 accuracy for the
+// ridge-bounded condition number.
+//
+// snap_ok of the date: 1 = fitted, 2 = fewer than 4 in-the-money paths (no
+// exercise at this date, as src/pricers/lsm.cpp does), 0 = failed.
+// ---------------------------------------------------------------------------
+constexpr double kRidge = 1e-3;
+constexpr int kSolveThreads = 256;
+constexpr int kM = kGramDim - 1;                                      // 65 regressors (64 features + bias)
+constexpr int kTri = kM * (kM + 1) / 2;                               // lower triangle of the 65 x 65 system
+constexpr int kOwn = (kTri + kSolveThreads - 1) / kSolveThreads;      // triangle entries per thread
+
+__device__ __forceinline__ int packed_index(int r, int q) {  // r <= q
+    return r * kGramDim - r * (r - 1) / 2 + (q - r);
+}
+
+// Sum of the group partials of every contract: one thread per packed entry,
+// a fixed-order compensated (Kahan) FP32 sum over the groups (loads issued
+// eight at a time), stored as the FP64 value sum - compensation.
+__global__ void __launch_bounds__(128)
+    lsm_mlp_gram_reduce(int k, const LsmDev* __restrict__ cs, int n_contracts, const float* __restrict__ gram_part,
+                        double* __restrict__ gram_sum) {
+    const int idx = blockIdx.x * 128 + threadIdx.x;
+    if (idx >= kGramPacked) return;
+    for (int ci = blockIdx.y; ci < n_contracts; ci += gridDim.y) {
+        const LsmDev c = cs[ci];
+        if (c.n_steps - k - 1 < 1) continue;
+        const float* base = gram_part + static_cast<size_t>(c.group_begin) * kGramPacked + idx;
+        float sum = 0.0f, comp = 0.0f;
+        auto add = [&](float v) {
+            const float y = __fsub_rn(v, comp);
+            const float t = __fadd_rn(sum, y);
+            comp = __fsub_rn(__fsub_rn(t, sum), y);
+            sum = t;
+        };
+        uint32_t gg = 0;
+        for (; gg + 8 <= c.n_groups; gg += 8) {
+            float v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = base[static_cast<size_t>(gg + u) * kGramPacked];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) add(v[u]);
+        }
+        for (; gg < c.n_groups; ++gg) add(base[static_cast<size_t>(gg) * kGramPacked]);
+        gram_sum[static_cast<size_t>(ci) * kGramPacked + idx] = static_cast<double>(sum) - static_cast<double>(comp);
+    }
+}
+
+// x = L^-T L^-1 b for the FP32 factor L (lower, row stride kGramDim,
+// reciprocal diagonal in inv_diag), by one warp on shared vectors: b is
+// overwritten, the solution lands in x.  Dropped regressors give 0 (their
+// inv_diag is 0).
+__device__ void chol_solve_warp(const float* L, const float* inv_diag, float* b, float* z, float* x, int lane) {
+    for (int i = 0; i < kM; ++i) {  // L z = b, column by column
+        __syncwarp();
+        const float zi = b[i] * inv_diag[i];
+        if (lane == 0) z[i] = zi;
+        for (int r = i + 1 + lane; r < kM; r += 32) b[r] = __fmaf_rn(-L[r * kGramDim + i], zi, b[r]);
+    }
+    for (int i = kM - 1; i >= 0; --i) {  // L^T x = z
+        __syncwarp();
+        const float xi = z[i] * inv_diag[i];
+        if (lane == 0) x[i] = xi;
+        for (int r = lane; r < i; r += 32) z[r] = __fmaf_rn(-L[i * kGramDim + r], xi, z[r]);
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(kSolveThreads)
+    lsm_mlp_solve(int k, const LsmDev* __restrict__ cs, int n_contracts, const double* __restrict__ gram_sum,
+                  float* __restrict__ nets, float* __restrict__ snaps, int* __restrict__ snap_ok) {
+    __shared__ double G[kGramPacked];   // Gram matrix, packed upper triangle; standardised in place
+    __shared__ float L[kM * kGramDim];  // FP32 Cholesky factor (lower)
+    __shared__ float col[2][kM];        // column j of the partially reduced matrix (double-buffered)
+    __shared__ float inv_diag[kM];
+    __shared__ float vb[kM], vz[kM], vx[kM];
+    __shared__ double sc[kM], xs[kM], res[kM];
+    __shared__ int bad;
+    const int ci = blockIdx.x;
+    if (ci >= n_contracts) return;
+    const LsmDev c = cs[ci];
+    const int d = c.n_steps - k - 1;
+    if (d < 1) return;
+    const int s = threadIdx.x, lane = s & 31, warp = s >> 5;
+    for (int idx = s; idx < kGramPacked; idx += kSolveThreads) G[idx] = gram_sum[static_cast<size_t>(ci) * kGramPacked + idx];
+    if (s == 0) bad = 0;
+    __syncthreads();
+    const double count = G[packed_index(64, 64)];
+    if (!(count >= 4.0)) {
+        if (s == 0) snap_ok[c.reg_offset + d] = 2;
+        return;
+    }
+    if (s < kM) {
+        const double a = G[packed_index(s, s)];
+        sc[s] = a > 0.0 ? 1.0 / sqrt(a) : 0.0;  // a feature that is zero on every path gets coefficient 0
+    }
+    __syncthreads();
+    // Owned entries (r, q), q <= r, of the lower triangle, standardised, in
+    // registers; the packed FP64 copy is standardised too (for residuals).
+    int own_r[kOwn], own_q[kOwn];
+    float a[kOwn];
+#pragma unroll
+    for (int u = 0; u < kOwn; ++u) {
+        const int e = s + kSolveThreads * u;
+        own_r[u] = -1;
+        own_q[u] = -1;
+        a[u] = 0.0f;
+        if (e < kTri) {
+            int r = static_cast<int>((sqrtf(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
+            while (r * (r + 1) / 2 > e) --r;
+            while ((r + 1) * (r + 2) / 2 <= e) ++r;
+            const int q = e - r * (r + 1) / 2;
+            const int pi = packed_index(q, r);
+            double v = G[pi] * sc[r] * sc[q];
+            if (q == r) v = (sc[r] > 0.0 ? 1.0 : 0.0) + kRidge;
+            G[pi] = v;
+            own_r[u] = r;
+            own_q[u] = q;
+            a[u] = static_cast<float>(v);
+        }
+    }
+    if (s < kM) G[packed_index(s, 65)] *= sc[s];  // right-hand side
+    // right-looking Cholesky in FP32 on the owned entries, one barrier per column
+    for (int j = 0; j < kM; ++j) {
+        float* cj = col[j & 1];
+#pragma unroll
+        for (int u = 0; u < kOwn; ++u)
+            if (own_q[u] == j) cj[own_r[u]] = a[u];
         __syncthreads();
-        if (s == 0) final_part[chunk] = welford_merge(welford_merge(swf[0], swf[1]), welford_merge(swf[2], swf[3]));
+        const float dj = cj[j];
+        const bool drop = !(dj >= static_cast<float>(0.5 * kRidge));
+        const float inv = drop ? 0.0f : rsqrtf(dj);
+#pragma unroll
+        for (int u = 0; u < kOwn; ++u) {
+            const int r = own_r[u], q = own_q[u];
+            if (q > j) a[u] = __fmaf_rn(-(cj[r] * inv), cj[q] * inv, a[u]);
+            else if (q == j) L[r * kGramDim + j] = r == j ? (drop ? 1.0f : dj * inv) : cj[r] * inv;
+        }
+        if (s == 0) inv_diag[j] = inv;  // 1 / L[j][j], 0 when the regressor is dropped
     }
+    __syncthreads();
+    // solve, then refinement with FP64 residuals r = b - A x
+    if (s < kM) xs[s] = 0.0;
+    if (s < kM) res[s] = G[packed_index(s, 65)];
+    __syncthreads();
+    for (int it = 0; it < 3; ++it) {
+        if (warp == 0) {
+            for (int i = lane; i < kM; i += 32) vb[i] = static_cast<float>(res[i]);
+            chol_solve_warp(L, inv_diag, vb, vz, vx, lane);
+            for (int i = lane; i < kM; i += 32) xs[i] += static_cast<double>(vx[i]);
+        }
+        __syncthreads();
+        if (it == 2) break;
+        for (int i = warp; i < kM; i += kSolveThreads / 32) {  // one warp per row
+            double acc = 0.0;
+            for (int j = lane; j < kM; j += 32)
+                if (inv_diag[j] != 0.0f) acc += G[i <= j ? packed_index(i, j) : packed_index(j, i)] * xs[j];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) res[i] = inv_diag[i] != 0.0f ? G[packed_index(i, 65)] - acc : 0.0;
+        }
+        __syncthreads();
+    }
+    if (s < kM) {
+        const double b = inv_diag[s] != 0.0f ? xs[s] * sc[s] : 0.0;
+        res[s] = b;  // beta
+        if (!(fabs(b) <= 1e30)) atomicOr(&bad, 1);  // also catches NaN
+    }
+    __syncthreads();
+    // snapshot of date d: current features + fitted output layer
+    float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
+    float* snap = snaps + (static_cast<size_t>(c.reg_offset) + d) * kParamStride;
+    const bool ok = bad == 0;
+    for (int i = s; i < kParamStride; i += kSolveThreads) {
+        float val = net[i];
+        if (ok) {
+            if (i >= kW3 && i < kB3) val = static_cast<float>(res[i - kW3]);
+            else if (i == kB3) val = static_cast<float>(res[64]);
+        }
+        snap[i] = val;
+        if (ok && i >= kW3 && i <= kB3) net[i] = val;  // fine-tuning continues from the fit
+    }
+    if (s == 0) snap_ok[c.reg_offset + d] = ok ? 1 : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -667,33 +982,51 @@ cudaError_t mlp_prepare() {
     cudaError_t e = set_smem(lsm_mlp_train<0>, sizeof(TrainSmem));
     if (e == cudaSuccess) e = set_smem(lsm_mlp_train<1>, sizeof(TrainSmem));
     if (e == cudaSuccess) e = set_smem(mlp_grad_kernel, sizeof(TrainSmem));
-    if (e == cudaSuccess) e = set_smem(lsm_mlp_exercise<0>, sizeof(InferSmem));
-    if (e == cudaSuccess) e = set_smem(lsm_mlp_exercise<1>, sizeof(InferSmem));
+    if (e == cudaSuccess) e = set_smem(lsm_mlp_pass<0>, sizeof(PassSmem));
+    if (e == cudaSuccess) e = set_smem(lsm_mlp_pass<1>, sizeof(PassSmem));
     if (e == cudaSuccess) e = set_smem(mlp_forward_kernel, sizeof(InferSmem));
     return e;
 }
 
 cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int n_contracts,
-                                     const uint32_t* chunk_contract, uint32_t total_chunks, const void* store,
+                                     const uint32_t* group_contract, uint32_t total_groups, const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
-                                     const MlpConfig& cfg, Welford* final_part, uint32_t* err,
-                                     cudaStream_t stream) {
+                                     float* gram_part, double* gram_sum, const MlpConfig& cfg, Welford* final_part,
+                                     uint32_t* err, cudaStream_t stream) {
     cudaGetLastError();
-    if (total_chunks == 0) return cudaSuccess;
-    if (precision == 0)
-        lsm_mlp_exercise<0><<<total_chunks, 128, sizeof(InferSmem), stream>>>(k, c, chunk_contract, total_chunks,
-                                                                             store, cf, snaps, snap_ok, final_part, err);
-    else
-        lsm_mlp_exercise<1><<<total_chunks, 128, sizeof(InferSmem), stream>>>(k, c, chunk_contract, total_chunks,
-                                                                             store, cf, snaps, snap_ok, final_part, err);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess || !train) return e;
-    if (precision == 0)
-        lsm_mlp_train<0><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, n_contracts, store, cf, nets, snaps,
-                                                                          snap_ok, adam_t, cfg, err);
-    else
-        lsm_mlp_train<1><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, n_contracts, store, cf, nets, snaps,
-                                                                          snap_ok, adam_t, cfg, err);
+    if (total_groups == 0) return cudaSuccess;
+    const size_t pass_smem = sizeof(PassSmem);
+    auto pass = [&](int mode) {
+        if (precision == 0)
+            lsm_mlp_pass<0><<<total_groups, 128, pass_smem, stream>>>(k, mode, c, group_contract, total_groups, store,
+                                                                      cf, nets, snaps, snap_ok, gram_part, final_part, err);
+        else
+            lsm_mlp_pass<1><<<total_groups, 128, pass_smem, stream>>>(k, mode, c, group_contract, total_groups, store,
+                                                                      cf, nets, snaps, snap_ok, gram_part, final_part, err);
+    };
+    auto trainer = [&]() {
+        if (precision == 0)
+            lsm_mlp_train<0><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, n_contracts, store, cf, nets, snaps,
+                                                                              snap_ok, adam_t, cfg, err);
+        else
+            lsm_mlp_train<1><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, n_contracts, store, cf, nets, snaps,
+                                                                              snap_ok, adam_t, cfg, err);
+    };
+    if (!train) {
+        pass(kStep);
+        return cudaGetLastError();
+    }
+    if (k == 0) {
+        pass(kStep);                 // terminal cash flows, first discount
+        trainer();                   // learn the features on the latest date
+        pass(kGram);                 // Gram matrix of that date
+    } else {
+        pass(kStep | kGram);         // exercise at date e, discount, Gram of date e-1
+    }
+    const dim3 rgrid((kGramPacked + 127) / 128, static_cast<unsigned>(n_contracts < 65535 ? n_contracts : 65535));
+    lsm_mlp_gram_reduce<<<rgrid, 128, 0, stream>>>(k, c, n_contracts, gram_part, gram_sum);
+    lsm_mlp_solve<<<n_contracts, kSolveThreads, 0, stream>>>(k, c, n_contracts, gram_sum, nets, snaps, snap_ok);
+    if (k > 0 && cfg.steps > 0) trainer();  // optional fine-tuning of the features
     return cudaGetLastError();
 }
 

@@ -13,7 +13,7 @@ namespace mcdg {
 // Training schedule of the continuation network (per contract, per date).
 struct MlpConfig {
     int steps_first;  // Adam steps at the first (latest) exercise date, from the initial weights
-    int steps;        // Adam steps at every earlier date, warm-started from the later date
+    int steps;        // Adam steps at every earlier date (feature fine-tuning; 0 = features fixed)
     float lr_first;
     float lr;
 };
@@ -21,13 +21,14 @@ struct MlpConfig {
 size_t mlp_train_smem_bytes();
 size_t mlp_infer_smem_bytes();
 cudaError_t mlp_prepare();  // opts the kernels into their dynamic shared memory
-// One backward iteration: exercise with the network of date n-k, discount,
-// then (train = true) train the network of date n-k-1 (one CTA per contract).
+// One backward iteration k: exercise at date n-k with that date's network,
+// discount, and (train = true) the Gram matrix and output-layer fit of date
+// n-k-1; at k = 0 the features are first trained on that date.
 cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int n_contracts,
-                                     const uint32_t* chunk_contract, uint32_t total_chunks, const void* store,
+                                     const uint32_t* group_contract, uint32_t total_groups, const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
-                                     const MlpConfig& cfg, Welford* final_part, uint32_t* err,
-                                     cudaStream_t stream);
+                                     float* gram_part, double* gram_sum, const MlpConfig& cfg, Welford* final_part,
+                                     uint32_t* err, cudaStream_t stream);
 cudaError_t launch_mlp_grad(const float* params, const float* x0, const float* x1, const float* y, const float* w,
                             int n, float* grad, float* loss, uint32_t* err, cudaStream_t stream);
 cudaError_t launch_mlp_forward(const float* params, const float* x0, const float* x1, int n, float* out,

@@ -270,12 +270,19 @@ int mcd_lsm_batch(mcd_ctx* ctx, const mcd_lsm_contract* contracts, size_t n, int
 
 /* Learned regression (MCD_LSM_MLP).  No counterpart in the reference: it
  * replaces the Laguerre least-squares fit of src/pricers/lsm.cpp:88-108 by a
- * 2 -> 64 -> 64 -> 1 GELU network of (4 (S/K - 1), tau/T) trained at every
- * exercise date on in-the-money paths (Adam, BF16 tensor-core GEMMs with FP32
- * accumulation), warm-started from the later date.  A contract whose training
- * produced non-finite weights is priced by the QR regression instead
- * (mcd_lsm_result.reserved = 1).  Schedule: steps_first Adam steps of 128
- * samples at the latest date, steps at each earlier date. */
+ * 2 -> 64 -> 64 -> 1 GELU network of (4 (S/K - 1), tau/T).  The network is
+ * trained on the GPU (Adam on 128-sample tiles of in-the-money paths,
+ * BF16 tensor-core forward/backward with FP32 accumulation) at the latest
+ * exercise date; its 64 hidden features plus a bias are then the regression
+ * basis at every date, whose output layer is fitted by ridge least squares
+ * over all in-the-money paths of that date (tensor-core Gram matrix, ridge
+ * 1e-3 in unit-diagonal scaling).  Target and decision: the time value
+ * (continuation - exercise)/K; exercise where it is predicted negative.  A
+ * date with fewer than 4 in-the-money paths has no exercise; a contract whose
+ * fit produced non-finite weights is priced by the QR regression instead
+ * (mcd_lsm_result.reserved = 1).  Schedule: steps_first Adam steps at the
+ * latest date (default 300, learning rate lr_first), steps at each earlier
+ * date (default 0: features fixed, learning rate lr). */
 int mcd_lsm_set_mlp_config(mcd_ctx* ctx, int steps_first, int steps, double lr_first, double lr);
 /* Networks of contract `contract` of the last learned run:
  * weights (monitoring_points+1) x 4417 floats (layout: W1[64][2], b1[64],
