@@ -73,6 +73,7 @@ Ctx::~Ctx() {
     for (auto& g : graphs) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
     }
+    if (greeks_graph) cudaGraphExecDestroy(greeks_graph);
     for (DeviceBuffer* b : {&d_contracts, &d_prefix, &d_partials, &d_results, &d_scratch, &d_scratch2}) {
         if (b->ptr) cudaFree(b->ptr);
     }
@@ -88,7 +89,9 @@ Ctx::~Ctx() {
 
 }  // namespace mcdg
 
-namespace {
+// Planning and graph helpers, shared with the other modules through
+// context.hpp (greeks_api.cpp builds its batches with them).
+namespace mcdg {
 
 bool finite_all(std::initializer_list<double> xs) {
     for (double x : xs)
@@ -358,7 +361,7 @@ int price_batch_host(Ctx& ctx, const mcd_contract* contracts, size_t n, int prec
     return collect_after_sync(ctx);
 }
 
-}  // namespace
+}  // namespace mcdg
 
 // ---------------------------------------------------------------------------
 // C ABI

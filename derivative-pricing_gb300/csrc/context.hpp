@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "engine.hpp"
+#include "mcd_gpu.h"
 
 namespace mcdg {
 
@@ -92,7 +93,12 @@ struct Ctx {
 
     // State owned by the other modules (Heston, LSM, QMC, Greeks); freed by
     // release_extensions().
-    DeviceBuffer ext[24];
+    DeviceBuffer ext[32];
+
+    // Sensitivity engine (greeks_api.cpp): launch shape and the last graph.
+    LaunchShape greeks_shape[2];
+    cudaGraphExec_t greeks_graph = nullptr;
+    GraphKey greeks_key{};
 
     // Training schedule of the learned LSM regression (mcd_lsm_set_mlp_config).
     int mlp_steps_first = 300;
@@ -110,6 +116,12 @@ struct Ctx {
     void release_extensions();
     ~Ctx();
 };
+
+// Batch planning and execution of the path engine (context.cpp).
+int plan_contract(Ctx& ctx, const mcd_contract& in, uint32_t index, DevContract& out);
+int plan_batch(Ctx& ctx, const mcd_contract* contracts, size_t n, BatchPlan& plan);
+int price_batch_host(Ctx& ctx, const mcd_contract* contracts, size_t n, int precision,
+                     mcd_mc_result* results);
 
 }  // namespace mcdg
 

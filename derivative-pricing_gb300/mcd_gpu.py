@@ -100,6 +100,39 @@ RESULT_DTYPE = np.dtype([("price", "<f8"), ("standard_error", "<f8"), ("path_cou
 assert CONTRACT_DTYPE.itemsize == 128 and RESULT_DTYPE.itemsize == 24
 
 
+GREEK_NAMES = ("price", "fd_delta", "fd_gamma", "fd_vega", "pathwise_delta", "pathwise_vega",
+               "pathwise_rho", "lr_delta", "lr_gamma", "lr_vega", "lr_rho", "lr_theta")
+# numpy mirror of mcd_greeks_result: (value, standard_error) per Greek, path count, defined bits.
+GREEKS_DTYPE = np.dtype([(n, "<f8", (2,)) for n in GREEK_NAMES] +
+                        [("path_count", "<u8"), ("defined", "<u4"), ("reserved", "<u4")])
+assert GREEKS_DTYPE.itemsize == 208
+
+
+class Greek(C.Structure):
+    """mcd_greek (= LrGreeksResult / PathwiseGreeksResult)."""
+    _fields_ = [("value", dbl), ("standard_error", dbl)]
+
+    def __repr__(self):
+        return f"Greek(value={self.value!r}, standard_error={self.standard_error!r})"
+
+
+class EuropeanGreeks(C.Structure):
+    _fields_ = [(n, dbl) for n in ("delta", "gamma", "vega", "theta", "rho")]
+
+
+class BumpSizes(C.Structure):
+    _fields_ = [(n, dbl) for n in ("spot", "vol", "rate", "time")]
+
+
+class LrGreeks(C.Structure):
+    _fields_ = [(n, Greek) for n in ("delta", "gamma", "vega", "rho", "theta")] + \
+               [("has_theta", C.c_int32), ("reserved", C.c_int32)]
+
+
+class PathwiseGreeks(C.Structure):
+    _fields_ = [(n, Greek) for n in ("delta", "vega", "rho")]
+
+
 class McdError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{STATUS.get(status, status)}: {message}")
@@ -161,6 +194,16 @@ def lib():
     sig("mcd_umma_selftest", vp, F, F, F)
     sig("mcd_mlp_gradients", vp, F, F, F, F, F, i32, F, F)
     sig("mcd_mlp_forward", vp, F, F, F, C.c_size_t, F)
+    sig("mcd_greeks_batch", vp, vp, C.c_size_t, dbl, dbl, i32, vp)
+    sig("mcd_greeks_set_launch_shape", vp, i32, i32, i32)
+    sig("mcd_greeks_autotune", vp, vp, C.c_size_t, dbl, dbl, i32, P(i32), P(i32), P(dbl))
+    sig("mcd_default_bump_sizes", dbl, dbl, dbl, res=BumpSizes)
+    sig("mcd_fd_european", vp, *D6, i32, u64, u64, BumpSizes, i32, P(EuropeanGreeks))
+    sig("mcd_lr_european", vp, *D6, i32, u64, u64, i32, P(LrGreeks))
+    sig("mcd_lr_digital", vp, *D6, i32, dbl, u64, u64, i32, P(LrGreeks))
+    sig("mcd_lr_barrier", vp, *([dbl] * 7), i32, i32, i32, dbl, i32, u64, u64, i32, P(LrGreeks))
+    sig("mcd_pathwise_european", vp, *D6, i32, u64, u64, i32, P(PathwiseGreeks))
+    sig("mcd_pathwise_asian", vp, *D6, i32, i32, i32, i32, u64, u64, i32, P(PathwiseGreeks))
     sig("mcd_philox", vp, P(u32), P(u32), C.c_size_t, P(u32))
     sig("mcd_draws", vp, u64, u64, u64, u32, u32, i32, i32, P(dbl))
     sig("mcd_kernel_timing", vp, i32, P(dbl), P(u64))
@@ -409,6 +452,85 @@ class Engine:
         return ms.value, n.value
 
     # -- draws -----------------------------------------------------------------------------
+    # -- Greeks ----------------------------------------------------------------------------
+    def greeks_batch(self, contracts: np.ndarray, spot_bump_rel=1e-4, vol_bump_rel=1e-4,
+                     precision="fp32") -> np.ndarray:
+        """Price, CRN finite-difference, pathwise and likelihood-ratio Greeks of every contract
+        in one launch (mcd_greeks_batch); returns a GREEKS_DTYPE array."""
+        contracts = np.ascontiguousarray(contracts, dtype=CONTRACT_DTYPE)
+        out = np.zeros(len(contracts), dtype=GREEKS_DTYPE)
+        self._check(self._lib.mcd_greeks_batch(self.handle, contracts.ctypes.data, len(contracts),
+                                               spot_bump_rel, vol_bump_rel, _prec(precision),
+                                               out.ctypes.data))
+        return out
+
+    def set_greeks_launch_shape(self, precision, variant: int, ctas_per_sm: int):
+        self._check(self._lib.mcd_greeks_set_launch_shape(self.handle, _prec(precision), variant,
+                                                          ctas_per_sm))
+
+    def greeks_autotune(self, contracts: np.ndarray, spot_bump_rel=1e-4, vol_bump_rel=1e-4,
+                        precision="fp32"):
+        contracts = np.ascontiguousarray(contracts, dtype=CONTRACT_DTYPE)
+        v, c, ms = i32(), i32(), dbl()
+        self._check(self._lib.mcd_greeks_autotune(self.handle, contracts.ctypes.data, len(contracts),
+                                                  spot_bump_rel, vol_bump_rel, _prec(precision),
+                                                  C.byref(v), C.byref(c), C.byref(ms)))
+        return v.value, c.value, ms.value
+
+    def default_bump_sizes(self, spot, vol, time) -> BumpSizes:
+        return self._lib.mcd_default_bump_sizes(spot, vol, time)
+
+    def finite_difference_european(self, spot, strike, rate, carry_yield, vol, time, type,
+                                   path_count, seed, bumps=None, precision="fp64") -> EuropeanGreeks:
+        b = bumps if bumps is not None else self.default_bump_sizes(spot, vol, time)
+        out = EuropeanGreeks()
+        self._check(self._lib.mcd_fd_european(self.handle, spot, strike, rate, carry_yield, vol, time,
+                                              type, path_count, seed, b, _prec(precision),
+                                              C.byref(out)))
+        return out
+
+    def likelihood_ratio_european(self, spot, strike, rate, carry_yield, vol, time, type,
+                                  path_count, seed, precision="fp64") -> LrGreeks:
+        out = LrGreeks()
+        self._check(self._lib.mcd_lr_european(self.handle, spot, strike, rate, carry_yield, vol, time,
+                                              type, path_count, seed, _prec(precision), C.byref(out)))
+        return out
+
+    def likelihood_ratio_digital(self, spot, strike, rate, carry_yield, vol, time, type,
+                                 cash_amount, path_count, seed, precision="fp64") -> LrGreeks:
+        out = LrGreeks()
+        self._check(self._lib.mcd_lr_digital(self.handle, spot, strike, rate, carry_yield, vol, time,
+                                             type, cash_amount, path_count, seed, _prec(precision),
+                                             C.byref(out)))
+        return out
+
+    def likelihood_ratio_barrier(self, spot, strike, barrier, rate, carry_yield, vol, time, type,
+                                 direction, knock, rebate, monitoring_points, path_count, seed,
+                                 precision="fp64") -> LrGreeks:
+        out = LrGreeks()
+        self._check(self._lib.mcd_lr_barrier(self.handle, spot, strike, barrier, rate, carry_yield, vol,
+                                             time, type, direction, knock, rebate, monitoring_points,
+                                             path_count, seed, _prec(precision), C.byref(out)))
+        return out
+
+    def pathwise_european(self, spot, strike, rate, carry_yield, vol, time, type, path_count, seed,
+                          precision="fp64") -> PathwiseGreeks:
+        out = PathwiseGreeks()
+        self._check(self._lib.mcd_pathwise_european(self.handle, spot, strike, rate, carry_yield, vol,
+                                                    time, type, path_count, seed, _prec(precision),
+                                                    C.byref(out)))
+        return out
+
+    def pathwise_asian(self, spot, strike, rate, carry_yield, vol, time, type, strike_style,
+                       average_style, monitoring_points, path_count, seed,
+                       precision="fp64") -> PathwiseGreeks:
+        out = PathwiseGreeks()
+        self._check(self._lib.mcd_pathwise_asian(self.handle, spot, strike, rate, carry_yield, vol,
+                                                 time, type, strike_style, average_style,
+                                                 monitoring_points, path_count, seed,
+                                                 _prec(precision), C.byref(out)))
+        return out
+
     def philox(self, counters: np.ndarray, keys: np.ndarray) -> np.ndarray:
         counters = np.ascontiguousarray(counters, dtype=np.uint32).reshape(-1, 4)
         keys = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 2)

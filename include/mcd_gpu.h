@@ -305,6 +305,100 @@ int mcd_mlp_gradients(mcd_ctx* ctx, const float* params, const float* x0, const 
 int mcd_mlp_forward(mcd_ctx* ctx, const float* params, const float* x0, const float* x1, size_t n,
                     float* out);
 
+/* ---- Greeks --------------------------------------------------------------- */
+/* mcd::greeks::LrGreeksResult / PathwiseGreeksResult
+ * (include/mcd/greeks/likelihood_ratio.hpp:15-18, pathwise.hpp:14-17). */
+typedef struct {
+    double value;
+    double standard_error;
+} mcd_greek;
+
+/* Sensitivities of one contract from mcd_greeks_batch.  Bit i of `defined`
+ * is set when field i (in declaration order, price = bit 0) is defined for
+ * the product: price and the finite differences always; pathwise for European
+ * and Asian (src/greeks/pathwise.cpp); likelihood ratio delta/gamma/vega/rho
+ * always (European and digital as likelihood_ratio.cpp:33-73, every
+ * path-dependent product with the barrier's first-step score :105-154, which
+ * the reference applies to barriers only); likelihood-ratio theta for European
+ * and digital. */
+typedef struct {
+    mcd_greek price;
+    mcd_greek fd_delta, fd_gamma, fd_vega;
+    mcd_greek pathwise_delta, pathwise_vega, pathwise_rho;
+    mcd_greek lr_delta, lr_gamma, lr_vega, lr_rho, lr_theta;
+    uint64_t path_count;
+    uint32_t defined;
+    uint32_t reserved;
+} mcd_greeks_result;
+
+/* Batched risk: price, common-random-number finite-difference delta, gamma
+ * and vega (central differences with bumps spot_bump_rel * spot and
+ * vol_bump_rel * vol, as finite_difference.cpp:40-65 re-prices with the same
+ * seed), pathwise and likelihood-ratio Greeks of every contract, in one
+ * persistent launch (a CUDA graph of the sensitivity kernel and its merge).
+ * Every estimate is the mean of a per-path quantity and comes with its
+ * standard error.  The price equals mcd_price_batch's bit for bit.
+ * Unsupported: antithetic pairing, the control-variate Asian and the
+ * Brownian-bridge barrier (MCD_ERR_UNSUPPORTED).  The spot-down and vol-down
+ * states must stay positive (bumps < 1). */
+int mcd_greeks_batch(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, double spot_bump_rel,
+                     double vol_bump_rel, int precision, mcd_greeks_result* results);
+/* Launch shape of the sensitivity kernel (variant 0..1: register budget for
+ * 2 or 4 resident CTAs; ctas_per_sm 0 = occupancy limit) and its tuner, which
+ * times every candidate on the given batch and keeps the fastest. */
+int mcd_greeks_set_launch_shape(mcd_ctx* ctx, int precision, int variant, int ctas_per_sm);
+int mcd_greeks_autotune(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, double spot_bump_rel,
+                        double vol_bump_rel, int precision, int* variant, int* ctas_per_sm,
+                        double* best_ms);
+
+/* mcd::greeks::EuropeanGreeks and BumpSizes (finite_difference.hpp:9-22). */
+typedef struct {
+    double delta, gamma, vega, theta, rho;
+} mcd_european_greeks;
+typedef struct {
+    double spot, vol, rate, time;
+} mcd_bump_sizes;
+/* replaces mcd::greeks::default_bump_sizes (src/greeks/finite_difference.cpp:23-38) */
+mcd_bump_sizes mcd_default_bump_sizes(double spot, double vol, double time);
+/* replaces mcd::greeks::finite_difference_european (finite_difference.cpp:40-65):
+ * the nine common-random-number re-prices run as one batch launch. */
+int mcd_fd_european(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                    double vol, double time, int type, uint64_t path_count, uint64_t seed,
+                    mcd_bump_sizes bumps, int precision, mcd_european_greeks* out);
+
+/* mcd::greeks::LrGreeks (likelihood_ratio.hpp:20-29); has_theta = 0 where
+ * the reference leaves theta empty (barrier). */
+typedef struct {
+    mcd_greek delta, gamma, vega, rho, theta;
+    int32_t has_theta;
+    int32_t reserved;
+} mcd_lr_greeks;
+/* replace mcd::greeks::likelihood_ratio_european / _digital (cash-or-nothing)
+ * / _barrier (src/greeks/likelihood_ratio.cpp:75-154) */
+int mcd_lr_european(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                    double vol, double time, int type, uint64_t path_count, uint64_t seed,
+                    int precision, mcd_lr_greeks* out);
+int mcd_lr_digital(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                   double vol, double time, int type, double cash_amount, uint64_t path_count,
+                   uint64_t seed, int precision, mcd_lr_greeks* out);
+int mcd_lr_barrier(mcd_ctx* ctx, double spot, double strike, double barrier, double rate,
+                   double carry_yield, double vol, double time, int type, int direction, int knock,
+                   double rebate, int monitoring_points, uint64_t path_count, uint64_t seed,
+                   int precision, mcd_lr_greeks* out);
+
+/* mcd::greeks::PathwiseGreeks (pathwise.hpp:23-25). */
+typedef struct {
+    mcd_greek delta, vega, rho;
+} mcd_pathwise_greeks;
+/* replace mcd::greeks::pathwise_european / pathwise_asian (src/greeks/pathwise.cpp:28-147) */
+int mcd_pathwise_european(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                          double vol, double time, int type, uint64_t path_count, uint64_t seed,
+                          int precision, mcd_pathwise_greeks* out);
+int mcd_pathwise_asian(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                       double vol, double time, int type, int strike_style, int average_style,
+                       int monitoring_points, uint64_t path_count, uint64_t seed, int precision,
+                       mcd_pathwise_greeks* out);
+
 /* ---- draws (parity and diagnostics) ------------------------------------- */
 /* Philox4x32-10 of n (counter, key) pairs; replaces mcd::philox4x32_10
  * (src/core/rng.cpp:41-47).  counters: n x 4, keys: n x 2, out: n x 4. */
