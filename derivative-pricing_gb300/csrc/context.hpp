@@ -93,7 +93,7 @@ struct Ctx {
 
     // State owned by the other modules (Heston, LSM, QMC, Greeks); freed by
     // release_extensions().
-    DeviceBuffer ext[32];
+    DeviceBuffer ext[40];
 
     // Sensitivity engine (greeks_api.cpp): launch shape and the last graph.
     LaunchShape greeks_shape[2];

@@ -187,10 +187,8 @@ __device__ __forceinline__ float fast_rcp(float x) {
 // its break point and loses ~4 digits in FP32, which is why it is not used
 // here.  Both branches are evaluated as one Horner chain with per-lane
 // coefficient selects, so a warp never diverges.
-__device__ __forceinline__ float normal_from_bits_f32(uint32_t bits) {
-    const bool upper = (bits >> 31) != 0u;
-    const uint32_t m = upper ? ~bits : bits;
-    const float q = __fmaf_rn(__uint2float_rn(m), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
+// Lower-half deviate Phi^-1(q) for q in (0, 1/2] (AS241 PPND7, see above).
+__device__ __forceinline__ float ppnd7_lower(float q) {
     const float t = q - 0.5f;                      // in [-0.5, 0]
     const bool central = t >= -0.425f;
     const float s = fast_sqrt(-__logf(q)) - 1.6f;  // tail variable (unused when central)
@@ -203,7 +201,23 @@ __device__ __forceinline__ float normal_from_bits_f32(uint32_t bits) {
     den = __fmaf_rn(den, v, central ? 7.8757757664e+01f : 1.2021132975e-01f);
     den = __fmaf_rn(den, v, central ? 1.7895169469e+01f : 7.3700164250e-01f);
     den = __fmaf_rn(den, v, 1.0f);
-    const float z = num * fast_rcp(den) * (central ? t : -1.0f);  // lower-half deviate
+    return num * fast_rcp(den) * (central ? t : -1.0f);
+}
+
+__device__ __forceinline__ float normal_from_bits_f32(uint32_t bits) {
+    const bool upper = (bits >> 31) != 0u;
+    const uint32_t m = upper ? ~bits : bits;
+    const float q = __fmaf_rn(__uint2float_rn(m), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
+    const float z = ppnd7_lower(q);
+    return upper ? -z : z;
+}
+
+// Standard normal of a Sobol coordinate u = x / 2^32 (x > 0), in FP32: the
+// mirror 1 - u = (2^32 - x) / 2^32 is formed exactly from the bits.
+__device__ __forceinline__ float normal_from_sobol_f32(uint32_t x) {
+    const bool upper = x > 0x80000000u;
+    const uint32_t m = upper ? (0u - x) : x;
+    const float z = ppnd7_lower(__uint2float_rn(m) * 2.3283064365386963e-10f);
     return upper ? -z : z;
 }
 

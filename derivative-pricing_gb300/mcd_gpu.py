@@ -204,6 +204,10 @@ def lib():
     sig("mcd_lr_barrier", vp, *([dbl] * 7), i32, i32, i32, dbl, i32, u64, u64, i32, P(LrGreeks))
     sig("mcd_pathwise_european", vp, *D6, i32, u64, u64, i32, P(PathwiseGreeks))
     sig("mcd_pathwise_asian", vp, *D6, i32, i32, i32, i32, u64, u64, i32, P(PathwiseGreeks))
+    sig("mcd_qmc_batch", vp, vp, C.c_size_t, i32, vp)
+    sig("mcd_qmc_sobol_european", vp, *D6, i32, u64, i32, P(dbl))
+    sig("mcd_qmc_sobol_asian", vp, *D6, i32, i32, i32, u64, i32, P(dbl))
+    sig("mcd_sobol_points", vp, C.c_uint, C.c_uint, u64, u64, P(dbl))
     sig("mcd_philox", vp, P(u32), P(u32), C.c_size_t, P(u32))
     sig("mcd_draws", vp, u64, u64, u64, u32, u32, i32, i32, P(dbl))
     sig("mcd_kernel_timing", vp, i32, P(dbl), P(u64))
@@ -529,6 +533,37 @@ class Engine:
                                                  time, type, strike_style, average_style,
                                                  monitoring_points, path_count, seed,
                                                  _prec(precision), C.byref(out)))
+        return out
+
+    # -- Sobol quasi-Monte Carlo ------------------------------------------------------------
+    def qmc_batch(self, contracts: np.ndarray, precision="fp64") -> np.ndarray:
+        """QMC prices (Sobol + Brownian bridge) of a batch; standard_error is 0."""
+        contracts = np.ascontiguousarray(contracts, dtype=CONTRACT_DTYPE)
+        out = np.zeros(len(contracts), dtype=RESULT_DTYPE)
+        self._check(self._lib.mcd_qmc_batch(self.handle, contracts.ctypes.data, len(contracts),
+                                            _prec(precision), out.ctypes.data))
+        return out
+
+    def qmc_sobol_european(self, spot, strike, rate, carry_yield, vol, time, type, path_count,
+                           precision="fp64") -> float:
+        p = dbl()
+        self._check(self._lib.mcd_qmc_sobol_european(self.handle, spot, strike, rate, carry_yield, vol,
+                                                     time, type, path_count, _prec(precision),
+                                                     C.byref(p)))
+        return p.value
+
+    def qmc_sobol_asian(self, spot, strike, rate, carry_yield, vol, time, type, strike_style,
+                        monitoring_points, path_count, precision="fp64") -> float:
+        p = dbl()
+        self._check(self._lib.mcd_qmc_sobol_asian(self.handle, spot, strike, rate, carry_yield, vol,
+                                                  time, type, strike_style, monitoring_points,
+                                                  path_count, _prec(precision), C.byref(p)))
+        return p.value
+
+    def sobol_points(self, dim_begin, n_dims, index_begin, n_indices) -> np.ndarray:
+        out = np.zeros((n_indices, n_dims), dtype=np.float64)
+        self._check(self._lib.mcd_sobol_points(self.handle, dim_begin, n_dims, index_begin, n_indices,
+                                               out.ctypes.data_as(P(dbl))))
         return out
 
     def philox(self, counters: np.ndarray, keys: np.ndarray) -> np.ndarray:

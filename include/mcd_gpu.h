@@ -399,6 +399,38 @@ int mcd_pathwise_asian(mcd_ctx* ctx, double spot, double strike, double rate, do
                        int monitoring_points, uint64_t path_count, uint64_t seed, int precision,
                        mcd_pathwise_greeks* out);
 
+/* ---- Sobol quasi-Monte Carlo ----------------------------------------------- */
+/* Dimensions of the Sobol generator: the reference's seven
+ * (src/core/sobol.cpp:22-30) followed by every further primitive polynomial
+ * in ascending (degree, coefficient bits) order, same initial direction
+ * numbers (m_i = 1) and recurrence.  Path-dependent contracts need
+ * monitoring_points <= this. */
+#define MCD_SOBOL_MAX_DIMS 256
+/* Quasi-Monte Carlo prices of a batch in one persistent launch: Sobol points
+ * at indices 1..path_count, Brownian-bridge paths with dimension k on the
+ * k-th breadth-first bisection point (src/models/brownian_bridge_path.cpp
+ * :20-77), mean of the discounted payoffs (src/pricers/qmc.cpp:15-57).  Every
+ * batch product is accepted (the reference covers the European and the
+ * arithmetic Asian); antithetic pairing, the control-variate Asian and the
+ * Brownian-bridge barrier are not (MCD_ERR_UNSUPPORTED).  standard_error is
+ * 0: a low-discrepancy sequence has none (include/mcd/pricers/qmc.hpp:9-15). */
+int mcd_qmc_batch(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, int precision,
+                  mcd_mc_result* results);
+/* replaces mcd::pricers::qmc_sobol_european (src/pricers/qmc.cpp:15-30) */
+int mcd_qmc_sobol_european(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                           double vol, double time, int type, uint64_t path_count, int precision,
+                           double* price);
+/* replaces mcd::pricers::qmc_sobol_asian (src/pricers/qmc.cpp:32-57); the
+ * reference caps monitoring_points at 7, this at MCD_SOBOL_MAX_DIMS. */
+int mcd_qmc_sobol_asian(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                        double vol, double time, int type, int strike_style, int monitoring_points,
+                        uint64_t path_count, int precision, double* price);
+/* Sobol coordinates of dims [dim_begin, dim_begin + n_dims) at indices
+ * [index_begin, index_begin + n_indices) from the device generator, row-major
+ * by index; mcd::sobol_point (src/core/sobol.cpp:83-97) for each. */
+int mcd_sobol_points(mcd_ctx* ctx, unsigned dim_begin, unsigned n_dims, uint64_t index_begin,
+                     uint64_t n_indices, double* out);
+
 /* ---- draws (parity and diagnostics) ------------------------------------- */
 /* Philox4x32-10 of n (counter, key) pairs; replaces mcd::philox4x32_10
  * (src/core/rng.cpp:41-47).  counters: n x 4, keys: n x 2, out: n x 4. */
