@@ -121,7 +121,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
 
 def _build_shim(verbose: bool) -> None:
-    srcs = [os.path.join(CPP, f) for f in ("pricers.cpp", "json.cpp") if os.path.exists(os.path.join(CPP, f))]
+    srcs = sorted(os.path.join(CPP, f) for f in os.listdir(CPP) if f.endswith(".cpp") and f != "mcd_gpu_cli.cpp")
     if srcs:
         _run(["g++", "-std=c++20", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-I", INCLUDE,
               "-I", CPP, "-o", SHIM_LIB] + srcs + ["-L", BUILD, "-lmcd_gpu",

@@ -373,12 +373,12 @@ int mcd_lr_european(mcd_ctx* handle, double spot, double strike, double rate, do
 }
 
 int mcd_lr_digital(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield, double vol,
-                   double time, int type, double cash_amount, uint64_t path_count, uint64_t seed, int precision,
-                   mcd_lr_greeks* out) {
+                   double time, int type, int digital_style, double cash_amount, uint64_t path_count, uint64_t seed,
+                   int precision, mcd_lr_greeks* out) {
     if (!out) return MCD_ERR_INVALID_ARGUMENT;
     mcd_contract c = make_contract(MCD_PRODUCT_DIGITAL, spot, strike, rate, carry_yield, vol, time, type, path_count,
                                    seed);
-    c.digital_style = MCD_CASH_OR_NOTHING;
+    c.digital_style = digital_style;
     c.cash_amount = cash_amount;
     mcd_greeks_result r;
     const int rc = greeks_one(handle, c, precision, &r);

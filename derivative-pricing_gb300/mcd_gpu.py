@@ -200,7 +200,7 @@ def lib():
     sig("mcd_default_bump_sizes", dbl, dbl, dbl, res=BumpSizes)
     sig("mcd_fd_european", vp, *D6, i32, u64, u64, BumpSizes, i32, P(EuropeanGreeks))
     sig("mcd_lr_european", vp, *D6, i32, u64, u64, i32, P(LrGreeks))
-    sig("mcd_lr_digital", vp, *D6, i32, dbl, u64, u64, i32, P(LrGreeks))
+    sig("mcd_lr_digital", vp, *D6, i32, i32, dbl, u64, u64, i32, P(LrGreeks))
     sig("mcd_lr_barrier", vp, *([dbl] * 7), i32, i32, i32, dbl, i32, u64, u64, i32, P(LrGreeks))
     sig("mcd_pathwise_european", vp, *D6, i32, u64, u64, i32, P(PathwiseGreeks))
     sig("mcd_pathwise_asian", vp, *D6, i32, i32, i32, i32, u64, u64, i32, P(PathwiseGreeks))
@@ -500,12 +500,12 @@ class Engine:
                                               type, path_count, seed, _prec(precision), C.byref(out)))
         return out
 
-    def likelihood_ratio_digital(self, spot, strike, rate, carry_yield, vol, time, type,
+    def likelihood_ratio_digital(self, spot, strike, rate, carry_yield, vol, time, type, style,
                                  cash_amount, path_count, seed, precision="fp64") -> LrGreeks:
         out = LrGreeks()
         self._check(self._lib.mcd_lr_digital(self.handle, spot, strike, rate, carry_yield, vol, time,
-                                             type, cash_amount, path_count, seed, _prec(precision),
-                                             C.byref(out)))
+                                             type, style, cash_amount, path_count, seed,
+                                             _prec(precision), C.byref(out)))
         return out
 
     def likelihood_ratio_barrier(self, spot, strike, barrier, rate, carry_yield, vol, time, type,

@@ -373,14 +373,14 @@ typedef struct {
     int32_t has_theta;
     int32_t reserved;
 } mcd_lr_greeks;
-/* replace mcd::greeks::likelihood_ratio_european / _digital (cash-or-nothing)
- * / _barrier (src/greeks/likelihood_ratio.cpp:75-154) */
+/* replace mcd::greeks::likelihood_ratio_european / _digital / _barrier
+ * (src/greeks/likelihood_ratio.cpp:75-154) */
 int mcd_lr_european(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
                     double vol, double time, int type, uint64_t path_count, uint64_t seed,
                     int precision, mcd_lr_greeks* out);
 int mcd_lr_digital(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
-                   double vol, double time, int type, double cash_amount, uint64_t path_count,
-                   uint64_t seed, int precision, mcd_lr_greeks* out);
+                   double vol, double time, int type, int digital_style, double cash_amount,
+                   uint64_t path_count, uint64_t seed, int precision, mcd_lr_greeks* out);
 int mcd_lr_barrier(mcd_ctx* ctx, double spot, double strike, double barrier, double rate,
                    double carry_yield, double vol, double time, int type, int direction, int knock,
                    double rebate, int monitoring_points, uint64_t path_count, uint64_t seed,

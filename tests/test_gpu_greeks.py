@@ -43,8 +43,8 @@ def test_lr_matches_reference(engine, golden):
     for x, y in zip(got, lr["european"]["out"]):
         assert close(x, y), (got, lr["european"]["out"])
     assert r.has_theta == 1
-    a = lr["digital"]["args"]  # (..., type, digital style 0 = cash, cash, paths, seed)
-    r = engine.likelihood_ratio_digital(*a[:7], a[8], a[9], a[10], precision="fp64")
+    a = lr["digital"]["args"]  # (..., type, digital style, cash, paths, seed)
+    r = engine.likelihood_ratio_digital(*a, precision="fp64")
     got = [r.delta.value, r.delta.standard_error, r.gamma.value, r.gamma.standard_error, r.vega.value,
            r.vega.standard_error, r.rho.value, r.rho.standard_error, r.theta.value, r.theta.standard_error]
     for x, y in zip(got, lr["digital"]["out"]):
