@@ -163,6 +163,123 @@ def cpu_baseline_sample(c, budget_s=12.0):
             "path_steps_per_s": path_steps(sample) / dt}
 
 
+def lsm_grid():
+    """The American-put grid: S0 in {36,38,40,42,44}, K=40, r=.06, sigma in {.2,.4},
+    T in {1,2}, 50 exercise dates, 2^20 paths, seed 42+i."""
+    import mcd_gpu as M
+    rows = [(s, 40.0, 0.06, 0.0, v, t, 1, 50, 1 << 20, 42 + i)
+            for i, (s, v, t) in enumerate((s, v, t) for s in (36, 38, 40, 42, 44) for v in (0.2, 0.4) for t in (1.0, 2.0))]
+    return np.array(rows, dtype=M.LSM_CONTRACT_DTYPE)
+
+
+def _timed(fn, reps=2):
+    fn()
+    ts = []
+    out = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out = fn()
+        ts.append(time.perf_counter() - t0)
+    return out, min(ts)
+
+
+def bench_lsm(eng):
+    """Time-to-price of the 20-put grid: plain FP64 GPU path (QR, FP64 paths),
+    FP32 QR, and the learned regression (FP32 paths, BF16 tensor-core network).
+    Errors are measured against the FP64 result (the reference's arithmetic,
+    parity-tested to 1e-10) in units of its standard error."""
+    g = lsm_grid()
+    r64, t64 = _timed(lambda: eng.lsm_batch(g, "fp64", "qr"))
+    r32, t32 = _timed(lambda: eng.lsm_batch(g, "fp32", "qr"))
+    rml, tml = _timed(lambda: eng.lsm_batch(g, "fp32", "mlp"))
+    se = r64["standard_error"]
+    e32 = np.abs(r32["price"] - r64["price"]) / se
+    eml = np.abs(rml["price"] - r64["price"]) / se
+    return {"workload": "20 American puts (S0 36..44, sigma .2/.4, T 1/2), 50 dates, 2^20 paths each",
+            "fp64_qr_s": t64, "fp32_qr_s": t32, "learned_s": tml,
+            "speedup_learned_over_fp64": t64 / tml, "speedup_fp32_qr_over_fp64": t64 / t32,
+            "learned_err_vs_fp64_max_se": float(eml.max()), "learned_err_vs_fp64_mean_se": float(eml.mean()),
+            "fp32_qr_err_vs_fp64_max_se": float(e32.max()),
+            "learned_fallbacks": int((rml["reserved"] != 0).sum()),
+            "timing": "wall clock of one mcd_lsm_batch call (host arrays, graph capture and copies included), "
+                      "best of 2 after a warm-up"}
+
+
+def risk_batch(n=1024, seed=42):
+    """Asian/barrier contracts drawn as in the batch configuration, 252 steps, 2^18 paths."""
+    c = make_batch(4 * n, seed)
+    c = c[np.isin(c["product"], [2, 3])][:n].copy()
+    c["monitoring_points"] = 252
+    c["path_count"] = 1 << 18
+    return c
+
+
+def bench_risk(eng):
+    """Batched risk: price, CRN finite-difference delta/gamma/vega (bump 1e-4
+    relative), pathwise and likelihood-ratio Greeks of 1024 Asian/barrier
+    contracts in one graph launch; learned LSM on 512 American puts with
+    uneven date counts U{10..100}, 2^18 paths."""
+    import mcd_gpu as M
+    c = risk_batch()
+    v, ctas, _ = eng.greeks_autotune(c[::8], 1e-4, 1e-4, "fp32")
+    res, tg = _timed(lambda: eng.greeks_batch(c, 1e-4, 1e-4, "fp32"))
+    steps = float(len(c)) * 252 * (1 << 18)
+    rng = np.random.default_rng(7)
+    n = 512
+    puts = np.zeros(n, dtype=M.LSM_CONTRACT_DTYPE)
+    puts["spot"] = rng.uniform(36, 44, n)
+    puts["strike"] = 40.0
+    puts["rate"] = 0.06
+    puts["vol"] = rng.uniform(0.2, 0.4, n)
+    puts["time"] = rng.uniform(0.5, 2.0, n)
+    puts["type"] = 1
+    puts["monitoring_points"] = rng.integers(10, 101, n)
+    puts["path_count"] = 1 << 18
+    puts["seed"] = 1000 + np.arange(n)
+    ml, tl = _timed(lambda: eng.lsm_batch(puts, "fp32", "mlp"), reps=1)
+    qr, tq = _timed(lambda: eng.lsm_batch(puts, "fp32", "qr"), reps=1)
+    return {"greeks": {"contracts": len(c), "s": tg, "contracts_per_second": len(c) / tg,
+                       "path_steps_per_second": steps / tg, "launch_shape": {"variant": v, "ctas_per_sm": ctas},
+                       "outputs": "price, FD delta/gamma/vega, pathwise delta/vega/rho, LR delta/gamma/vega/rho"},
+            "learned_lsm_512": {"s": tl, "contracts_per_second": n / tl, "qr_s": tq,
+                                "max_abs_diff_vs_qr_in_se": float(np.max(np.abs(ml["price"] - qr["price"]) /
+                                                                         qr["standard_error"])),
+                                "fallbacks": int((ml["reserved"] != 0).sum())}}
+
+
+def bench_heston(eng, n_sets=256):
+    """Heston QE: parameter sets drawn from the configuration's ranges, 64
+    strikes linspace(70,130) each, 252 steps, 2^20 paths, FP32 paths."""
+    import mcd_gpu as M
+    rng = np.random.default_rng(42)
+    sets = np.zeros(n_sets, dtype=M.HESTON_DTYPE)
+    sets["spot"] = 100.0
+    sets["rate"] = 0.03
+    sets["kappa"] = rng.uniform(0.5, 3.0, n_sets)
+    sets["theta"] = rng.uniform(0.02, 0.09, n_sets)
+    sets["xi"] = rng.uniform(0.2, 1.0, n_sets)
+    sets["rho"] = rng.uniform(-0.9, -0.3, n_sets)
+    sets["v0"] = rng.uniform(0.01, 0.09, n_sets)
+    sets["time"] = 1.0
+    strikes = np.linspace(70.0, 130.0, 64)
+    out, t = _timed(lambda: eng.heston_qe_batch(sets, strikes, 0, 252, 1 << 20, 42, "fp32"), reps=1)
+    steps = float(n_sets) * 252 * (1 << 20)
+    return {"sets": n_sets, "strikes": 64, "s": t, "paths_per_second": n_sets * (1 << 20) / t,
+            "path_steps_per_second": steps / t, "prices_per_second": n_sets * 64 / t}
+
+
+def bench_qmc(eng, c):
+    """The Sobol + Brownian-bridge variant of the batch (dims = steps)."""
+    q = c.copy()
+    q["antithetic"] = 0
+    q["control_variate"] = 0
+    q["brownian_bridge"] = 0
+    _, t = _timed(lambda: eng.qmc_batch(q, "fp32"))
+    return {"s": t, "paths_per_second": float(q["path_count"].astype(np.float64).sum()) / t,
+            "path_steps_per_second": path_steps(q) / t,
+            "timing": "wall clock of one mcd_qmc_batch call (host arrays), best of 2 after a warm-up"}
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU algorithm (the oracle port,
     bit-identical to the reference built from source) on the host cores."""
@@ -198,6 +315,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the LSM, risk, Heston and QMC sections")
     ap.add_argument("--contracts", type=int, default=4096,
                     help="batch size (the configuration is 4096; smaller only for profiling)")
     args = ap.parse_args()
@@ -352,6 +471,11 @@ def main():
             "fp32_err_vs_fp64_max_se": float(err.max()), "fp32_err_vs_fp64_mean_se": float(err.mean()),
             "fp64_wall_s": t64}
         assert r32b.tobytes() == r32.tobytes()
+    if not args.no_extra and rank == 0:
+        line["lsm"] = bench_lsm(eng)
+        line["risk"] = bench_risk(eng)
+        line["heston"] = bench_heston(eng)
+        line["qmc"] = bench_qmc(eng, c)
     if not args.no_cpu and rank == 0:
         line["cpu_baseline"] = cpu_baseline_sample(c)
     if rank == 0:
