@@ -29,8 +29,12 @@
 // removes the conditioning (cond(X) reaches ~2e6 for these bases, cond(G)
 // ~4e12), the second is solved at QR accuracy, so the coefficients agree with
 // the reference's Householder QR to ~1e-10 relative and exercise decisions
-// essentially never differ.  All sums are FP64 and every reduction tree is
-// fixed by chunk index.
+// essentially never differ.  Every reduction tree is fixed by chunk index.
+// Precision: the FP64 path is the reference's arithmetic throughout.  The
+// FP32 path evaluates the basis, the exercise tests and the Gram products in
+// FP32 (FP64 runs at a small fraction of the FP32 rate here) and accumulates
+// them with compensated FP32 sums per chunk; chunk partials, the Cholesky-QR2
+// solves, the continuation value and the cash flows stay FP64.
 //
 // nvcc-flags: --fmad=false
 #include <cuda_runtime.h>
@@ -48,24 +52,72 @@ __device__ __forceinline__ double intrinsic(double s, double k, int type) {
     return dmax((type == 0 ? 1.0 : -1.0) * (s - k), 0.0);
 }
 
-// Weighted Laguerre basis on x = S/K (src/pricers/lsm.cpp:21-25).  FP64 path:
-// the reference's expressions.  FP32 path: the common factor exp(-x/2) in
-// FP32 (a relative error there scales the continuation value, it is not
-// amplified by the large coefficients), the polynomials in FP64.
-template <int PREC>
-__device__ __forceinline__ void basis(double s, double strike, double inv_strike, double b[4]) {
-    double x, e;
-    if (PREC == 0) {
-        x = s / strike;
-        e = exp(-x / 2.0);
-    } else {
-        x = s * inv_strike;
-        e = static_cast<double>(__expf(-0.5f * static_cast<float>(x)));
-    }
+// Weighted Laguerre basis on x = S/K (src/pricers/lsm.cpp:21-25), the
+// reference's expressions (FP64 path).
+__device__ __forceinline__ void basis64(double s, double strike, double b[4]) {
+    const double x = s / strike;
+    const double e = exp(-x / 2.0);
     b[0] = e;
     b[1] = e * (1.0 - x);
     b[2] = e * (1.0 - 2.0 * x + 0.5 * x * x);
     b[3] = e * (1.0 - 3.0 * x + 1.5 * x * x - x * x * x / 6.0);
+}
+
+// FP32 path: the same basis evaluated in FP32.  FP64 arithmetic runs at a
+// small fraction of the FP32 rate on this GPU, and with FP32 paths the basis
+// carries FP32 inputs anyway; the regression is fitted to exactly this
+// evaluated basis and the sums that need the range stay compensated (below).
+__device__ __forceinline__ void basis32(float s, float inv_strike, float b[4]) {
+    const float x = s * inv_strike;
+    const float e = __expf(-0.5f * x);
+    b[0] = e;
+    b[1] = e * (1.0f - x);
+    b[2] = e * __fmaf_rn(0.5f * x, x, __fmaf_rn(-2.0f, x, 1.0f));
+    b[3] = e * __fmaf_rn(__fmaf_rn(-x / 6.0f, x, 1.5f * x), x, __fmaf_rn(-3.0f, x, 1.0f));
+}
+
+// Compensated FP32 accumulation (Knuth's TwoSum): hi + lo carries ~44 bits,
+// enough for Gram sums of a chunk; chunk partials are then merged in FP64.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+}
+
+// Fixed-shape block reduction of N compensated sums (256 threads): warp
+// trees, then thread 0 folds the 8 warps in order; FP64 results in out
+// (valid in thread 0).
+template <int N>
+__device__ void block_sum_df(float (&hi)[N], float (&lo)[N], float (*smem)[N][2], double (&out)[N]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+            const float oh = __shfl_down_sync(0xffffffffu, hi[i], off);
+            const float ol = __shfl_down_sync(0xffffffffu, lo[i], off);
+            df_add(hi[i], lo[i], oh);
+            lo[i] += ol;
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            smem[warp][i][0] = hi[i];
+            smem[warp][i][1] = lo[i];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            double x = 0.0;
+            for (int w = 0; w < kLsmThreads / 32; ++w)
+                x += static_cast<double>(smem[w][i][0]) + static_cast<double>(smem[w][i][1]);
+            out[i] = x;
+        }
+    }
 }
 
 template <int PREC>
@@ -150,6 +202,7 @@ __global__ void __launch_bounds__(kLsmThreads)
                  const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_a,
                  Welford* __restrict__ final_part) {
     __shared__ double smem[kLsmThreads / 32][11];
+    __shared__ float smem_f[kLsmThreads / 32][11][2];
     __shared__ Welford swf[kLsmThreads / 32];
     const uint32_t chunk = blockIdx.x;
     if (chunk >= total_chunks) return;
@@ -169,58 +222,132 @@ __global__ void __launch_bounds__(kLsmThreads)
         g2 = re->gamma[2];
         g3 = re->gamma[3];
     }
-    const double inv_k = 1.0 / c.strike;
-    double acc[11];
-#pragma unroll
-    for (int q = 0; q < 11; ++q) acc[q] = 0.0;
-    Welford w{0ull, 0.0, 0.0};
     const uint32_t local = chunk - c.chunk_begin;
-    for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
-        const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
-        if (i >= c.path_count) break;
-        double v;
-        if (init) {
-            v = intrinsic(load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(n - 1) * c.path_count + i),
-                          c.strike, c.type);
-        } else {
-            v = cf[c.cf_offset + i];
-            if (exercise) {
-                const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 1) * c.path_count + i);
-                const double ex = intrinsic(s, c.strike, c.type);
-                if (ex > 0.0) {
-                    double b[4];
-                    basis<PREC>(s, c.strike, inv_k, b);
-                    double cont = 0.0;
-                    cont += g0 * b[0];
-                    cont += g1 * b[1];
-                    cont += g2 * b[2];
-                    cont += g3 * b[3];
-                    if (ex > cont) v = ex;
+    Welford w{0ull, 0.0, 0.0};
+    if constexpr (PREC == 0) {
+        double acc[11];
+#pragma unroll
+        for (int q = 0; q < 11; ++q) acc[q] = 0.0;
+        for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+            const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
+            if (i >= c.path_count) break;
+            double v;
+            if (init) {
+                v = intrinsic(load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(n - 1) * c.path_count + i),
+                              c.strike, c.type);
+            } else {
+                v = cf[c.cf_offset + i];
+                if (exercise) {
+                    const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 1) * c.path_count + i);
+                    const double ex = intrinsic(s, c.strike, c.type);
+                    if (ex > 0.0) {
+                        double b[4];
+                        basis64(s, c.strike, b);
+                        double cont = 0.0;
+                        cont += g0 * b[0];
+                        cont += g1 * b[1];
+                        cont += g2 * b[2];
+                        cont += g3 * b[3];
+                        if (ex > cont) v = ex;
+                    }
+                }
+            }
+            v *= c.disc;
+            if (last) {
+                welford_add(w, v);
+            } else {
+                cf[c.cf_offset + i] = v;
+                if (gram) {
+                    const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 2) * c.path_count + i);
+                    if (intrinsic(s, c.strike, c.type) > 0.0) {
+                        double b[4];
+                        basis64(s, c.strike, b);
+                        acc[0] += 1.0;
+                        acc[1] += b[0] * b[0];
+                        acc[2] += b[0] * b[1];
+                        acc[3] += b[0] * b[2];
+                        acc[4] += b[0] * b[3];
+                        acc[5] += b[1] * b[1];
+                        acc[6] += b[1] * b[2];
+                        acc[7] += b[1] * b[3];
+                        acc[8] += b[2] * b[2];
+                        acc[9] += b[2] * b[3];
+                        acc[10] += b[3] * b[3];
+                    }
                 }
             }
         }
-        v *= c.disc;
-        if (last) {
-            welford_add(w, v);
-        } else {
-            cf[c.cf_offset + i] = v;
-            if (gram) {
-                const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 2) * c.path_count + i);
-                if (intrinsic(s, c.strike, c.type) > 0.0) {
-                    double b[4];
-                    basis<PREC>(s, c.strike, inv_k, b);
-                    acc[0] += 1.0;
-                    acc[1] += b[0] * b[0];
-                    acc[2] += b[0] * b[1];
-                    acc[3] += b[0] * b[2];
-                    acc[4] += b[0] * b[3];
-                    acc[5] += b[1] * b[1];
-                    acc[6] += b[1] * b[2];
-                    acc[7] += b[1] * b[3];
-                    acc[8] += b[2] * b[2];
-                    acc[9] += b[2] * b[3];
-                    acc[10] += b[3] * b[3];
+        if (gram) {
+            block_sum<11>(acc, smem);
+            if (threadIdx.x == 0) {
+#pragma unroll
+                for (int q = 0; q < 11; ++q) part_a[chunk].v[q] = acc[q];
+            }
+        }
+    } else {
+        // FP32 paths: FP32 basis, exercise tests and Gram products; FP64
+        // cash flows and the continuation value (large coefficients cancel).
+        const float phi = c.type == 0 ? 1.0f : -1.0f;
+        const float strike = static_cast<float>(c.strike);
+        const float inv_kf = static_cast<float>(1.0 / c.strike);
+        const float* S = static_cast<const float*>(store) + c.s_offset;
+        float hi[11], lo[11];
+#pragma unroll
+        for (int q = 0; q < 11; ++q) hi[q] = lo[q] = 0.0f;
+        for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+            const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
+            if (i >= c.path_count) break;
+            double v;
+            if (init) {
+                v = static_cast<double>(fmaxf(phi * (S[static_cast<uint64_t>(n - 1) * c.path_count + i] - strike), 0.0f));
+            } else {
+                v = cf[c.cf_offset + i];
+                if (exercise) {
+                    const float s = S[static_cast<uint64_t>(e - 1) * c.path_count + i];
+                    const float ex = phi * (s - strike);
+                    if (ex > 0.0f) {
+                        float b[4];
+                        basis32(s, inv_kf, b);
+                        double cont = 0.0;
+                        cont += g0 * static_cast<double>(b[0]);
+                        cont += g1 * static_cast<double>(b[1]);
+                        cont += g2 * static_cast<double>(b[2]);
+                        cont += g3 * static_cast<double>(b[3]);
+                        if (static_cast<double>(ex) > cont) v = static_cast<double>(ex);
+                    }
                 }
+            }
+            v *= c.disc;
+            if (last) {
+                welford_add(w, v);
+            } else {
+                cf[c.cf_offset + i] = v;
+                if (gram) {
+                    const float s = S[static_cast<uint64_t>(e - 2) * c.path_count + i];
+                    if (phi * (s - strike) > 0.0f) {
+                        float b[4];
+                        basis32(s, inv_kf, b);
+                        df_add(hi[0], lo[0], 1.0f);
+                        df_add(hi[1], lo[1], b[0] * b[0]);
+                        df_add(hi[2], lo[2], b[0] * b[1]);
+                        df_add(hi[3], lo[3], b[0] * b[2]);
+                        df_add(hi[4], lo[4], b[0] * b[3]);
+                        df_add(hi[5], lo[5], b[1] * b[1]);
+                        df_add(hi[6], lo[6], b[1] * b[2]);
+                        df_add(hi[7], lo[7], b[1] * b[3]);
+                        df_add(hi[8], lo[8], b[2] * b[2]);
+                        df_add(hi[9], lo[9], b[2] * b[3]);
+                        df_add(hi[10], lo[10], b[3] * b[3]);
+                    }
+                }
+            }
+        }
+        if (gram) {
+            double acc[11];
+            block_sum_df<11>(hi, lo, smem_f, acc);
+            if (threadIdx.x == 0) {
+#pragma unroll
+                for (int q = 0; q < 11; ++q) part_a[chunk].v[q] = acc[q];
             }
         }
     }
@@ -232,12 +359,6 @@ __global__ void __launch_bounds__(kLsmThreads)
             Welford m = swf[0];
             for (int q = 1; q < kLsmThreads / 32; ++q) m = welford_merge(m, swf[q]);
             final_part[chunk] = m;
-        }
-    } else if (gram) {
-        block_sum<11>(acc, smem);
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int q = 0; q < 11; ++q) part_a[chunk].v[q] = acc[q];
         }
     }
 }
@@ -318,6 +439,7 @@ __global__ void __launch_bounds__(kLsmThreads)
                uint32_t total_chunks, const void* __restrict__ store, const double* __restrict__ cf,
                const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_b) {
     __shared__ double smem[kLsmThreads / 32][15];
+    __shared__ float smem_f[kLsmThreads / 32][15][2];
     const uint32_t chunk = blockIdx.x;
     if (chunk >= total_chunks) return;
     const LsmDev c = cs[chunk_contract[chunk]];
@@ -325,47 +447,91 @@ __global__ void __launch_bounds__(kLsmThreads)
     if (date < 1) return;
     const LsmReg& r = reg[c.reg_offset + date];
     if (r.has == -1) return;  // no regression at this date
-    double T[10];
-#pragma unroll
-    for (int q = 0; q < 10; ++q) T[q] = r.T[q];
-    const double inv_k = 1.0 / c.strike;
-    double acc[15];
-#pragma unroll
-    for (int q = 0; q < 15; ++q) acc[q] = 0.0;
     const uint32_t local = chunk - c.chunk_begin;
-    for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
-        const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
-        if (i >= c.path_count) break;
-        const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(date - 1) * c.path_count + i);
-        if (!(intrinsic(s, c.strike, c.type) > 0.0)) continue;
-        double b[4];
-        basis<PREC>(s, c.strike, inv_k, b);
-        // b'_l = sum_{j <= l} b_j T[j][l]
-        double q0 = b[0] * T[0];
-        double q1 = b[0] * T[1] + b[1] * T[4];
-        double q2 = b[0] * T[2] + b[1] * T[5] + b[2] * T[7];
-        double q3 = b[0] * T[3] + b[1] * T[6] + b[2] * T[8] + b[3] * T[9];
-        const double y = cf[c.cf_offset + i];
-        acc[0] += 1.0;
-        acc[1] += q0 * q0;
-        acc[2] += q0 * q1;
-        acc[3] += q0 * q2;
-        acc[4] += q0 * q3;
-        acc[5] += q1 * q1;
-        acc[6] += q1 * q2;
-        acc[7] += q1 * q3;
-        acc[8] += q2 * q2;
-        acc[9] += q2 * q3;
-        acc[10] += q3 * q3;
-        acc[11] += q0 * y;
-        acc[12] += q1 * y;
-        acc[13] += q2 * y;
-        acc[14] += q3 * y;
+    double out[15];
+    if constexpr (PREC == 0) {
+        double T[10];
+#pragma unroll
+        for (int q = 0; q < 10; ++q) T[q] = r.T[q];
+        double acc[15];
+#pragma unroll
+        for (int q = 0; q < 15; ++q) acc[q] = 0.0;
+        for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+            const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
+            if (i >= c.path_count) break;
+            const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(date - 1) * c.path_count + i);
+            if (!(intrinsic(s, c.strike, c.type) > 0.0)) continue;
+            double b[4];
+            basis64(s, c.strike, b);
+            // b'_l = sum_{j <= l} b_j T[j][l]
+            double q0 = b[0] * T[0];
+            double q1 = b[0] * T[1] + b[1] * T[4];
+            double q2 = b[0] * T[2] + b[1] * T[5] + b[2] * T[7];
+            double q3 = b[0] * T[3] + b[1] * T[6] + b[2] * T[8] + b[3] * T[9];
+            const double y = cf[c.cf_offset + i];
+            acc[0] += 1.0;
+            acc[1] += q0 * q0;
+            acc[2] += q0 * q1;
+            acc[3] += q0 * q2;
+            acc[4] += q0 * q3;
+            acc[5] += q1 * q1;
+            acc[6] += q1 * q2;
+            acc[7] += q1 * q3;
+            acc[8] += q2 * q2;
+            acc[9] += q2 * q3;
+            acc[10] += q3 * q3;
+            acc[11] += q0 * y;
+            acc[12] += q1 * y;
+            acc[13] += q2 * y;
+            acc[14] += q3 * y;
+        }
+        block_sum<15>(acc, smem);
+#pragma unroll
+        for (int q = 0; q < 15; ++q) out[q] = acc[q];
+    } else {
+        float T[10];
+#pragma unroll
+        for (int q = 0; q < 10; ++q) T[q] = static_cast<float>(r.T[q]);
+        const float phi = c.type == 0 ? 1.0f : -1.0f;
+        const float strike = static_cast<float>(c.strike);
+        const float inv_kf = static_cast<float>(1.0 / c.strike);
+        const float* S = static_cast<const float*>(store) + c.s_offset;
+        float hi[15], lo[15];
+#pragma unroll
+        for (int q = 0; q < 15; ++q) hi[q] = lo[q] = 0.0f;
+        for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+            const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
+            if (i >= c.path_count) break;
+            const float s = S[static_cast<uint64_t>(date - 1) * c.path_count + i];
+            if (!(phi * (s - strike) > 0.0f)) continue;
+            float b[4];
+            basis32(s, inv_kf, b);
+            const float q0 = b[0] * T[0];
+            const float q1 = __fmaf_rn(b[1], T[4], b[0] * T[1]);
+            const float q2 = __fmaf_rn(b[2], T[7], __fmaf_rn(b[1], T[5], b[0] * T[2]));
+            const float q3 = __fmaf_rn(b[3], T[9], __fmaf_rn(b[2], T[8], __fmaf_rn(b[1], T[6], b[0] * T[3])));
+            const float y = static_cast<float>(cf[c.cf_offset + i]);
+            df_add(hi[0], lo[0], 1.0f);
+            df_add(hi[1], lo[1], q0 * q0);
+            df_add(hi[2], lo[2], q0 * q1);
+            df_add(hi[3], lo[3], q0 * q2);
+            df_add(hi[4], lo[4], q0 * q3);
+            df_add(hi[5], lo[5], q1 * q1);
+            df_add(hi[6], lo[6], q1 * q2);
+            df_add(hi[7], lo[7], q1 * q3);
+            df_add(hi[8], lo[8], q2 * q2);
+            df_add(hi[9], lo[9], q2 * q3);
+            df_add(hi[10], lo[10], q3 * q3);
+            df_add(hi[11], lo[11], q0 * y);
+            df_add(hi[12], lo[12], q1 * y);
+            df_add(hi[13], lo[13], q2 * y);
+            df_add(hi[14], lo[14], q3 * y);
+        }
+        block_sum_df<15>(hi, lo, smem_f, out);
     }
-    block_sum<15>(acc, smem);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int q = 0; q < 15; ++q) part_b[chunk].v[q] = acc[q];
+        for (int q = 0; q < 15; ++q) part_b[chunk].v[q] = out[q];
     }
 }
 
