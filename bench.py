@@ -192,15 +192,25 @@ def bench_lsm(eng):
     r64, t64 = _timed(lambda: eng.lsm_batch(g, "fp64", "qr"))
     r32, t32 = _timed(lambda: eng.lsm_batch(g, "fp32", "qr"))
     rml, tml = _timed(lambda: eng.lsm_batch(g, "fp32", "mlp"))
+    import mcd_gpu as M
     se = r64["standard_error"]
     e32 = np.abs(r32["price"] - r64["price"]) / se
     eml = np.abs(rml["price"] - r64["price"]) / se
+    tree = np.array([M.crr_binomial_american(r["spot"], r["strike"], r["rate"], r["carry_yield"], r["vol"],
+                                             r["time"], 2000, 1) for r in g])
     return {"workload": "20 American puts (S0 36..44, sigma .2/.4, T 1/2), 50 dates, 2^20 paths each",
             "fp64_qr_s": t64, "fp32_qr_s": t32, "learned_s": tml,
             "speedup_learned_over_fp64": t64 / tml, "speedup_fp32_qr_over_fp64": t64 / t32,
             "learned_err_vs_fp64_max_se": float(eml.max()), "learned_err_vs_fp64_mean_se": float(eml.mean()),
             "fp32_qr_err_vs_fp64_max_se": float(e32.max()),
             "learned_fallbacks": int((rml["reserved"] != 0).sum()),
+            "vs_crr_tree_2000": {
+                "note": "in-sample LSM prices against the American lattice price; the 50-date Bermudan "
+                        "and the in-sample foresight bias both enter",
+                "fp64_qr_mean_abs_err": float(np.mean(np.abs(r64["price"] - tree))),
+                "fp32_qr_mean_abs_err": float(np.mean(np.abs(r32["price"] - tree))),
+                "learned_mean_abs_err": float(np.mean(np.abs(rml["price"] - tree))),
+                "mean_se": float(np.mean(se))},
             "timing": "wall clock of one mcd_lsm_batch call (host arrays, graph capture and copies included), "
                       "best of 2 after a warm-up"}
 

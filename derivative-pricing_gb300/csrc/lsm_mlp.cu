@@ -328,6 +328,19 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
     return x;
 }
 
+// Cash flows: FP64 on the FP64 path, FP32 (in the same buffer) on the FP32
+// path, as the QR kernels keep them (lsm.cu).
+template <int PREC>
+__device__ __forceinline__ double cf_load(const double* cf, uint64_t idx) {
+    if (PREC == 0) return cf[idx];
+    return static_cast<double>(reinterpret_cast<const float*>(cf)[idx]);
+}
+template <int PREC>
+__device__ __forceinline__ void cf_store(double* cf, uint64_t idx, double v) {
+    if (PREC == 0) cf[idx] = v;
+    else reinterpret_cast<float*>(cf)[idx] = static_cast<float>(v);
+}
+
 template <int PREC>
 __device__ __forceinline__ double path_s(const void* store, uint64_t idx) {
     if (PREC == 0) return static_cast<const double*>(store)[idx];
@@ -390,7 +403,7 @@ __global__ void __launch_bounds__(128, 1)
         // decision only needs its sign, and it is an order of magnitude
         // smaller than the continuation value itself, so the network's
         // relative error costs far fewer wrong decisions.
-        S.y[s] = itm ? static_cast<float>((cf[c.cf_offset + i] - ex) * inv_k) : 0.0f;
+        S.y[s] = itm ? static_cast<float>((cf_load<PREC>(cf, c.cf_offset + i) - ex) * inv_k) : 0.0f;
         S.w[s] = itm ? 1.0f : 0.0f;
         const int n_eff = __syncthreads_count(itm);
         ++t;
@@ -511,7 +524,7 @@ __global__ void __launch_bounds__(128)
                     const double x = phi * (sT - c.strike);
                     v = x > 0.0 ? x : 0.0;
                 } else {
-                    v = cf[c.cf_offset + i];
+                    v = cf_load<PREC>(cf, c.cf_offset + i);
                 }
             }
             if (exercise) {
@@ -569,7 +582,7 @@ __global__ void __launch_bounds__(128)
             if (live && step) {
                 v *= c.disc;
                 if (last) welford_add(w, v);
-                else cf[c.cf_offset + i] = v;
+                else cf_store<PREC>(cf, c.cf_offset + i, v);
             }
             if (gram) {
                 const bool itm = live && ex_d > 0.0;

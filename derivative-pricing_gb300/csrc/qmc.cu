@@ -56,6 +56,7 @@ __device__ __forceinline__ uint32_t gray_of(uint64_t path) {
 struct QmcTables {
     BridgeNode node[kSobolDims];
     double a[kSobolDims], sd[kSobolDims], drift[kSobolDims];
+    float af[kSobolDims], sdf[kSobolDims], driftf[kSobolDims];  // FP32 copies (no conversion per path-step)
 };
 
 // Bridge coefficients of one contract in program order, with the reference's
@@ -79,6 +80,9 @@ __device__ void fill_tables(const DevContract& c, const DevQmc& q, const BridgeN
             S.sd[e] = sqrt((tm - tl) * (tr - tm) / (tr - tl));
         }
         S.drift[e] = q.drift_rate * tm;
+        S.af[e] = static_cast<float>(S.a[e]);
+        S.sdf[e] = static_cast<float>(S.sd[e]);
+        S.driftf[e] = static_cast<float>(S.drift[e]);
     }
 }
 
@@ -173,16 +177,16 @@ __device__ double sample_qmc32(const DevContract& c, const DevQmc& q, const QmcT
         for (int e = 0; e < n; ++e) {
             const BridgeNode& b = S.node[e];
             const float z = normal_from_sobol_f32(sobol_x(dirs, b.dim, gray));
-            const float sd = static_cast<float>(S.sd[e]);
+            const float sd = S.sdf[e];
             float val;
             if (b.t_left < 0 && b.t_right < 0) {
                 val = sd * z;
             } else {
                 const float wl = w[b.slot_left], wr = w[b.slot_right];
-                val = __fmaf_rn(sd, z, __fmaf_rn(static_cast<float>(S.a[e]), wr - wl, wl));
+                val = __fmaf_rn(sd, z, __fmaf_rn(S.af[e], wr - wl, wl));
             }
             w[b.slot_out] = val;
-            const float x = __fmaf_rn(vol, val, static_cast<float>(S.drift[e]));
+            const float x = __fmaf_rn(vol, val, S.driftf[e]);
             if (b.t_mid == n - 1) xlast = x;
             if constexpr (KIND == kAsianArith) {
                 acc += __expf(x);

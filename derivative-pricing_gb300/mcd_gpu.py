@@ -211,6 +211,7 @@ def lib():
     sig("mcd_philox", vp, P(u32), P(u32), C.c_size_t, P(u32))
     sig("mcd_draws", vp, u64, u64, u64, u32, u32, i32, i32, P(dbl))
     sig("mcd_kernel_timing", vp, i32, P(dbl), P(u64))
+    sig("mcd_crr_binomial_american", *D6, i32, i32, res=dbl)
     _lib = L
     return L
 
@@ -581,6 +582,11 @@ class Engine:
         self._check(self._lib.mcd_draws(self.handle, seed, path_begin, n_paths, draw_begin, n_draws,
                                         stream_id, _prec(precision), out.ctypes.data_as(P(dbl))))
         return out
+
+
+def crr_binomial_american(spot, strike, rate, carry_yield, vol, time, steps, type) -> float:
+    """Cox-Ross-Rubinstein American price (host code in libmcd_gpu.so)."""
+    return lib().mcd_crr_binomial_american(spot, strike, rate, carry_yield, vol, time, steps, type)
 
 
 def contracts(n: int) -> np.ndarray:

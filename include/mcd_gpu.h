@@ -444,6 +444,12 @@ int mcd_philox(mcd_ctx* ctx, const uint32_t* counters, const uint32_t* keys, siz
 int mcd_draws(mcd_ctx* ctx, uint64_t seed, uint64_t path_begin, uint64_t n_paths,
               uint32_t draw_begin, uint32_t n_draws, int stream_id, int precision, double* out);
 
+/* ---- lattice reference price (host code) ---------------------------------- */
+/* replaces mcd::pricers::crr_binomial_american (src/pricers/binomial.cpp): the
+ * Cox-Ross-Rubinstein American price, the yardstick for Longstaff-Schwartz. */
+double mcd_crr_binomial_american(double spot, double strike, double rate, double carry_yield, double vol,
+                                 double time, int steps, int type);
+
 /* ---- timing helper for benchmarks ---------------------------------------- */
 /* Average device time (ms) of the persistent path kernel over the calls made
  * since the last reset, measured with CUDA events on the launching stream. */
