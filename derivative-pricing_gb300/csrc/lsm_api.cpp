@@ -20,7 +20,7 @@ namespace {
 // Extension slots of Ctx::ext used by this module (Heston uses 0..3).
 enum { kDev = 4, kChunkMap = 5, kStore = 6, kCf = 7, kReg = 8, kPartA = 9, kPartB = 10,
        kFinal = 11, kOut = 12, kNets = 13, kSnaps = 14, kSnapOk = 15, kAdamT = 16, kErr = 17,
-       kGroupMap = 18, kGramPart = 19, kGramSum = 20 };
+       kGroupMap = 18, kGramPart = 19, kGramSum = 20, kFeatCache = 35 };
 
 struct LsmPlan {
     std::vector<LsmDev> dev;
@@ -113,6 +113,8 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
         if (!rc) rc = ctx.reserve(ctx.ext[kGroupMap], sizeof(uint32_t) * std::max<uint32_t>(p.total_groups, 1), "mlp group map");
         if (!rc) rc = ctx.reserve(ctx.ext[kGramPart], sizeof(float) * kGramPacked * std::max<uint32_t>(p.total_groups, 1), "mlp gram partials");
         if (!rc) rc = ctx.reserve(ctx.ext[kGramSum], sizeof(double) * kGramPacked * n, "mlp gram sums");
+        if (!rc && !frozen)
+            rc = ctx.reserve(ctx.ext[kFeatCache], 128 * std::max<uint64_t>(p.cf_elems, 1), "mlp feature cache");
         if (!rc) {
             cudaError_t pe = mlp_prepare();
             if (pe != cudaSuccess) rc = ctx.cuda_fail(pe, "mlp shared memory opt-in");
@@ -169,7 +171,8 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
                                           static_cast<int*>(ctx.ext[kSnapOk].ptr),
                                           static_cast<int*>(ctx.ext[kAdamT].ptr),
                                           static_cast<float*>(ctx.ext[kGramPart].ptr),
-                                          static_cast<double*>(ctx.ext[kGramSum].ptr), cfg,
+                                          static_cast<double*>(ctx.ext[kGramSum].ptr),
+                                          frozen ? nullptr : ctx.ext[kFeatCache].ptr, cfg,
                                           static_cast<Welford*>(ctx.ext[kFinal].ptr),
                                           static_cast<uint32_t*>(ctx.ext[kErr].ptr), ctx.stream);
         else

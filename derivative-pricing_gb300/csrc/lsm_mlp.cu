@@ -464,14 +464,15 @@ __device__ __forceinline__ void layer1_row(const float* small, float x0, float x
     }
 }
 
-enum PassMode { kStep = 1, kGram = 2 };
+enum PassMode { kStep = 1, kGram = 2, kCache = 4, kFill = 8 };
 
 template <int PREC>
 __global__ void __launch_bounds__(128)
     lsm_mlp_pass(int k, int mode, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
                  uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
                  const float* __restrict__ nets, const float* __restrict__ snaps, const int* __restrict__ snap_ok,
-                 float* __restrict__ gram_part, Welford* __restrict__ final_part, uint32_t* __restrict__ err) {
+                 float* __restrict__ gram_part, Welford* __restrict__ final_part, uint4* __restrict__ feat_cache,
+                 uint32_t* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     PassSmem& S = *reinterpret_cast<PassSmem*>(smem_raw);
     __shared__ Welford swf[4];
@@ -488,12 +489,25 @@ __global__ void __launch_bounds__(128)
     const bool exercise = step && k > 0 && e <= n - 1 && snap_ok[c.reg_offset + e] == 1;
     const bool gram = (mode & kGram) != 0 && e - 1 >= 1;
     if (!step && !gram) return;
+    // Feature cache (mode bit kCache): the hidden layers do not change between
+    // dates, so the features of S_e computed for date e's Gram matrix in the
+    // previous iteration are the decision network's features now; they are
+    // read back (BF16, exactly what the output layer was fitted on) instead of
+    // re-running layers 1 and 2, and this iteration's Gram features are
+    // stored for the next one.  One path's 64 features = 128 B, in place.
+    const bool cached = (mode & kCache) != 0;
+    const bool fill = (mode & kFill) != 0;  // store this pass's Gram features
+    const bool dec_net = exercise && !cached;  // evaluate the decision network's hidden layers
     const int s = threadIdx.x, warp = s >> 5;
     const double phi = c.type == 0 ? 1.0 : -1.0;
     const double inv_k = 1.0 / c.strike;
-    const bool mma = exercise || gram;
+    const bool mma = dec_net || gram;
+    if (exercise && cached) {  // output layer only
+        const float* net = snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride;
+        for (int i = s; i < kParams - kB2; i += 128) S.pd[kW2 + i] = net[kB2 + i];
+    }
     if (mma) {
-        if (exercise) load_net(snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride, S.pd, S.w2d);
+        if (dec_net) load_net(snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride, S.pd, S.w2d);
         if (gram) load_net(nets + static_cast<size_t>(ci) * 3 * kParamStride, S.pc, S.w2c);
         for (int i = s; i < 128 * 128 / 2; i += 128) reinterpret_cast<uint32_t*>(S.xt)[i] = 0u;
         if (s == 0) umma::mbar_init(&S.mbar, 1);
@@ -527,6 +541,7 @@ __global__ void __launch_bounds__(128)
                     v = cf_load<PREC>(cf, c.cf_offset + i);
                 }
             }
+            float yhat_cached = 0.0f;
             if (exercise) {
                 float x0 = 0.0f;
                 if (live) {
@@ -535,7 +550,24 @@ __global__ void __launch_bounds__(128)
                     ex_e = xx > 0.0 ? xx : 0.0;
                     x0 = static_cast<float>(4.0 * (se * inv_k - 1.0));
                 }
-                layer1_row(S.pd, x0, x1e, S.h1d, s);
+                if (dec_net) {
+                    layer1_row(S.pd, x0, x1e, S.h1d, s);
+                } else if (live && ex_e > 0.0) {  // cached features: output layer only
+                    const uint4* src = feat_cache + (c.cf_offset + i) * 8;
+                    float yh = S.pd[sB3];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const uint4 u = src[q];
+                        const uint32_t words[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                        for (int h = 0; h < 4; ++h) {
+                            const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&words[h]));
+                            yh = __fmaf_rn(S.pd[sW3 + q * 8 + 2 * h], f.x, yh);
+                            yh = __fmaf_rn(S.pd[sW3 + q * 8 + 2 * h + 1], f.y, yh);
+                        }
+                    }
+                    yhat_cached = yh;
+                }
             }
             if (gram) {
                 float x0 = 0.0f;
@@ -553,7 +585,7 @@ __global__ void __launch_bounds__(128)
                 __syncthreads();
                 if (s == 0) {
                     umma::fence_after_sync();
-                    if (exercise)
+                    if (dec_net)
                         for (int kk = 0; kk < 4; ++kk)
                             umma::mma_bf16(tm, desc(S.h1d, 1024, kk), desc(S.w2d, 1024, kk), kIdesc, kk > 0);
                     if (gram)
@@ -567,13 +599,16 @@ __global__ void __launch_bounds__(128)
                 umma::fence_after_sync();
             }
             if (exercise) {
-                float yhat = S.pd[sB3];
-                for (int cc = 0; cc < 4; ++cc) {
-                    float zz[16];
-                    umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, cc * 16), zz);
-                    for (int q = 0; q < 16; ++q) {
-                        float t;
-                        yhat = __fmaf_rn(S.pd[sW3 + cc * 16 + q], gelu(zz[q] + S.pd[sB2 + cc * 16 + q], t), yhat);
+                float yhat = yhat_cached;
+                if (dec_net) {
+                    yhat = S.pd[sB3];
+                    for (int cc = 0; cc < 4; ++cc) {
+                        float zz[16];
+                        umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, cc * 16), zz);
+                        for (int q = 0; q < 16; ++q) {
+                            float t;
+                            yhat = __fmaf_rn(S.pd[sW3 + cc * 16 + q], gelu(zz[q] + S.pd[sB2 + cc * 16 + q], t), yhat);
+                        }
                     }
                 }
                 // predicted time value < 0: exercise
@@ -587,13 +622,24 @@ __global__ void __launch_bounds__(128)
             if (gram) {
                 const bool itm = live && ex_d > 0.0;
                 const float y = itm ? static_cast<float>((v - ex_d) * inv_k) : 0.0f;
+                uint4* dst = fill && itm ? feat_cache + (c.cf_offset + i) * 8 : nullptr;
                 for (int cc = 0; cc < 4; ++cc) {
                     float zz[16];
                     umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 64 + cc * 16), zz);
-                    for (int q = 0; q < 16; ++q) {
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int q = 0; q < 16; q += 2) {
                         float t;
-                        const float h = itm ? gelu(zz[q] + S.pc[sB2 + cc * 16 + q], t) : 0.0f;
-                        *at(S.xt, cc * 16 + q, s, 128) = __float2bfloat16_rn(h);
+                        const float ha = itm ? gelu(zz[q] + S.pc[sB2 + cc * 16 + q], t) : 0.0f;
+                        const float hb = itm ? gelu(zz[q + 1] + S.pc[sB2 + cc * 16 + q + 1], t) : 0.0f;
+                        const __nv_bfloat162 hp = __floats2bfloat162_rn(ha, hb);
+                        *at(S.xt, cc * 16 + q, s, 128) = hp.x;
+                        *at(S.xt, cc * 16 + q + 1, s, 128) = hp.y;
+                        packed[q / 2] = *reinterpret_cast<const uint32_t*>(&hp);
+                    }
+                    if (dst) {  // the decision features of this date, for the next iteration
+                        dst[2 * cc] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                        dst[2 * cc + 1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
                     }
                 }
                 *at(S.xt, 64, s, 128) = __float2bfloat16_rn(itm ? 1.0f : 0.0f);
@@ -1004,19 +1050,25 @@ cudaError_t mlp_prepare() {
 cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int n_contracts,
                                      const uint32_t* group_contract, uint32_t total_groups, const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
-                                     float* gram_part, double* gram_sum, const MlpConfig& cfg, Welford* final_part,
-                                     uint32_t* err, cudaStream_t stream) {
+                                     float* gram_part, double* gram_sum, void* feat_cache, const MlpConfig& cfg,
+                                     Welford* final_part, uint32_t* err, cudaStream_t stream) {
     cudaGetLastError();
     if (total_groups == 0) return cudaSuccess;
     const size_t pass_smem = sizeof(PassSmem);
+    uint4* cache = static_cast<uint4*>(feat_cache);
     auto pass = [&](int mode) {
         if (precision == 0)
             lsm_mlp_pass<0><<<total_groups, 128, pass_smem, stream>>>(k, mode, c, group_contract, total_groups, store,
-                                                                      cf, nets, snaps, snap_ok, gram_part, final_part, err);
+                                                                      cf, nets, snaps, snap_ok, gram_part, final_part,
+                                                                      cache, err);
         else
             lsm_mlp_pass<1><<<total_groups, 128, pass_smem, stream>>>(k, mode, c, group_contract, total_groups, store,
-                                                                      cf, nets, snaps, snap_ok, gram_part, final_part, err);
+                                                                      cf, nets, snaps, snap_ok, gram_part, final_part,
+                                                                      cache, err);
     };
+    // With the features fixed after the first date (no fine-tuning), each
+    // pass reuses the previous pass's features for its decisions.
+    const int reuse = (cache != nullptr && cfg.steps == 0) ? (kCache | kFill) : 0;
     auto trainer = [&]() {
         if (precision == 0)
             lsm_mlp_train<0><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, n_contracts, store, cf, nets, snaps,
@@ -1030,11 +1082,11 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
         return cudaGetLastError();
     }
     if (k == 0) {
-        pass(kStep);                 // terminal cash flows, first discount
-        trainer();                   // learn the features on the latest date
-        pass(kGram);                 // Gram matrix of that date
+        pass(kStep);                        // terminal cash flows, first discount
+        trainer();                          // learn the features on the latest date
+        pass(kGram | (reuse & kFill));      // Gram matrix of that date
     } else {
-        pass(kStep | kGram);         // exercise at date e, discount, Gram of date e-1
+        pass(kStep | kGram | reuse);        // exercise at date e, discount, Gram of date e-1
     }
     const dim3 rgrid((kGramPacked + 127) / 128, static_cast<unsigned>(n_contracts < 65535 ? n_contracts : 65535));
     lsm_mlp_gram_reduce<<<rgrid, 128, 0, stream>>>(k, c, n_contracts, gram_part, gram_sum);
