@@ -304,23 +304,36 @@ __global__ void __launch_bounds__(kLsmThreads)
         for (int q = 0; q < 11; ++q) hi[q] = lo[q] = 0.0f;
         unsigned count = 0;
         double s1 = 0.0, s2 = 0.0;
-        for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+        constexpr int kPer = kLsmChunk / kLsmThreads;
+        // all loads of this thread's paths first (independent, in flight together)
+        float vv[kPer], se[kPer], sd[kPer];
+        bool live[kPer];
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
             const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
-            if (i >= c.path_count) break;
-            float v;
-            if (init) {
-                v = fmaxf(phi * (S[static_cast<uint64_t>(n - 1) * c.path_count + i] - strike), 0.0f);
-            } else {
-                v = cff[i];
-                if (exercise) {
-                    const float s = S[static_cast<uint64_t>(e - 1) * c.path_count + i];
-                    const float ex = phi * (s - strike);
-                    if (ex > 0.0f) {
-                        float b[4];
-                        basis32(s, inv_kf, b);
-                        const float cont = __fmaf_rn(g3f, b[3], __fmaf_rn(g2f, b[2], __fmaf_rn(g1f, b[1], g0f * b[0])));
-                        if (ex > cont) v = ex;
-                    }
+            live[j] = i < c.path_count;
+            vv[j] = 0.0f;
+            se[j] = 0.0f;
+            sd[j] = 0.0f;
+            if (live[j]) {
+                if (init) vv[j] = S[static_cast<uint64_t>(n - 1) * c.path_count + i];
+                else vv[j] = cff[i];
+                if (exercise) se[j] = S[static_cast<uint64_t>(e - 1) * c.path_count + i];
+                if (gram) sd[j] = S[static_cast<uint64_t>(e - 2) * c.path_count + i];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            if (!live[j]) continue;
+            const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
+            float v = init ? fmaxf(phi * (vv[j] - strike), 0.0f) : vv[j];
+            if (exercise) {
+                const float ex = phi * (se[j] - strike);
+                if (ex > 0.0f) {
+                    float b[4];
+                    basis32(se[j], inv_kf, b);
+                    const float cont = __fmaf_rn(g3f, b[3], __fmaf_rn(g2f, b[2], __fmaf_rn(g1f, b[1], g0f * b[0])));
+                    if (ex > cont) v = ex;
                 }
             }
             v *= disc;
@@ -331,23 +344,20 @@ __global__ void __launch_bounds__(kLsmThreads)
                 s2 = fma(vd, vd, s2);
             } else {
                 cff[i] = v;
-                if (gram) {
-                    const float s = S[static_cast<uint64_t>(e - 2) * c.path_count + i];
-                    if (phi * (s - strike) > 0.0f) {
-                        float b[4];
-                        basis32(s, inv_kf, b);
-                        df_add(hi[0], lo[0], 1.0f);
-                        df_add(hi[1], lo[1], b[0] * b[0]);
-                        df_add(hi[2], lo[2], b[0] * b[1]);
-                        df_add(hi[3], lo[3], b[0] * b[2]);
-                        df_add(hi[4], lo[4], b[0] * b[3]);
-                        df_add(hi[5], lo[5], b[1] * b[1]);
-                        df_add(hi[6], lo[6], b[1] * b[2]);
-                        df_add(hi[7], lo[7], b[1] * b[3]);
-                        df_add(hi[8], lo[8], b[2] * b[2]);
-                        df_add(hi[9], lo[9], b[2] * b[3]);
-                        df_add(hi[10], lo[10], b[3] * b[3]);
-                    }
+                if (gram && phi * (sd[j] - strike) > 0.0f) {
+                    float b[4];
+                    basis32(sd[j], inv_kf, b);
+                    df_add(hi[0], lo[0], 1.0f);
+                    df_add(hi[1], lo[1], b[0] * b[0]);
+                    df_add(hi[2], lo[2], b[0] * b[1]);
+                    df_add(hi[3], lo[3], b[0] * b[2]);
+                    df_add(hi[4], lo[4], b[0] * b[3]);
+                    df_add(hi[5], lo[5], b[1] * b[1]);
+                    df_add(hi[6], lo[6], b[1] * b[2]);
+                    df_add(hi[7], lo[7], b[1] * b[3]);
+                    df_add(hi[8], lo[8], b[2] * b[2]);
+                    df_add(hi[9], lo[9], b[2] * b[3]);
+                    df_add(hi[10], lo[10], b[3] * b[3]);
                 }
             }
         }
@@ -509,18 +519,27 @@ __global__ void __launch_bounds__(kLsmThreads)
         float hi[15], lo[15];
 #pragma unroll
         for (int q = 0; q < 15; ++q) hi[q] = lo[q] = 0.0f;
-        for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+        constexpr int kPer = kLsmChunk / kLsmThreads;
+        float sv[kPer], yv[kPer];
+        bool live[kPer];
+        const float* cff = reinterpret_cast<const float*>(cf) + c.cf_offset;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
             const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
-            if (i >= c.path_count) break;
-            const float s = S[static_cast<uint64_t>(date - 1) * c.path_count + i];
-            if (!(phi * (s - strike) > 0.0f)) continue;
+            live[j] = i < c.path_count;
+            sv[j] = live[j] ? S[static_cast<uint64_t>(date - 1) * c.path_count + i] : 0.0f;
+            yv[j] = live[j] ? cff[i] : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            if (!live[j] || !(phi * (sv[j] - strike) > 0.0f)) continue;
             float b[4];
-            basis32(s, inv_kf, b);
+            basis32(sv[j], inv_kf, b);
             const float q0 = b[0] * T[0];
             const float q1 = __fmaf_rn(b[1], T[4], b[0] * T[1]);
             const float q2 = __fmaf_rn(b[2], T[7], __fmaf_rn(b[1], T[5], b[0] * T[2]));
             const float q3 = __fmaf_rn(b[3], T[9], __fmaf_rn(b[2], T[8], __fmaf_rn(b[1], T[6], b[0] * T[3])));
-            const float y = reinterpret_cast<const float*>(cf)[c.cf_offset + i];
+            const float y = yv[j];
             df_add(hi[0], lo[0], 1.0f);
             df_add(hi[1], lo[1], q0 * q0);
             df_add(hi[2], lo[2], q0 * q1);
