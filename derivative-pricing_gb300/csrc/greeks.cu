@@ -261,10 +261,11 @@ __device__ void greeks32(const DevContract& c, const DevGreeks& g, const PhiloxK
         const double h = v[0];
         const double zd = static_cast<double>(z);
         const double sqrt_t = g.sqrt_dt;
-        lr_first_step(h, zd, S0, g.vol, sqrt_t, g.time, o);
-        o[kGLrVega] = h * ((zd * zd - 1.0) / g.vol - sqrt_t * zd);
-        o[kGLrRho] = h * (sqrt_t * zd / g.vol - g.time);
-        o[kGLrTheta] = h * (g.rate - ((zd * zd - 1.0) / (2.0 * g.time) + g.mu * zd / (g.vol * sqrt_t)));
+        o[kGLrDelta] = h * (zd * g.lr_delta_scale);
+        o[kGLrGamma] = h * ((zd * zd - g.vol * sqrt_t * zd - 1.0) * g.lr_gamma_scale);
+        o[kGLrVega] = h * ((zd * zd - 1.0) * g.inv_vol - sqrt_t * zd);
+        o[kGLrRho] = h * (g.sqrt_dt_over_vol * zd - g.time);
+        o[kGLrTheta] = h * (g.rate - ((zd * zd - 1.0) * g.inv_2t + g.mu_over_vol_sqrt_t * zd));
         if constexpr (KIND == kEuropean) {
             const bool itm = phid * (st0 - K) > 0.0;
             const double slope = itm ? phid : 0.0;
@@ -360,15 +361,15 @@ __device__ void greeks32(const DevContract& c, const DevGreeks& g, const PhiloxK
         if constexpr (KIND == kAsianArith || KIND == kAsianGeo) {
             double avg[5];
             if constexpr (KIND == kAsianArith) {
-                const double a = static_cast<double>(acc) / n;
+                const double a = static_cast<double>(acc) * g.inv_n;
                 avg[0] = S0 * a;
                 avg[1] = (S0 + hs) * a;
                 avg[2] = (S0 - hs) * a;
-                avg[3] = avg[0] + S0 * (static_cast<double>(a_up) / n);
-                avg[4] = avg[0] + S0 * (static_cast<double>(a_dn) / n);
+                avg[3] = avg[0] + S0 * (static_cast<double>(a_up) * g.inv_n);
+                avg[4] = avg[0] + S0 * (static_cast<double>(a_dn) * g.inv_n);
             } else {
-                const double gm = exp(static_cast<double>(acc2) / n);
-                const double dbar = static_cast<double>(sd) / n;
+                const double gm = exp(static_cast<double>(acc2) * g.inv_n);
+                const double dbar = static_cast<double>(sd) * g.inv_n;
                 const double ibar = 0.5 * (n + 1.0) * g.dt;  // mean of i dt
                 avg[0] = S0 * gm;
                 avg[1] = (S0 + hs) * gm;
@@ -406,15 +407,18 @@ __device__ void greeks32(const DevContract& c, const DevGreeks& g, const PhiloxK
             }
         }
         const double h = v[0];
-        lr_first_step(h, static_cast<double>(z1), S0, g.vol, g.sqrt_dt, g.dt, o);
+        const double z1d = static_cast<double>(z1);
+        o[kGLrDelta] = h * (z1d * g.lr_delta_scale);
+        o[kGLrGamma] = h * ((z1d * z1d - g.vol * g.sqrt_dt * z1d - 1.0) * g.lr_gamma_scale);
         o[kGLrVega] = h * static_cast<double>(lr_vega);
-        o[kGLrRho] = h * (g.sqrt_dt * static_cast<double>(zsum) / g.vol - g.time);
+        o[kGLrRho] = h * (g.sqrt_dt_over_vol * static_cast<double>(zsum) - g.time);
         if constexpr (KIND == kAsianArith || KIND == kAsianGeo) {
             const bool arith = KIND == kAsianArith;
-            const double d_avg_dspot = avg0 / S0;
-            const double d_avg_dvol = arith ? S0 * static_cast<double>(a_d) / n : avg0 * (static_cast<double>(sd) / n);
+            const double d_avg_dspot = avg0 * g.inv_spot;
+            const double d_avg_dvol =
+                arith ? S0 * static_cast<double>(a_d) * g.inv_n : avg0 * (static_cast<double>(sd) * g.inv_n);
             const double d_avg_drate =
-                arith ? S0 * static_cast<double>(a_r) * g.dt / n : avg0 * (0.5 * (n + 1.0) * g.dt);
+                arith ? S0 * static_cast<double>(a_r) * g.dt * g.inv_n : avg0 * (0.5 * (n + 1.0) * g.dt);
             const double ref = c.floating ? (last0 - avg0) : (avg0 - K);
             const double slope = phid * ref > 0.0 ? phid : 0.0;
             double delta_raw, vega_raw, rate_raw;
@@ -432,9 +436,9 @@ __device__ void greeks32(const DevContract& c, const DevGreeks& g, const PhiloxK
             o[kGPwRho] = disc * rate_raw - g.time * h;
         }
     }
-    o[kGFdDelta] = (v[1] - v[2]) / (2.0 * hs);
-    o[kGFdGamma] = (v[1] - 2.0 * v[0] + v[2]) / (hs * hs);
-    o[kGFdVega] = (v[3] - v[4]) / (2.0 * hv);
+    o[kGFdDelta] = (v[1] - v[2]) * g.inv_2hs;
+    o[kGFdGamma] = (v[1] - 2.0 * v[0] + v[2]) * g.inv_hs2;
+    o[kGFdVega] = (v[3] - v[4]) * g.inv_2hv;
 }
 
 // One slab: per-thread accumulation in path order (FP64: Welford per sample;

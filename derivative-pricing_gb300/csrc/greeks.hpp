@@ -35,6 +35,12 @@ struct DevGreeks {
     double drift_dn, vs_dn;    // ... at vol - h_vol
     double log_h_rel_up;       // ln(H / (S0 + h_spot))  FP32 barrier test of the spot-up state
     double log_h_rel_dn;       // ln(H / (S0 - h_spot))
+    // reciprocals for the FP32 kernel (FP64 divisions are costly on this GPU;
+    // the FP64 kernel keeps the reference's divisions)
+    double inv_2hs, inv_hs2, inv_2hv;
+    double lr_delta_scale;     // 1 / (S0 vol sqrt(dt1)), dt1 = first-step length
+    double lr_gamma_scale;     // 1 / (S0^2 vol^2 dt1)
+    double sqrt_dt_over_vol, inv_vol, inv_n, inv_spot, inv_2t, mu_over_vol_sqrt_t;
 };
 
 cudaError_t launch_greeks_kernel(int precision, int variant, int grid, const DevContract* contracts,

@@ -69,6 +69,17 @@ int plan_greeks(Ctx& ctx, const mcd_contract* cs, size_t n, double spot_rel, dou
             g.log_h_rel_up = std::log(in.barrier / (in.spot + g.h_spot));
             g.log_h_rel_dn = std::log(in.barrier / (in.spot - g.h_spot));
         }
+        g.inv_2hs = 1.0 / (2.0 * g.h_spot);
+        g.inv_hs2 = 1.0 / (g.h_spot * g.h_spot);
+        g.inv_2hv = 1.0 / (2.0 * g.h_vol);
+        g.lr_delta_scale = 1.0 / (in.spot * in.vol * g.sqrt_dt);
+        g.lr_gamma_scale = 1.0 / (in.spot * in.spot * in.vol * in.vol * g.dt);
+        g.sqrt_dt_over_vol = g.sqrt_dt / in.vol;
+        g.inv_vol = 1.0 / in.vol;
+        g.inv_n = 1.0 / static_cast<double>(d.n_steps);
+        g.inv_spot = 1.0 / in.spot;
+        g.inv_2t = 1.0 / (2.0 * in.time);
+        g.mu_over_vol_sqrt_t = g.mu / (in.vol * g.sqrt_dt);
     }
     return MCD_OK;
 }

@@ -88,6 +88,12 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
     hi = s;
 }
 
+// Folded sum i, stored in the 8 bytes of warp 0's (hi, lo) pair of sum i.
+template <int N>
+__device__ __forceinline__ double& smem_out_slot(float (*smem)[N][2], int i) {
+    return *reinterpret_cast<double*>(&smem[0][i][0]);
+}
+
 // Fixed-shape block reduction of N compensated sums (256 threads): warp
 // trees, then thread 0 folds the 8 warps in order; FP64 results in out
 // (valid in thread 0).
@@ -112,14 +118,19 @@ __device__ void block_sum_df(float (&hi)[N], float (&lo)[N], float (*smem)[N][2]
         }
     }
     __syncthreads();
+    // one thread per sum folds the warps in order (a lone FP64 lane costs the
+    // FP64 pipe as much as a full warp, so the N folds run side by side)
+    if (threadIdx.x < N) {
+        const int i = threadIdx.x;
+        double x = 0.0;
+        for (int w = 0; w < kLsmThreads / 32; ++w)
+            x += static_cast<double>(smem[w][i][0]) + static_cast<double>(smem[w][i][1]);
+        smem_out_slot(smem, i) = x;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int i = 0; i < N; ++i) {
-            double x = 0.0;
-            for (int w = 0; w < kLsmThreads / 32; ++w)
-                x += static_cast<double>(smem[w][i][0]) + static_cast<double>(smem[w][i][1]);
-            out[i] = x;
-        }
+        for (int i = 0; i < N; ++i) out[i] = smem_out_slot(smem, i);
     }
 }
 
@@ -205,7 +216,7 @@ __global__ void __launch_bounds__(kLsmThreads)
                  const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_a,
                  Welford* __restrict__ final_part) {
     __shared__ double smem[kLsmThreads / 32][11];
-    __shared__ float smem_f[kLsmThreads / 32][11][2];
+    __shared__ __align__(8) float smem_f[kLsmThreads / 32][11][2];
     __shared__ Welford swf[kLsmThreads / 32];
     const uint32_t chunk = blockIdx.x;
     if (chunk >= total_chunks) return;
@@ -459,7 +470,7 @@ __global__ void __launch_bounds__(kLsmThreads)
                uint32_t total_chunks, const void* __restrict__ store, const double* __restrict__ cf,
                const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_b) {
     __shared__ double smem[kLsmThreads / 32][15];
-    __shared__ float smem_f[kLsmThreads / 32][15][2];
+    __shared__ __align__(8) float smem_f[kLsmThreads / 32][15][2];
     const uint32_t chunk = blockIdx.x;
     if (chunk >= total_chunks) return;
     const LsmDev c = cs[chunk_contract[chunk]];
