@@ -290,6 +290,54 @@ def bench_qmc(eng, c):
             "timing": "wall clock of one mcd_qmc_batch call (host arrays), best of 2 after a warm-up"}
 
 
+PROFILE_CASES = ("path", "greeks", "qmc", "heston", "lsm", "lsm_grid", "mlp", "mlp_grid")
+
+
+def run_case(case):
+    """Small fixed workloads for profiling one kernel family (each priced twice:
+    the second launch is the one to capture).  Sizes keep an ncu capture short:
+      path      256 contracts of the batch configuration (FP32)
+      greeks    64 Asian/barrier contracts, 252 steps, 2^16 paths (FP32)
+      qmc       256 contracts of the batch configuration under Sobol + bridge
+      heston    8 parameter sets x 64 strikes, 252 steps, 2^18 paths
+      lsm       4 puts of the American grid (2^20 paths, 50 dates), FP32 QR
+      lsm_grid  the 20-put grid, FP32 QR
+      mlp       4 puts of the grid, learned regression
+      mlp_grid  the 20-put grid, learned regression"""
+    import mcd_gpu as M
+    eng = M.Engine(0)
+    for _ in range(2):
+        if case == "path":
+            r = eng.price_batch(make_batch(256), "fp32")["price"]
+        elif case == "greeks":
+            c = risk_batch(64)
+            c["path_count"] = 1 << 16
+            r = eng.greeks_batch(c, 1e-4, 1e-4, "fp32")["fd_delta"][:, 0]
+        elif case == "qmc":
+            r = eng.qmc_batch(make_batch(256), "fp32")["price"]
+        elif case == "heston":
+            rng = np.random.default_rng(1)
+            n = 8
+            sets = np.zeros(n, dtype=M.HESTON_DTYPE)
+            sets["spot"], sets["rate"], sets["time"] = 100.0, 0.03, 1.0
+            sets["kappa"] = rng.uniform(0.5, 3.0, n)
+            sets["theta"] = rng.uniform(0.02, 0.09, n)
+            sets["xi"] = rng.uniform(0.2, 1.0, n)
+            sets["rho"] = rng.uniform(-0.9, -0.3, n)
+            sets["v0"] = rng.uniform(0.01, 0.09, n)
+            r = eng.heston_qe_batch(sets, np.linspace(70.0, 130.0, 64), 0, 252, 1 << 18, 42, "fp32")["price"][0]
+        elif case in ("lsm", "lsm_grid", "mlp", "mlp_grid"):
+            g = lsm_grid()
+            if case in ("lsm", "mlp"):
+                g = g[:4]
+            r = eng.lsm_batch(g, "fp32", "mlp" if case.startswith("mlp") else "qr")["price"]
+        else:
+            raise SystemExit(f"unknown case {case!r}; one of {PROFILE_CASES}")
+    print(case, np.asarray(r)[:4])
+    eng.close()
+    return 0
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU algorithm (the oracle port,
     bit-identical to the reference built from source) on the host cores."""
@@ -325,11 +373,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--case", choices=PROFILE_CASES,
+                    help="run one small profiling workload (see run_case) instead of the benchmark")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the LSM, risk, Heston and QMC sections")
     ap.add_argument("--contracts", type=int, default=4096,
                     help="batch size (the configuration is 4096; smaller only for profiling)")
     args = ap.parse_args()
+    if args.case:
+        return run_case(args.case)
     if args.impl == "reference":
         return run_reference(args)
 

@@ -302,12 +302,9 @@ __global__ void __launch_bounds__(kLsmThreads)
         // FP32 paths: FP32 cash flows (stored in the FP64 buffer's space),
         // basis, continuation value, exercise tests and Gram products; the
         // Gram sums are compensated, the final payoff sums FP64.
-        const float phi = c.type == 0 ? 1.0f : -1.0f;
-        const float strike = static_cast<float>(c.strike);
-        const float inv_kf = static_cast<float>(1.0 / c.strike);
-        const float disc = static_cast<float>(c.disc);
-        const float g0f = static_cast<float>(g0), g1f = static_cast<float>(g1), g2f = static_cast<float>(g2),
-                    g3f = static_cast<float>(g3);
+        const float phi = c.phi_f, strike = c.strike_f, inv_kf = c.inv_strike_f, disc = c.disc_f;
+        const float g0f = exercise ? re->gamma_f[0] : 0.0f, g1f = exercise ? re->gamma_f[1] : 0.0f,
+                    g2f = exercise ? re->gamma_f[2] : 0.0f, g3f = exercise ? re->gamma_f[3] : 0.0f;
         const float* S = static_cast<const float*>(store) + c.s_offset;
         float* cff = reinterpret_cast<float*>(cf) + c.cf_offset;
         float hi[11], lo[11];
@@ -460,7 +457,10 @@ __global__ void lsm_solve_a(int k, const LsmDev* __restrict__ cs, int n_contract
         r.degenerate = 1;
     }
     for (int a = 0; a < 4; ++a)
-        for (int b2 = a; b2 < 4; ++b2) r.T[tri(a, b2)] = T[a][b2];
+        for (int b2 = a; b2 < 4; ++b2) {
+            r.T[tri(a, b2)] = T[a][b2];
+            r.T_f[tri(a, b2)] = static_cast<float>(T[a][b2]);
+        }
 }
 
 // Pass B: Gram sums and right-hand side in the preconditioned basis b' = b T.
@@ -522,10 +522,8 @@ __global__ void __launch_bounds__(kLsmThreads)
     } else {
         float T[10];
 #pragma unroll
-        for (int q = 0; q < 10; ++q) T[q] = static_cast<float>(r.T[q]);
-        const float phi = c.type == 0 ? 1.0f : -1.0f;
-        const float strike = static_cast<float>(c.strike);
-        const float inv_kf = static_cast<float>(1.0 / c.strike);
+        for (int q = 0; q < 10; ++q) T[q] = r.T_f[q];
+        const float phi = c.phi_f, strike = c.strike_f, inv_kf = c.inv_strike_f;
         const float* S = static_cast<const float*>(store) + c.s_offset;
         float hi[15], lo[15];
 #pragma unroll
@@ -640,6 +638,7 @@ __global__ void lsm_solve_b(int k, const LsmDev* __restrict__ cs, int n_contract
         double x = 0.0;
         for (int b2 = a; b2 < 4; ++b2) x += r.T[tri(a, b2)] * beta[b2];
         r.gamma[a] = x;
+        r.gamma_f[a] = static_cast<float>(x);
     }
     r.has = 1;
 }

@@ -28,6 +28,7 @@ struct LsmDev {
     int32_t n_steps, type;
     uint32_t group_begin, n_groups;  // learned regression: CTAs of group_chunks chunks each
     uint32_t group_chunks;
+    float strike_f, inv_strike_f, disc_f, phi_f;  // FP32 copies for the FP32-path kernels
 };
 
 constexpr int kLsmMaxGroups = 256;  // learned-regression CTAs per contract at most
@@ -41,6 +42,8 @@ struct LsmReg {
     double gamma[4];
     int32_t has;          // coefficients valid at this date (>= 4 ITM paths)
     int32_t degenerate;   // Cholesky of the first pass failed; solved without preconditioning
+    float T_f[10];        // FP32 copies for the FP32-path kernels (written with T and gamma)
+    float gamma_f[4];
 };
 
 // Per-chunk partial sums.  Pass A: count + 10 Gram entries.  Pass B: count +

@@ -56,6 +56,10 @@ int plan_lsm(Ctx& ctx, const mcd_lsm_contract* cs, size_t n, LsmPlan& p) {
         const double phi = c.type == 0 ? 1.0 : -1.0;
         const double x = phi * (c.spot - c.strike);
         d.inception = x > 0.0 ? x : 0.0;
+        d.strike_f = static_cast<float>(c.strike);
+        d.inv_strike_f = static_cast<float>(1.0 / c.strike);
+        d.disc_f = static_cast<float>(d.disc);
+        d.phi_f = c.type == 0 ? 1.0f : -1.0f;
         d.seed = c.seed;
         d.path_count = c.path_count;
         d.n_steps = c.monitoring_points;
@@ -328,7 +332,10 @@ int mcd_lsm_reprice_frozen(mcd_ctx* handle, double spot, double strike, double r
     for (int d = 1; d < monitoring_points; ++d) {
         if (!has_coefficients[d]) continue;
         reg[d].has = 1;
-        for (int b = 0; b < 4; ++b) reg[d].gamma[b] = coefficients[4 * d + b];
+        for (int b = 0; b < 4; ++b) {
+            reg[d].gamma[b] = coefficients[4 * d + b];
+            reg[d].gamma_f[b] = static_cast<float>(coefficients[4 * d + b]);
+        }
     }
     std::vector<double> out;
     rc = upload_and_run(*ctx, p, precision, true, &reg, out);

@@ -426,7 +426,6 @@ __global__ void __launch_bounds__(128, 1)
 // ---------------------------------------------------------------------------
 constexpr int kGramN = 80;    // MMA N of the Gram product (66 used)
 constexpr int kGramDim = 66;  // 64 features, bias, target
-constexpr int kSmall = 321;   // W1, b1 (as layout), then b2, W3, b3 copied below
 
 struct __align__(1024) PassSmem {
     __nv_bfloat16 h1d[128 * 64];   // decision network input tile (S at date e)
@@ -693,6 +692,224 @@ __global__ void __launch_bounds__(128)
             }
         }
         if (!ok) umma::mbar_wait(&S.mbar, phase, err, 13);
+        umma::fence_before_sync();
+        __syncthreads();
+        if (warp == 0) umma::tmem_dealloc(tm, 256);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The same pass with cached decision features, two tiles per CTA: 256 threads
+// work on 256-path tiles; the two halves' Z2 = H1 W2^T go to tensor-memory
+// columns [0,64) and [64,128), and one Gram MMA with K = 256 paths
+// accumulates both halves into columns [128,208).  Twice the resident warps
+// of lsm_mlp_pass for the same 256 tensor-memory columns per CTA.  Used for
+// the cached modes only (no decision network to evaluate).
+// ---------------------------------------------------------------------------
+constexpr int kWideThreads = 256;
+
+struct __align__(1024) WideSmem {
+    __nv_bfloat16 h1c[2][128 * 64];  // current network input, one 128-path half each
+    __nv_bfloat16 xt[128 * 256];     // Gram operand [row][path]; rows 66..127 stay zero
+    __nv_bfloat16 w2c[64 * 64];
+    float pc[kParamStride - 4096];   // current network without W2
+    float pd[kParamStride - 4096];   // decision output layer (b2 W3 b3 at the small-layout slots)
+    uint64_t mbar;
+    uint32_t tmem_base;
+};
+
+template <int PREC>
+__global__ void __launch_bounds__(kWideThreads)
+    lsm_mlp_pass_wide(int k, int mode, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
+                      uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
+                      const float* __restrict__ nets, const float* __restrict__ snaps,
+                      const int* __restrict__ snap_ok, float* __restrict__ gram_part,
+                      Welford* __restrict__ final_part, uint4* __restrict__ feat_cache, uint32_t* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    WideSmem& S = *reinterpret_cast<WideSmem*>(smem_raw);
+    __shared__ Welford swf[kWideThreads / 32];
+    const uint32_t g = blockIdx.x;
+    if (g >= total_groups) return;
+    const uint32_t ci = group_contract[g];
+    const LsmDev c = cs[ci];
+    const int n = c.n_steps;
+    const int e = n - k;
+    if (e < 1) return;
+    const bool step = (mode & kStep) != 0;
+    const bool init = step && k == 0;
+    const bool last = step && e == 1;
+    const bool exercise = step && k > 0 && e <= n - 1 && snap_ok[c.reg_offset + e] == 1;  // cached features
+    const bool gram = (mode & kGram) != 0 && e - 1 >= 1;
+    const bool fill = (mode & kFill) != 0;
+    if (!step && !gram) return;
+    const int s = threadIdx.x, warp = s >> 5, half = s >> 7, row = s & 127;
+    const double phi = c.type == 0 ? 1.0 : -1.0;
+    const double inv_k = 1.0 / c.strike;
+    if (exercise) {
+        const float* net = snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride;
+        for (int i = s; i < kParams - kB2; i += kWideThreads) S.pd[kW2 + i] = net[kB2 + i];
+    }
+    if (gram) {
+        const float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
+        for (int i = s; i < kW2; i += kWideThreads) S.pc[i] = net[i];
+        for (int i = s; i < kParams - kB2; i += kWideThreads) S.pc[kW2 + i] = net[kB2 + i];
+        if (s < 64)
+            for (int j = 0; j < 64; j += 2)
+                *reinterpret_cast<__nv_bfloat162*>(at(S.w2c, s, j, 64)) =
+                    __floats2bfloat162_rn(net[kW2 + s * 64 + j], net[kW2 + s * 64 + j + 1]);
+        for (int i = s; i < 128 * 256 / 2; i += kWideThreads) reinterpret_cast<uint32_t*>(S.xt)[i] = 0u;
+        if (s == 0) umma::mbar_init(&S.mbar, 1);
+        if (warp == 0) umma::tmem_alloc(&S.tmem_base, 256);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        umma::fence_before_sync();
+    }
+    __syncthreads();
+    if (gram) umma::fence_after_sync();
+    const uint32_t tm = gram ? S.tmem_base : 0u;
+    uint32_t phase = 0;
+    bool ok = true;
+    bool gram_pending = false, gram_started = false;
+    const float x1d = static_cast<float>(n - (e - 1)) / static_cast<float>(n);
+    const uint32_t gl = g - c.group_begin;
+    const uint32_t chunk0 = gl * c.group_chunks;
+    const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
+    Welford w{0ull, 0.0, 0.0};
+    for (uint32_t ch = chunk0; ch < chunk1; ++ch) {
+        for (int tile = 0; tile < kLsmChunk / kWideThreads; ++tile) {
+            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + tile * kWideThreads + s;
+            const bool live = i < c.path_count;
+            double v = 0.0, ex_e = 0.0, ex_d = 0.0;
+            if (live) {
+                if (init) {
+                    const double sT = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(n - 1) * c.path_count + i);
+                    const double x = phi * (sT - c.strike);
+                    v = x > 0.0 ? x : 0.0;
+                } else {
+                    v = cf_load<PREC>(cf, c.cf_offset + i);
+                }
+            }
+            if (exercise && live) {
+                const double se = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 1) * c.path_count + i);
+                const double xx = phi * (se - c.strike);
+                ex_e = xx > 0.0 ? xx : 0.0;
+                if (ex_e > 0.0) {
+                    const uint4* src = feat_cache + (c.cf_offset + i) * 8;
+                    float yh = S.pd[sB3];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const uint4 u = src[q];
+                        const uint32_t words[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                        for (int h = 0; h < 4; ++h) {
+                            const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&words[h]));
+                            yh = __fmaf_rn(S.pd[sW3 + q * 8 + 2 * h], f.x, yh);
+                            yh = __fmaf_rn(S.pd[sW3 + q * 8 + 2 * h + 1], f.y, yh);
+                        }
+                    }
+                    if (yh < 0.0f) v = ex_e;  // predicted time value < 0: exercise
+                }
+            }
+            if (live && step) {
+                v *= c.disc;
+                if (last) welford_add(w, v);
+                else cf_store<PREC>(cf, c.cf_offset + i, v);
+            }
+            if (gram) {
+                float x0 = 0.0f;
+                if (live) {
+                    const double s_d = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 2) * c.path_count + i);
+                    const double xx = phi * (s_d - c.strike);
+                    ex_d = xx > 0.0 ? xx : 0.0;
+                    x0 = static_cast<float>(4.0 * (s_d * inv_k - 1.0));
+                }
+                layer1_row(S.pc, x0, x1d, S.h1c[half], row);
+                umma::fence_smem_to_async();
+                umma::fence_before_sync();
+                __syncthreads();
+                if (s == 0) {
+                    umma::fence_after_sync();
+                    for (int hh = 0; hh < 2; ++hh)
+                        for (int kk = 0; kk < 4; ++kk)
+                            umma::mma_bf16(tm + 64 * hh, desc(S.h1c[hh], 1024, kk), desc(S.w2c, 1024, kk), kIdesc,
+                                           kk > 0);
+                    umma::mma_commit(&S.mbar);  // also covers the previous tile's Gram MMA
+                }
+                ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 21));
+                phase ^= 1u;
+                gram_pending = false;
+                umma::fence_after_sync();
+                const bool itm = live && ex_d > 0.0;
+                const float y = itm ? static_cast<float>((v - ex_d) * inv_k) : 0.0f;
+                uint4* dst = fill && itm ? feat_cache + (c.cf_offset + i) * 8 : nullptr;
+                for (int cc = 0; cc < 4; ++cc) {
+                    float zz[16];
+                    umma::tmem_ld16(umma::tmem_addr(tm, 32 * (warp & 3), 64 * half + cc * 16), zz);
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int q = 0; q < 16; q += 2) {
+                        float t;
+                        const float ha = itm ? gelu(zz[q] + S.pc[sB2 + cc * 16 + q], t) : 0.0f;
+                        const float hb = itm ? gelu(zz[q + 1] + S.pc[sB2 + cc * 16 + q + 1], t) : 0.0f;
+                        const __nv_bfloat162 hp = __floats2bfloat162_rn(ha, hb);
+                        *at(S.xt, cc * 16 + q, s, 256) = hp.x;
+                        *at(S.xt, cc * 16 + q + 1, s, 256) = hp.y;
+                        packed[q / 2] = *reinterpret_cast<const uint32_t*>(&hp);
+                    }
+                    if (dst) {
+                        dst[2 * cc] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                        dst[2 * cc + 1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                    }
+                }
+                *at(S.xt, 64, s, 256) = __float2bfloat16_rn(itm ? 1.0f : 0.0f);
+                *at(S.xt, 65, s, 256) = __float2bfloat16_rn(y);
+                umma::fence_smem_to_async();
+                umma::fence_before_sync();
+                __syncthreads();
+                if (s == 0) {
+                    umma::fence_after_sync();
+                    // D[i][j] += sum over the 256 paths of xt[i][p] xt[j][p]  (M = 128, N = 80, K = 256)
+                    for (int kk = 0; kk < 16; ++kk)
+                        umma::mma_bf16(tm + 128, desc(S.xt, 4096, kk), desc(S.xt, 4096, kk),
+                                       umma::idesc_bf16(128, kGramN), gram_started || kk > 0);
+                }
+                gram_started = true;
+                gram_pending = true;
+            }
+        }
+        if (last) {  // one final partial per chunk, fixed tree
+            Welford r = welford_warp_reduce(w);
+            if ((s & 31) == 0) swf[warp] = r;
+            __syncthreads();
+            if (s == 0) {
+                Welford m = swf[0];
+                for (int q = 1; q < kWideThreads / 32; ++q) m = welford_merge(m, swf[q]);
+                final_part[c.chunk_begin + ch] = m;
+            }
+            __syncthreads();
+            w = Welford{0ull, 0.0, 0.0};
+        }
+    }
+    if (gram) {
+        if (gram_pending) {
+            if (s == 0) umma::mma_commit(&S.mbar);
+            ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 22));
+            phase ^= 1u;
+            umma::fence_after_sync();
+        }
+        float* out = gram_part + static_cast<size_t>(g) * kGramPacked;
+        if (warp < 3) {  // lanes 0..95 hold rows 0..95; the upper triangle of rows 0..65 is kept
+            const int row0 = s * kGramDim - s * (s - 1) / 2;
+            for (int cc = 0; cc < 5; ++cc) {
+                float dd[16];
+                umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 128 + cc * 16), dd);
+                if (s < kGramDim)
+                    for (int q = 0; q < 16; ++q) {
+                        const int col = cc * 16 + q;
+                        if (col >= s && col < kGramDim) out[row0 + col - s] = ok ? dd[q] : 0.0f;
+                    }
+            }
+        }
+        if (!ok) umma::mbar_wait(&S.mbar, phase, err, 23);
         umma::fence_before_sync();
         __syncthreads();
         if (warp == 0) umma::tmem_dealloc(tm, 256);
@@ -1043,6 +1260,8 @@ cudaError_t mlp_prepare() {
     if (e == cudaSuccess) e = set_smem(mlp_grad_kernel, sizeof(TrainSmem));
     if (e == cudaSuccess) e = set_smem(lsm_mlp_pass<0>, sizeof(PassSmem));
     if (e == cudaSuccess) e = set_smem(lsm_mlp_pass<1>, sizeof(PassSmem));
+    if (e == cudaSuccess) e = set_smem(lsm_mlp_pass_wide<0>, sizeof(WideSmem));
+    if (e == cudaSuccess) e = set_smem(lsm_mlp_pass_wide<1>, sizeof(WideSmem));
     if (e == cudaSuccess) e = set_smem(mlp_forward_kernel, sizeof(InferSmem));
     return e;
 }
@@ -1067,8 +1286,20 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
                                                                       cache, err);
     };
     // With the features fixed after the first date (no fine-tuning), each
-    // pass reuses the previous pass's features for its decisions.
+    // pass reuses the previous pass's features for its decisions and runs as
+    // the two-tile kernel.
     const int reuse = (cache != nullptr && cfg.steps == 0) ? (kCache | kFill) : 0;
+    auto pass_wide = [&](int mode) {
+        const size_t smem = sizeof(WideSmem);
+        if (precision == 0)
+            lsm_mlp_pass_wide<0><<<total_groups, kWideThreads, smem, stream>>>(
+                k, mode, c, group_contract, total_groups, store, cf, nets, snaps, snap_ok, gram_part, final_part,
+                cache, err);
+        else
+            lsm_mlp_pass_wide<1><<<total_groups, kWideThreads, smem, stream>>>(
+                k, mode, c, group_contract, total_groups, store, cf, nets, snaps, snap_ok, gram_part, final_part,
+                cache, err);
+    };
     auto trainer = [&]() {
         if (precision == 0)
             lsm_mlp_train<0><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, n_contracts, store, cf, nets, snaps,
@@ -1084,9 +1315,12 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
     if (k == 0) {
         pass(kStep);                        // terminal cash flows, first discount
         trainer();                          // learn the features on the latest date
-        pass(kGram | (reuse & kFill));      // Gram matrix of that date
+        if (reuse) pass_wide(kGram | kFill);  // Gram matrix of that date
+        else pass(kGram);
+    } else if (reuse) {
+        pass_wide(kStep | kGram | reuse);   // exercise at date e (cached features), discount, Gram of date e-1
     } else {
-        pass(kStep | kGram | reuse);        // exercise at date e, discount, Gram of date e-1
+        pass(kStep | kGram);
     }
     const dim3 rgrid((kGramPacked + 127) / 128, static_cast<unsigned>(n_contracts < 65535 ? n_contracts : 65535));
     lsm_mlp_gram_reduce<<<rgrid, 128, 0, stream>>>(k, c, n_contracts, gram_part, gram_sum);
