@@ -592,15 +592,20 @@ cudaError_t launch_greeks_kernel(int precision, int variant, int grid, const Dev
                                  const DevGreeks* greeks, int n_contracts, const uint32_t* item_prefix,
                                  uint32_t total_items, uint32_t* ticket, Welford* partials,
                                  uint32_t* error_flag, cudaStream_t stream) {
-    if (precision == 0)
-        return variant == 0 ? launch_one<0, 2>(grid, contracts, greeks, n_contracts, item_prefix, total_items, ticket,
-                                               partials, error_flag, stream)
-                            : launch_one<0, 4>(grid, contracts, greeks, n_contracts, item_prefix, total_items, ticket,
-                                               partials, error_flag, stream);
-    return variant == 0 ? launch_one<1, 2>(grid, contracts, greeks, n_contracts, item_prefix, total_items, ticket,
-                                           partials, error_flag, stream)
-                        : launch_one<1, 4>(grid, contracts, greeks, n_contracts, item_prefix, total_items, ticket,
-                                           partials, error_flag, stream);
+#define MCD_GREEKS_ARGS grid, contracts, greeks, n_contracts, item_prefix, total_items, ticket, partials, error_flag, stream
+    if (precision == 0) {
+        switch (variant) {
+            case 0: return launch_one<0, 2>(MCD_GREEKS_ARGS);
+            case 1: return launch_one<0, 4>(MCD_GREEKS_ARGS);
+            default: return launch_one<0, 6>(MCD_GREEKS_ARGS);
+        }
+    }
+    switch (variant) {
+        case 0: return launch_one<1, 2>(MCD_GREEKS_ARGS);
+        case 1: return launch_one<1, 4>(MCD_GREEKS_ARGS);
+        default: return launch_one<1, 6>(MCD_GREEKS_ARGS);
+    }
+#undef MCD_GREEKS_ARGS
 }
 
 cudaError_t launch_greeks_merge(const DevContract* contracts, int n_contracts, const uint32_t* item_prefix,
@@ -616,12 +621,18 @@ cudaError_t launch_greeks_merge(const DevContract* contracts, int n_contracts, c
 }
 
 cudaError_t greeks_kernel_occupancy(int precision, int variant, int* blocks) {
-    if (precision == 0)
-        return variant == 0
-                   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<0, 2>, kSlabThreads, 0)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<0, 4>, kSlabThreads, 0);
-    return variant == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<1, 2>, kSlabThreads, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<1, 4>, kSlabThreads, 0);
+    if (precision == 0) {
+        switch (variant) {
+            case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<0, 2>, kSlabThreads, 0);
+            case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<0, 4>, kSlabThreads, 0);
+            default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<0, 6>, kSlabThreads, 0);
+        }
+    }
+    switch (variant) {
+        case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<1, 2>, kSlabThreads, 0);
+        case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<1, 4>, kSlabThreads, 0);
+        default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<1, 6>, kSlabThreads, 0);
+    }
 }
 
 }  // namespace mcdg

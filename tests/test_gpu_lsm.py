@@ -119,3 +119,27 @@ def test_invalid_lsm_arguments(engine, gpu_lib):
         engine.monte_carlo_lsm_american(36, 40, .06, 0, .2, 1, 1, 0, 1000, 1)
     with pytest.raises(gpu_lib.McdError):
         engine.monte_carlo_lsm_american(36, -40, .06, 0, .2, 1, 1, 10, 1000, 1)
+
+
+def test_frozen_boundary_delta_has_lower_variance_than_naive_refit(engine):
+    # tests/lsm_test.cpp:138-185 on the GPU: delta by CRN spot bumps of the
+    # frozen base policy against delta by re-fitting LSM at each bumped spot,
+    # over 40 seeds; the frozen estimator must have the smaller spread.
+    s, k, r, q, v, t, h = 100.0, 100.0, 0.05, 0.0, 0.25, 1.0, 0.1
+    paths, n = 5000, 20
+    frozen, naive = [], []
+    for trial in range(40):
+        seed = 42 + trial * 1013
+        base, co, hq = engine.monte_carlo_lsm_american(s, k, r, q, v, t, 1, n, paths, seed, policy=True)
+        up = engine.reprice_against_frozen_policy(s + h, k, r, q, v, t, 1, n, paths, seed, co, hq,
+                                                  base.exercise_at_inception)
+        dn = engine.reprice_against_frozen_policy(s - h, k, r, q, v, t, 1, n, paths, seed, co, hq,
+                                                  base.exercise_at_inception)
+        frozen.append((up - dn) / (2 * h))
+        nu = engine.monte_carlo_lsm_american(s + h, k, r, q, v, t, 1, n, paths, seed).price
+        nd = engine.monte_carlo_lsm_american(s - h, k, r, q, v, t, 1, n, paths, seed).price
+        naive.append((nu - nd) / (2 * h))
+    sf, sn = float(np.std(frozen, ddof=1)), float(np.std(naive, ddof=1))
+    print(f"frozen-boundary delta sd {sf:.5f}, naive refit sd {sn:.5f}, ratio {sn / sf:.2f}")
+    assert sf < sn
+    assert -0.6 < float(np.mean(frozen)) < -0.2  # an at-the-money American put's delta
