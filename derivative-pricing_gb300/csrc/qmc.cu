@@ -48,10 +48,22 @@ __device__ __forceinline__ uint32_t sobol_x(const uint32_t* __restrict__ dirs, u
     return x;
 }
 
-__device__ __forceinline__ uint32_t gray_of(uint64_t path) {
-    const uint64_t index = path + 1;  // Sobol indices 1..N
-    return static_cast<uint32_t>(index ^ (index >> 1));  // 32 direction bits: higher bits do not contribute
-}
+// Sobol coordinates of a warp's 32 consecutive indices.  Path p has index
+// I = p + 1; a warp's paths are B .. B+31 with B a multiple of 32, so
+// I = B' + low with B' in {B, B + 32} (B + 32 for the last lane only) and
+// low < 32, and gray(B' + low) = gray(B') ^ gray(low).  The coordinate is
+// linear in the Gray-code bits over GF(2): x(I) = X(B') ^ Y(low).  X is
+// computed once per warp and dimension (lanes share the dimensions) into
+// shared memory; Y depends on the lane and dimension only and is a table
+// (kSobolDims x 32, uploaded with the directions).  A draw is then one XOR
+// of two loads instead of a loop over the set bits of the index.
+struct SobolLane {
+    const uint32_t* x;  // this warp's X for this lane's B' (indexed by dimension)
+    const uint32_t* y;  // Y table column of this lane (stride 32)
+    __device__ __forceinline__ uint32_t operator()(uint32_t dim) const { return x[dim] ^ __ldg(y + dim * 32u); }
+};
+
+constexpr int kSxStride = kSobolDims + 1;  // +1 word: the last lane's row sits in another bank
 
 struct QmcTables {
     BridgeNode node[kSobolDims];
@@ -87,12 +99,10 @@ __device__ void fill_tables(const DevContract& c, const DevQmc& q, const BridgeN
 }
 
 template <int KIND>
-__device__ double sample_qmc64(const DevContract& c, const DevQmc& q, const QmcTables& S,
-                               const uint32_t* __restrict__ dirs, uint64_t path) {
+__device__ double sample_qmc64(const DevContract& c, const DevQmc& q, const QmcTables& S, const SobolLane& sob) {
     const double phi = c.type == 0 ? 1.0 : -1.0;
-    const uint32_t gray = gray_of(path);
     if constexpr (KIND == kEuropean || KIND == kDigital) {  // qmc.cpp:20-27
-        const double z = inv_normal_cdf_f64(static_cast<double>(sobol_x(dirs, 0u, gray)) * (1.0 / 4294967296.0));
+        const double z = inv_normal_cdf_f64(static_cast<double>(sob(0u)) * (1.0 / 4294967296.0));
         const double s = c.spot * exp(c.drift + c.vs * z);
         if constexpr (KIND == kEuropean) {
             return c.discount * dmax(phi * (s - c.strike), 0.0);
@@ -108,7 +118,7 @@ __device__ double sample_qmc64(const DevContract& c, const DevQmc& q, const QmcT
         bool breached = false;
         for (int e = 0; e < n; ++e) {
             const BridgeNode& b = S.node[e];
-            const double z = inv_normal_cdf_f64(static_cast<double>(sobol_x(dirs, b.dim, gray)) * (1.0 / 4294967296.0));
+            const double z = inv_normal_cdf_f64(static_cast<double>(sob(b.dim)) * (1.0 / 4294967296.0));
             double val;
             if (b.t_left < 0 && b.t_right < 0) {
                 val = S.sd[e] * z;
@@ -149,14 +159,12 @@ __device__ double sample_qmc64(const DevContract& c, const DevQmc& q, const QmcT
 
 // FP32: log-space spots x = ln(S/S0), FP32 payoff, FP64 accumulation.
 template <int KIND>
-__device__ double sample_qmc32(const DevContract& c, const DevQmc& q, const QmcTables& S,
-                               const uint32_t* __restrict__ dirs, uint64_t path) {
+__device__ double sample_qmc32(const DevContract& c, const DevQmc& q, const QmcTables& S, const SobolLane& sob) {
     const float phi = c.type == 0 ? 1.0f : -1.0f;
     const float s0 = static_cast<float>(c.spot);
     const float strike = static_cast<float>(c.strike);
-    const uint32_t gray = gray_of(path);
     if constexpr (KIND == kEuropean || KIND == kDigital) {
-        const float z = normal_from_sobol_f32(sobol_x(dirs, 0u, gray));
+        const float z = normal_from_sobol_f32(sob(0u));
         const float s = s0 * __expf(__fmaf_rn(static_cast<float>(c.vs), z, static_cast<float>(c.drift)));
         float payoff;
         if constexpr (KIND == kEuropean) {
@@ -176,7 +184,7 @@ __device__ double sample_qmc32(const DevContract& c, const DevQmc& q, const QmcT
         bool breached = false;
         for (int e = 0; e < n; ++e) {
             const BridgeNode& b = S.node[e];
-            const float z = normal_from_sobol_f32(sobol_x(dirs, b.dim, gray));
+            const float z = normal_from_sobol_f32(sob(b.dim));
             const float sd = S.sdf[e];
             float val;
             if (b.t_left < 0 && b.t_right < 0) {
@@ -222,41 +230,54 @@ __device__ double sample_qmc32(const DevContract& c, const DevQmc& q, const QmcT
 
 template <int PREC, int KIND>
 __device__ Welford slab_qmc(const DevContract& c, const DevQmc& q, const QmcTables& S,
-                            const uint32_t* __restrict__ dirs, uint64_t base) {
-    if constexpr (PREC == 0) {
-        Welford w{0ull, 0.0, 0.0};
-        for (int j = 0; j < kPathsPerThread; ++j) {
-            const uint64_t path = base + static_cast<uint64_t>(j * kSlabThreads) + threadIdx.x;
-            if (path >= c.path_count) break;
-            welford_add(w, sample_qmc64<KIND>(c, q, S, dirs, path));
+                            const uint32_t* __restrict__ dirs, const uint32_t* __restrict__ ytab, uint32_t* sx,
+                            uint64_t base) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t ndims = (KIND == kEuropean || KIND == kDigital) ? 1u : static_cast<uint32_t>(c.n_steps);
+    uint32_t* xw = sx + warp * 2 * kSxStride;
+    const SobolLane sob{xw + (lane == 31 ? kSxStride : 0), ytab + lane};
+    Welford w{0ull, 0.0, 0.0};
+    unsigned count = 0;
+    double s1 = 0.0, s2 = 0.0;
+    for (int j = 0; j < kPathsPerThread; ++j) {
+        const uint64_t b0 = base + static_cast<uint64_t>(j * kSlabThreads) + 32u * warp;  // this warp's first path
+        if (b0 >= c.path_count) break;  // uniform per warp
+        // X for index bases B = b0 (lanes 0..30) and B + 32 (lane 31), dimensions spread over the lanes
+        const uint32_t g0 = static_cast<uint32_t>(b0 ^ (b0 >> 1));
+        const uint32_t g1 = static_cast<uint32_t>((b0 + 32) ^ ((b0 + 32) >> 1));
+        __syncwarp();
+        for (uint32_t d = lane; d < ndims; d += 32) {
+            xw[d] = sobol_x(dirs, d, g0);
+            xw[kSxStride + d] = sobol_x(dirs, d, g1);
         }
-        return w;
-    } else {
-        unsigned count = 0;
-        double s1 = 0.0, s2 = 0.0;
-        for (int j = 0; j < kPathsPerThread; ++j) {
-            const uint64_t path = base + static_cast<uint64_t>(j * kSlabThreads) + threadIdx.x;
-            if (path >= c.path_count) break;
-            const double v = sample_qmc32<KIND>(c, q, S, dirs, path);
+        __syncwarp();
+        const uint64_t path = b0 + lane;
+        if (path >= c.path_count) continue;
+        if constexpr (PREC == 0) {
+            welford_add(w, sample_qmc64<KIND>(c, q, S, sob));
+        } else {
+            const double v = sample_qmc32<KIND>(c, q, S, sob);
             ++count;
             s1 += v;
             s2 = fma(v, v, s2);
         }
-        return welford_from_sums(count, s1, s2);
     }
+    if constexpr (PREC == 1) w = welford_from_sums(count, s1, s2);
+    return w;
 }
 
 template <int PREC>
 __device__ Welford run_qmc_slab(const DevContract& c, const DevQmc& q, const QmcTables& S,
-                                const uint32_t* __restrict__ dirs, uint64_t base) {
+                                const uint32_t* __restrict__ dirs, const uint32_t* __restrict__ ytab, uint32_t* sx,
+                                uint64_t base) {
     switch (c.kind) {
-        case kEuropean: return slab_qmc<PREC, kEuropean>(c, q, S, dirs, base);
-        case kDigital: return slab_qmc<PREC, kDigital>(c, q, S, dirs, base);
-        case kAsianArith: return slab_qmc<PREC, kAsianArith>(c, q, S, dirs, base);
-        case kAsianGeo: return slab_qmc<PREC, kAsianGeo>(c, q, S, dirs, base);
-        case kBarrier: return slab_qmc<PREC, kBarrier>(c, q, S, dirs, base);
-        case kLookbackFixed: return slab_qmc<PREC, kLookbackFixed>(c, q, S, dirs, base);
-        default: return slab_qmc<PREC, kLookbackFloating>(c, q, S, dirs, base);
+        case kEuropean: return slab_qmc<PREC, kEuropean>(c, q, S, dirs, ytab, sx, base);
+        case kDigital: return slab_qmc<PREC, kDigital>(c, q, S, dirs, ytab, sx, base);
+        case kAsianArith: return slab_qmc<PREC, kAsianArith>(c, q, S, dirs, ytab, sx, base);
+        case kAsianGeo: return slab_qmc<PREC, kAsianGeo>(c, q, S, dirs, ytab, sx, base);
+        case kBarrier: return slab_qmc<PREC, kBarrier>(c, q, S, dirs, ytab, sx, base);
+        case kLookbackFixed: return slab_qmc<PREC, kLookbackFixed>(c, q, S, dirs, ytab, sx, base);
+        default: return slab_qmc<PREC, kLookbackFloating>(c, q, S, dirs, ytab, sx, base);
     }
 }
 
@@ -266,6 +287,8 @@ __global__ void __launch_bounds__(kSlabThreads)
                const uint32_t* __restrict__ item_prefix, uint32_t total_items,
                const BridgeNode* __restrict__ programs, const uint32_t* __restrict__ dirs,
                uint32_t* __restrict__ ticket, Welford* __restrict__ partials, uint32_t* __restrict__ error_flag) {
+    const uint32_t* ytab = dirs + kSobolDims * kSobolBits;  // Y table follows the directions
+    __shared__ uint32_t s_sx[(kSlabThreads / 32) * 2 * kSxStride];
     __shared__ uint32_t s_item;
     __shared__ Welford s_warp[kSlabThreads / 32];
     __shared__ DevContract s_c;
@@ -309,7 +332,7 @@ __global__ void __launch_bounds__(kSlabThreads)
             if (threadIdx.x == 0) atomicOr(error_flag, 1u);
             continue;
         }
-        Welford w = run_qmc_slab<PREC>(s_c, s_q, S, dirs, static_cast<uint64_t>(slab) * kSlabPaths);
+        Welford w = run_qmc_slab<PREC>(s_c, s_q, S, dirs, ytab, s_sx, static_cast<uint64_t>(slab) * kSlabPaths);
         w = welford_warp_reduce(w);
         if (lane == 0) s_warp[warp] = w;
         __syncthreads();

@@ -48,6 +48,8 @@ bool primitive(unsigned s, uint32_t interior) {
     return false;
 }
 
+// Direction numbers (kSobolDims x 32, dims-major) followed by the warp
+// decomposition's Y table (kSobolDims x 32 lanes).
 std::vector<uint32_t> sobol_directions() {
     std::vector<std::pair<unsigned, uint32_t>> polys;
     for (int d = 0; d < 7; ++d) polys.emplace_back(kRefDegree[d], kRefInterior[d]);
@@ -77,6 +79,19 @@ std::vector<uint32_t> sobol_directions() {
             dirs[static_cast<size_t>(d) * kSobolBits + (k - 1)] = m[k] << (kSobolBits - k);
         }
     }
+    // Y table of the warp decomposition (qmc.cu, SobolLane): for lane l the
+    // low index part is (l + 1) mod 32; Y[d][l] = the coordinate bits of its
+    // Gray code in dimension d.
+    dirs.resize(static_cast<size_t>(kSobolDims) * kSobolBits * 2);
+    uint32_t* y = dirs.data() + static_cast<size_t>(kSobolDims) * kSobolBits;
+    for (int d = 0; d < kSobolDims; ++d)
+        for (uint32_t l = 0; l < 32; ++l) {
+            const uint32_t low = (l + 1) & 31u, g = low ^ (low >> 1);
+            uint32_t x = 0;
+            for (int b = 0; b < 5; ++b)
+                if ((g >> b) & 1u) x ^= dirs[static_cast<size_t>(d) * kSobolBits + b];
+            y[static_cast<size_t>(d) * 32 + l] = x;
+        }
     return dirs;
 }
 
