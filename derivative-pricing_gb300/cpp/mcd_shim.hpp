@@ -138,7 +138,23 @@ double heston_semi_analytic(const models::HestonParams& params, double strike, O
 
 // include/mcd/pricers/analytic.hpp, binomial.hpp: closed forms and trees
 // (host code, no GPU)
+double black_scholes_merton(double spot, double strike, double rate, double carry_yield, double vol, double time,
+                            OptionType type);
+double black76(double forward, double strike, double rate, double vol, double time, OptionType type);
+double kemna_vorst(double spot, double strike, double rate, double carry_yield, double vol, double time,
+                   OptionType type);
+double reiner_rubinstein(double spot, double strike, double barrier, double rate, double carry_yield, double vol,
+                         double time, OptionType type, BarrierDirection direction, BarrierKnock knock,
+                         double rebate = 0.0);
+double lookback_fixed_strike(double spot, double strike, double rate, double carry_yield, double vol, double time,
+                             OptionType type);
+double lookback_floating_strike(double spot, double rate, double carry_yield, double vol, double time,
+                                OptionType type);
+double digital(double spot, double strike, double rate, double carry_yield, double vol, double time,
+               OptionType type, DigitalStyle style, double cash_amount = 1.0);
 double forward_price(double spot, double rate, double carry_yield, double time);
+double forward_value(double forward_now, double forward_at_inception, double rate, double time_to_expiry);
+double futures_mark_to_market(double futures_price_new, double futures_price_old);
 struct BinomialResult {
     double price;
     double risk_neutral_probability;

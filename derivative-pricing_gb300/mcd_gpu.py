@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import time as _time
 from dataclasses import dataclass
 
 import numpy as np
@@ -212,6 +213,18 @@ def lib():
     sig("mcd_draws", vp, u64, u64, u64, u32, u32, i32, i32, P(dbl))
     sig("mcd_kernel_timing", vp, i32, P(dbl), P(u64))
     sig("mcd_crr_binomial_american", *D6, i32, i32, res=dbl)
+    sig("mcd_crr_binomial", *D6, i32, i32, P(dbl))
+    sig("mcd_black_scholes_merton", *D6, i32, res=dbl)
+    sig("mcd_black76", *([dbl] * 5), i32, res=dbl)
+    sig("mcd_kemna_vorst", *D6, i32, res=dbl)
+    sig("mcd_reiner_rubinstein", *([dbl] * 7), i32, i32, i32, dbl, res=dbl)
+    sig("mcd_lookback_fixed_strike", *D6, i32, res=dbl)
+    sig("mcd_lookback_floating_strike", *([dbl] * 5), i32, res=dbl)
+    sig("mcd_digital_analytic", *D6, i32, i32, dbl, res=dbl)
+    sig("mcd_forward_price", *([dbl] * 4), res=dbl)
+    sig("mcd_forward_value", *([dbl] * 4), res=dbl)
+    sig("mcd_futures_mark_to_market", dbl, dbl, res=dbl)
+    sig("mcd_heston_semi_analytic", P(HestonParams), dbl, i32, res=dbl)
     _lib = L
     return L
 
@@ -262,6 +275,23 @@ class Engine:
                                                  time, type, path_count, seed, C.byref(o),
                                                  _prec(precision), C.byref(out)))
         return out
+
+    def benchmark_european(self, spot, strike, rate, carry_yield, vol, time, type, path_count, seed,
+                           options=None, antithetic=False, precision="fp64") -> dict:
+        """The reference's benchmark harness (bindings/python/src/module.cpp:29-60): one
+        European pricing call timed on the host clock around the whole call, as a dict.
+        ``simd_enabled`` reports the reference's NEON fast path, which this engine does
+        not have (the paths run on the GPU)."""
+        if options is not None:
+            antithetic = bool(options.antithetic)
+        t0 = _time.perf_counter()
+        r = self.monte_carlo_european(spot, strike, rate, carry_yield, vol, time, type, path_count,
+                                      seed, antithetic=antithetic, precision=precision)
+        elapsed = _time.perf_counter() - t0
+        return {"price": r.price, "standard_error": r.standard_error, "path_count": r.path_count,
+                "elapsed_seconds": elapsed,
+                "paths_per_second": r.path_count / elapsed if elapsed > 0.0 else 0.0,
+                "simd_enabled": False}
 
     def monte_carlo_digital(self, spot, strike, rate, carry_yield, vol, time, type, style,
                             cash_amount, path_count, seed, antithetic=False,
@@ -584,9 +614,74 @@ class Engine:
         return out
 
 
+# -- closed forms and lattices (host FP64 in libmcd_gpu.so; module.cpp:179-198, 284) -----
+@dataclass
+class BinomialResult:
+    """mcd::pricers::BinomialResult (include/mcd/pricers/binomial.hpp)."""
+    price: float
+    risk_neutral_probability: float
+    up_factor: float
+    down_factor: float
+
+
+def black_scholes_merton(spot, strike, rate, carry_yield, vol, time, type) -> float:
+    return lib().mcd_black_scholes_merton(spot, strike, rate, carry_yield, vol, time, int(type))
+
+
+def black76(forward, strike, rate, vol, time, type) -> float:
+    return lib().mcd_black76(forward, strike, rate, vol, time, int(type))
+
+
+def kemna_vorst(spot, strike, rate, carry_yield, vol, time, type) -> float:
+    return lib().mcd_kemna_vorst(spot, strike, rate, carry_yield, vol, time, int(type))
+
+
+def reiner_rubinstein(spot, strike, barrier, rate, carry_yield, vol, time, type, direction, knock,
+                      rebate=0.0) -> float:
+    return lib().mcd_reiner_rubinstein(spot, strike, barrier, rate, carry_yield, vol, time, int(type),
+                                       int(direction), int(knock), rebate)
+
+
+def lookback_fixed_strike(spot, strike, rate, carry_yield, vol, time, type) -> float:
+    return lib().mcd_lookback_fixed_strike(spot, strike, rate, carry_yield, vol, time, int(type))
+
+
+def lookback_floating_strike(spot, rate, carry_yield, vol, time, type) -> float:
+    return lib().mcd_lookback_floating_strike(spot, rate, carry_yield, vol, time, int(type))
+
+
+def digital(spot, strike, rate, carry_yield, vol, time, type, style, cash_amount=1.0) -> float:
+    return lib().mcd_digital_analytic(spot, strike, rate, carry_yield, vol, time, int(type), int(style),
+                                      cash_amount)
+
+
+def forward_price(spot, rate, carry_yield, time) -> float:
+    return lib().mcd_forward_price(spot, rate, carry_yield, time)
+
+
+def forward_value(forward_now, forward_at_inception, rate, time_to_expiry) -> float:
+    return lib().mcd_forward_value(forward_now, forward_at_inception, rate, time_to_expiry)
+
+
+def futures_mark_to_market(futures_price_new, futures_price_old) -> float:
+    return lib().mcd_futures_mark_to_market(futures_price_new, futures_price_old)
+
+
+def crr_binomial(spot, strike, rate, carry_yield, vol, time, steps, type) -> BinomialResult:
+    out = (dbl * 4)()
+    rc = lib().mcd_crr_binomial(spot, strike, rate, carry_yield, vol, time, steps, int(type), out)
+    if rc != 0:
+        raise McdError(rc, "crr_binomial: steps must be >= 1")
+    return BinomialResult(*out)
+
+
 def crr_binomial_american(spot, strike, rate, carry_yield, vol, time, steps, type) -> float:
-    """Cox-Ross-Rubinstein American price (host code in libmcd_gpu.so)."""
-    return lib().mcd_crr_binomial_american(spot, strike, rate, carry_yield, vol, time, steps, type)
+    """Cox-Ross-Rubinstein American price."""
+    return lib().mcd_crr_binomial_american(spot, strike, rate, carry_yield, vol, time, steps, int(type))
+
+
+def heston_semi_analytic(params: HestonParams, strike, type) -> float:
+    return lib().mcd_heston_semi_analytic(C.byref(params), strike, int(type))
 
 
 def contracts(n: int) -> np.ndarray:

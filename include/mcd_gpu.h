@@ -444,11 +444,47 @@ int mcd_philox(mcd_ctx* ctx, const uint32_t* counters, const uint32_t* keys, siz
 int mcd_draws(mcd_ctx* ctx, uint64_t seed, uint64_t path_begin, uint64_t n_paths,
               uint32_t draw_begin, uint32_t n_draws, int stream_id, int precision, double* out);
 
-/* ---- lattice reference price (host code) ---------------------------------- */
-/* replaces mcd::pricers::crr_binomial_american (src/pricers/binomial.cpp): the
- * Cox-Ross-Rubinstein American price, the yardstick for Longstaff-Schwartz. */
+/* ---- closed forms and lattices (host FP64, no GPU, no context) ------------ */
+/* The reference module exports these beside the Monte Carlo pricers
+ * (bindings/python/src/module.cpp); each keeps the reference's operation
+ * order.  type: mcd_option_type; direction/knock/style: the enums above. */
+/* replaces mcd::pricers::crr_binomial_american (src/pricers/binomial.cpp:39-72): the
+ * Cox-Ross-Rubinstein American price, the yardstick for Longstaff-Schwartz.
+ * NaN when steps < 1. */
 double mcd_crr_binomial_american(double spot, double strike, double rate, double carry_yield, double vol,
                                  double time, int steps, int type);
+/* replaces mcd::pricers::crr_binomial (src/pricers/binomial.cpp:9-37): European
+ * CRR tree; writes {price, risk-neutral probability, up factor, down factor}. */
+int mcd_crr_binomial(double spot, double strike, double rate, double carry_yield, double vol, double time,
+                     int steps, int type, double* price_p_u_d);
+/* replaces mcd::pricers::black_scholes_merton (src/pricers/analytic.cpp:30-38) */
+double mcd_black_scholes_merton(double spot, double strike, double rate, double carry_yield, double vol,
+                                double time, int type);
+/* replaces mcd::pricers::black76 (src/pricers/analytic.cpp:40-49) */
+double mcd_black76(double forward, double strike, double rate, double vol, double time, int type);
+/* replaces mcd::pricers::kemna_vorst (src/pricers/analytic.cpp:51-59) */
+double mcd_kemna_vorst(double spot, double strike, double rate, double carry_yield, double vol, double time,
+                       int type);
+/* replaces mcd::pricers::reiner_rubinstein (src/pricers/analytic.cpp:61-132) */
+double mcd_reiner_rubinstein(double spot, double strike, double barrier, double rate, double carry_yield,
+                             double vol, double time, int type, int direction, int knock, double rebate);
+/* replaces mcd::pricers::lookback_fixed_strike (src/pricers/analytic.cpp:184-195) */
+double mcd_lookback_fixed_strike(double spot, double strike, double rate, double carry_yield, double vol,
+                                 double time, int type);
+/* replaces mcd::pricers::lookback_floating_strike (src/pricers/analytic.cpp:197-212) */
+double mcd_lookback_floating_strike(double spot, double rate, double carry_yield, double vol, double time,
+                                    int type);
+/* replaces mcd::pricers::digital (src/pricers/analytic.cpp:214-222) */
+double mcd_digital_analytic(double spot, double strike, double rate, double carry_yield, double vol, double time,
+                            int type, int style, double cash_amount);
+/* replace mcd::pricers::forward_price, forward_value, futures_mark_to_market
+ * (src/pricers/analytic.cpp:224-235) */
+double mcd_forward_price(double spot, double rate, double carry_yield, double time);
+double mcd_forward_value(double forward_now, double forward_at_inception, double rate, double time_to_expiry);
+double mcd_futures_mark_to_market(double futures_price_new, double futures_price_old);
+/* replaces mcd::pricers::heston_semi_analytic (src/pricers/heston.cpp:48-82):
+ * P1/P2 by 128-point Gauss-Legendre over [0, 200]. NaN for a null params. */
+double mcd_heston_semi_analytic(const mcd_heston_params* params, double strike, int type);
 
 /* ---- timing helper for benchmarks ---------------------------------------- */
 /* Average device time (ms) of the persistent path kernel over the calls made

@@ -237,5 +237,19 @@ double ref_digital_analytic(double s, double k, double r, double q, double v, do
 double ref_crr_american(double s, double k, double r, double q, double v, double t, int steps, int type) {
     return pricers::crr_binomial_american(s, k, r, q, v, t, steps, ot(type));
 }
+void ref_crr_european(double s, double k, double r, double q, double v, double t, int steps, int type,
+                      double* out4) {
+    const auto b = pricers::crr_binomial(s, k, r, q, v, t, steps, ot(type));
+    out4[0] = b.price;
+    out4[1] = b.risk_neutral_probability;
+    out4[2] = b.up_factor;
+    out4[3] = b.down_factor;
+}
+double ref_black76(double f, double k, double r, double v, double t, int type) {
+    return pricers::black76(f, k, r, v, t, ot(type));
+}
+double ref_forward_price(double s, double r, double q, double t) { return pricers::forward_price(s, r, q, t); }
+double ref_forward_value(double fn, double f0, double r, double t) { return pricers::forward_value(fn, f0, r, t); }
+double ref_futures_mtm(double a, double b) { return pricers::futures_mark_to_market(a, b); }
 
 } // extern "C"

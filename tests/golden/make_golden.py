@@ -152,11 +152,49 @@ def main() -> None:
                                       "out": list(pw)}
     out["pathwise"] = pwd
 
+    D = C.c_double
+    for name, res_t, args in (("ref_black76", D, [D] * 5 + [C.c_int]),
+                              ("ref_forward_price", D, [D] * 4), ("ref_forward_value", D, [D] * 4),
+                              ("ref_futures_mtm", D, [D] * 2),
+                              ("ref_crr_european", None, [D] * 6 + [C.c_int, C.c_int, C.POINTER(D)])):
+        getattr(r, name).restype = res_t
+        getattr(r, name).argtypes = args
+    crr4 = (D * 4)()
+    crr_eu = []
+    for args in ((100, 100, .05, 0, .2, 1, 500, 0), (36, 40, .06, .01, .3, 2, 301, 1)):
+        r.ref_crr_european(*args, crr4)
+        crr_eu.append(list(args) + list(crr4))
+    rr = []
+    for ty in (0, 1):
+        for d in (0, 1):
+            for kn in (0, 1):
+                for k, h in ((100, 120), (100, 80), (110, 105), (90, 95)):
+                    if (d == 0 and h <= 100) or (d == 1 and h >= 100):
+                        continue
+                    args = [100, k, h, .05, .01, .25, 1, ty, d, kn, 1.5]
+                    rr.append(args + [r.ref_reiner_rubinstein(*args)])
+    p9 = (D * 9)(100, .03, 0, .04, 1.5, .05, .6, -.7, 1)
     out["analytic"] = {
-        "bsm": [[100, 100, .05, 0, .2, 1, 0, r.ref_bsm(100, 100, .05, 0, .2, 1, 0)]],
-        "kemna_vorst": [[100, 95, .05, .01, .2, 1, 1, r.ref_kemna_vorst(100, 95, .05, .01, .2, 1, 1)]],
+        "bsm": [[100, 100, .05, 0, .2, 1, 0, r.ref_bsm(100, 100, .05, 0, .2, 1, 0)],
+                [90, 100, .03, .02, .35, 2, 1, r.ref_bsm(90, 100, .03, .02, .35, 2, 1)]],
+        "kemna_vorst": [[100, 95, .05, .01, .2, 1, 1, r.ref_kemna_vorst(100, 95, .05, .01, .2, 1, 1)],
+                        [100, 105, .05, .0, .3, 1.5, 0, r.ref_kemna_vorst(100, 105, .05, 0, .3, 1.5, 0)]],
         "crr_american": [[36, 40, .06, 0, .2, 1, 500, 1,
                           r.ref_crr_american(36, 40, .06, 0, .2, 1, 500, 1)]],
+        "crr_european": crr_eu,
+        "black76": [[105, 100, .04, .25, 1.5, ty, r.ref_black76(105, 100, .04, .25, 1.5, ty)] for ty in (0, 1)],
+        "reiner_rubinstein": rr,
+        "lookback_fixed": [[100, k, .05, .01, .3, 1, ty, r.ref_lookback_fixed(100, k, .05, .01, .3, 1, ty)]
+                           for k in (90, 100, 110) for ty in (0, 1)],
+        "lookback_floating": [[100, .05, .01, .3, 1, ty, r.ref_lookback_floating(100, .05, .01, .3, 1, ty)]
+                              for ty in (0, 1)],
+        "digital": [[100, 95, .05, .01, .2, 1, ty, st, 2.0, r.ref_digital_analytic(100, 95, .05, .01, .2, 1, ty, st, 2.0)]
+                    for ty in (0, 1) for st in (0, 1)],
+        "forward_price": [[100, .05, .01, 2, r.ref_forward_price(100, .05, .01, 2)]],
+        "forward_value": [[110, 104, .05, .5, r.ref_forward_value(110, 104, .05, .5)]],
+        "futures_mtm": [[101.5, 100.25, r.ref_futures_mtm(101.5, 100.25)]],
+        "heston_semi_analytic": [[list(p9), k, ty, r.ref_heston_semi_analytic(p9, k, ty)]
+                                 for k in (90, 105) for ty in (0, 1)],
     }
     path = os.path.join(HERE, "reference_vectors.json")
     with open(path, "w") as f:
