@@ -228,7 +228,8 @@ def bench_risk(eng):
     """Batched risk: price, CRN finite-difference delta/gamma/vega (bump 1e-4
     relative), pathwise and likelihood-ratio Greeks of 1024 Asian/barrier
     contracts in one graph launch; learned LSM on 512 American puts with
-    uneven date counts U{10..100}, 2^18 paths."""
+    uneven date counts U{10..100}, 2^18 paths, and their frozen-boundary
+    delta/gamma/vega."""
     import mcd_gpu as M
     c = risk_batch()
     v, ctas, _ = eng.greeks_autotune(c[::8], 1e-4, 1e-4, "fp32")
@@ -248,13 +249,18 @@ def bench_risk(eng):
     puts["seed"] = 1000 + np.arange(n)
     ml, tl = _timed(lambda: eng.lsm_batch(puts, "fp32", "mlp"), reps=1)
     qr, tq = _timed(lambda: eng.lsm_batch(puts, "fp32", "qr"), reps=1)
+    ag, ta = _timed(lambda: eng.lsm_greeks_batch(puts, 0.01, 0.01, "fp32"), reps=1)
     return {"greeks": {"contracts": len(c), "s": tg, "contracts_per_second": len(c) / tg,
                        "path_steps_per_second": steps / tg, "launch_shape": {"variant": v, "ctas_per_sm": ctas},
                        "outputs": "price, FD delta/gamma/vega, pathwise delta/vega/rho, LR delta/gamma/vega/rho"},
             "learned_lsm_512": {"s": tl, "contracts_per_second": n / tl, "qr_s": tq,
                                 "max_abs_diff_vs_qr_in_se": float(np.max(np.abs(ml["price"] - qr["price"]) /
                                                                          qr["standard_error"])),
-                                "fallbacks": int((ml["reserved"] != 0).sum())}}
+                                "fallbacks": int((ml["reserved"] != 0).sum())},
+            "american_greeks_512": {"s": ta, "contracts_per_second": n / ta,
+                                    "outputs": "QR fit, then price/delta/gamma/vega against the frozen policy "
+                                               "(bumps 1% of spot and vol), all scenarios in one streaming pass",
+                                    "mean_delta_se": float(np.mean(ag["delta"][:, 1]))}}
 
 
 def bench_heston(eng, n_sets=256):
@@ -290,7 +296,7 @@ def bench_qmc(eng, c):
             "timing": "wall clock of one mcd_qmc_batch call (host arrays), best of 2 after a warm-up"}
 
 
-PROFILE_CASES = ("path", "greeks", "qmc", "heston", "lsm", "lsm_grid", "mlp", "mlp_grid")
+PROFILE_CASES = ("path", "greeks", "qmc", "heston", "lsm", "lsm_grid", "mlp", "mlp_grid", "american_greeks")
 
 
 def run_case(case):
@@ -303,7 +309,8 @@ def run_case(case):
       lsm       4 puts of the American grid (2^20 paths, 50 dates), FP32 QR
       lsm_grid  the 20-put grid, FP32 QR
       mlp       4 puts of the grid, learned regression
-      mlp_grid  the 20-put grid, learned regression"""
+      mlp_grid  the 20-put grid, learned regression
+      american_greeks  the 20-put grid: QR fit, then frozen-boundary Greeks (FP32)"""
     import mcd_gpu as M
     eng = M.Engine(0)
     for _ in range(2):
@@ -331,6 +338,8 @@ def run_case(case):
             if case in ("lsm", "mlp"):
                 g = g[:4]
             r = eng.lsm_batch(g, "fp32", "mlp" if case.startswith("mlp") else "qr")["price"]
+        elif case == "american_greeks":
+            r = eng.lsm_greeks_batch(lsm_grid(), 0.01, 0.01, "fp32")["delta"][:, 0]
         else:
             raise SystemExit(f"unknown case {case!r}; one of {PROFILE_CASES}")
     print(case, np.asarray(r)[:4])

@@ -52,6 +52,22 @@ struct LsmPartial {
     double v[16];
 };
 
+// Frozen-policy replay (lsm_frozen.cu).  One scenario = the inputs of one
+// reprice_against_frozen_policy call (src/pricers/lsm.cpp:151-213) on the
+// contract's paths (same seed): spot and the per-step GBM constants of its
+// volatility, in FP64 and as the FP32 kernel's copies.
+struct FrozenScenario {
+    double spot, drift, vs;
+    float spot_f, mu_f, sg_f, pad;
+};
+constexpr int kFrozenScenarios = 5;  // base, spot+h, spot-h, vol+h, vol-h
+constexpr int kFrozenOutputs = 8;    // five scenario averages, then the CRN delta, gamma, vega
+struct FrozenDev {
+    FrozenScenario sc[kFrozenScenarios];
+    double inv_2hs, inv_hs2, inv_2hv;  // 1/(2h_S), 1/h_S^2, 1/(2h_vol)
+    float inv_2hs_f, inv_hs2_f, inv_2hv_f, pad;
+};
+
 cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
                                const uint32_t* chunk_contract, uint32_t total_chunks, void* s_store,
                                cudaStream_t stream);
@@ -63,5 +79,13 @@ cudaError_t launch_lsm_iteration(int precision, int k, bool frozen, const LsmDev
 cudaError_t launch_lsm_finish(const LsmDev* c, int n_contracts, const Welford* final_part,
                               double* out /* n x 6: price, se, count, inception, mean, se */,
                               cudaStream_t stream);
+// Streams every chunk's paths forward once against the regression table
+// `reg` (rows per contract at LsmDev::reg_offset), in n_scenarios (1 or
+// kFrozenScenarios) scenarios, and writes per contract and output the path
+// average, its standard error and the path count (out: n x outputs x 3;
+// outputs = 1 for one scenario, kFrozenOutputs for five).
+cudaError_t launch_lsm_frozen(int precision, int n_scenarios, const LsmDev* c, const FrozenDev* f,
+                              int n_contracts, const uint32_t* chunk_contract, uint32_t total_chunks,
+                              const LsmReg* reg, Welford* partials, double* out, cudaStream_t stream);
 
 }  // namespace mcdg

@@ -20,7 +20,8 @@ namespace {
 // Extension slots of Ctx::ext used by this module (Heston uses 0..3).
 enum { kDev = 4, kChunkMap = 5, kStore = 6, kCf = 7, kReg = 8, kPartA = 9, kPartB = 10,
        kFinal = 11, kOut = 12, kNets = 13, kSnaps = 14, kSnapOk = 15, kAdamT = 16, kErr = 17,
-       kGroupMap = 18, kGramPart = 19, kGramSum = 20, kFeatCache = 35 };
+       kGroupMap = 18, kGramPart = 19, kGramSum = 20, kFeatCache = 35, kFzDev = 36, kFzPart = 37,
+       kFzOut = 38 };
 
 struct LsmPlan {
     std::vector<LsmDev> dev;
@@ -91,12 +92,14 @@ int plan_lsm(Ctx& ctx, const mcd_lsm_contract* cs, size_t n, LsmPlan& p) {
     return MCD_OK;
 }
 
-// Runs a planned batch.  mlp = false: Laguerre QR regression (frozen: replay
-// frozen_reg).  mlp = true: learned regression (frozen: replay the networks in
-// frozen_nets, one kParamStride block per (contract, date) row).
-int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
-                   const std::vector<LsmReg>* frozen_reg, std::vector<double>& out, bool mlp = false,
-                   const std::vector<float>* frozen_nets = nullptr, const std::vector<int>* frozen_ok = nullptr) {
+// Runs a planned batch with stored paths.  mlp = false: Laguerre QR
+// regression, fitted (the table stays in kReg).  mlp = true: learned
+// regression, fitted, or (frozen) replaying the networks in frozen_nets, one
+// kParamStride block per (contract, date) row.  Frozen QR policies are
+// replayed by the streaming kernel instead (frozen_run).
+int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::vector<double>& out,
+                   bool mlp = false, const std::vector<float>* frozen_nets = nullptr,
+                   const std::vector<int>* frozen_ok = nullptr) {
     const size_t n = p.dev.size();
     const size_t elem = precision == 0 ? sizeof(double) : sizeof(float);
     int rc = ctx.reserve(ctx.ext[kDev], sizeof(LsmDev) * n, "lsm contracts");
@@ -129,13 +132,7 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen,
     if (e == cudaSuccess && p.total_chunks)
         e = cudaMemcpyAsync(ctx.ext[kChunkMap].ptr, p.chunk_contract.data(), sizeof(uint32_t) * p.total_chunks,
                             cudaMemcpyHostToDevice, ctx.stream);
-    if (e == cudaSuccess) {
-        if (frozen_reg)
-            e = cudaMemcpyAsync(ctx.ext[kReg].ptr, frozen_reg->data(), sizeof(LsmReg) * p.reg_rows,
-                                cudaMemcpyHostToDevice, ctx.stream);
-        else
-            e = cudaMemsetAsync(ctx.ext[kReg].ptr, 0, sizeof(LsmReg) * p.reg_rows, ctx.stream);
-    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx.ext[kReg].ptr, 0, sizeof(LsmReg) * p.reg_rows, ctx.stream);
     if (e == cudaSuccess && mlp) {
         e = cudaMemsetAsync(ctx.ext[kErr].ptr, 0, 256, ctx.stream);
         if (e == cudaSuccess && p.total_groups)
@@ -238,7 +235,7 @@ int lsm_batch(Ctx& ctx, const mcd_lsm_contract* cs, size_t n, int precision, int
     if (rc) return rc;
     std::vector<double> out;
     const bool mlp = regression == MCD_LSM_MLP;
-    rc = upload_and_run(ctx, p, precision, false, nullptr, out, mlp);
+    rc = upload_and_run(ctx, p, precision, false, out, mlp);
     if (rc) return rc;
     std::vector<int> ok;
     if (mlp) {
@@ -286,6 +283,121 @@ int lsm_batch(Ctx& ctx, const mcd_lsm_contract* cs, size_t n, int precision, int
     return MCD_OK;
 }
 
+// One scenario's inputs: the GBM step constants of `vol` in the order of
+// plan_lsm (src/models/gbm.cpp:8-10), plus the FP32 kernel's copies.
+FrozenScenario scenario(double spot, const mcd_lsm_contract& c, double vol) {
+    const double dt = c.time / static_cast<double>(c.monitoring_points);
+    FrozenScenario s{};
+    s.spot = spot;
+    s.drift = (c.rate - c.carry_yield - 0.5 * vol * vol) * dt;
+    s.vs = vol * std::sqrt(dt);
+    s.spot_f = static_cast<float>(spot);
+    s.mu_f = static_cast<float>(s.drift);
+    s.sg_f = static_cast<float>(s.vs);
+    return s;
+}
+
+// Scenarios base, spot +/- hs, vol +/- hv (hs = hv = 0: the base alone).
+FrozenDev frozen_dev(const mcd_lsm_contract& c, double hs, double hv) {
+    FrozenDev f{};
+    f.sc[0] = scenario(c.spot, c, c.vol);
+    f.sc[1] = scenario(c.spot + hs, c, c.vol);
+    f.sc[2] = scenario(c.spot - hs, c, c.vol);
+    f.sc[3] = scenario(c.spot, c, c.vol + hv);
+    f.sc[4] = scenario(c.spot, c, c.vol - hv);
+    f.inv_2hs = hs > 0.0 ? 0.5 / hs : 0.0;
+    f.inv_hs2 = hs > 0.0 ? 1.0 / (hs * hs) : 0.0;
+    f.inv_2hv = hv > 0.0 ? 0.5 / hv : 0.0;
+    f.inv_2hs_f = static_cast<float>(f.inv_2hs);
+    f.inv_hs2_f = static_cast<float>(f.inv_hs2);
+    f.inv_2hv_f = static_cast<float>(f.inv_2hv);
+    return f;
+}
+
+// Streams the planned contracts against the regression table in kReg
+// (uploaded from `reg` when given, else left there by a fit on this
+// context).  out: n x outputs x {mean, se, count}.
+int frozen_run(Ctx& ctx, const LsmPlan& p, const std::vector<FrozenDev>& fz, int precision, int n_scenarios,
+               const std::vector<LsmReg>* reg, std::vector<double>& out) {
+    const size_t n = p.dev.size();
+    const int nw = n_scenarios == 1 ? 1 : kFrozenOutputs;
+    int rc = ctx.reserve(ctx.ext[kDev], sizeof(LsmDev) * n, "lsm contracts");
+    if (!rc) rc = ctx.reserve(ctx.ext[kChunkMap], sizeof(uint32_t) * std::max<size_t>(p.total_chunks, 1), "lsm chunk map");
+    if (!rc) rc = ctx.reserve(ctx.ext[kReg], sizeof(LsmReg) * p.reg_rows, "lsm regression table");
+    if (!rc) rc = ctx.reserve(ctx.ext[kFzDev], sizeof(FrozenDev) * n, "frozen scenarios");
+    if (!rc) rc = ctx.reserve(ctx.ext[kFzPart], sizeof(Welford) * nw * std::max<size_t>(p.total_chunks, 1), "frozen partials");
+    if (!rc) rc = ctx.reserve(ctx.ext[kFzOut], sizeof(double) * 3 * nw * n, "frozen results");
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpyAsync(ctx.ext[kDev].ptr, p.dev.data(), sizeof(LsmDev) * n, cudaMemcpyHostToDevice, ctx.stream);
+    if (e == cudaSuccess && p.total_chunks)
+        e = cudaMemcpyAsync(ctx.ext[kChunkMap].ptr, p.chunk_contract.data(), sizeof(uint32_t) * p.total_chunks,
+                            cudaMemcpyHostToDevice, ctx.stream);
+    if (e == cudaSuccess && reg)
+        e = cudaMemcpyAsync(ctx.ext[kReg].ptr, reg->data(), sizeof(LsmReg) * p.reg_rows, cudaMemcpyHostToDevice,
+                            ctx.stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx.ext[kFzDev].ptr, fz.data(), sizeof(FrozenDev) * n, cudaMemcpyHostToDevice, ctx.stream);
+    if (e != cudaSuccess) return ctx.cuda_fail(e, "frozen upload");
+    int pair = -1;
+    rc = ctx.record_start(ctx.stream, &pair);
+    if (rc) return rc;
+    e = launch_lsm_frozen(precision, n_scenarios, static_cast<const LsmDev*>(ctx.ext[kDev].ptr),
+                          static_cast<const FrozenDev*>(ctx.ext[kFzDev].ptr), static_cast<int>(n),
+                          static_cast<const uint32_t*>(ctx.ext[kChunkMap].ptr), p.total_chunks,
+                          static_cast<const LsmReg*>(ctx.ext[kReg].ptr), static_cast<Welford*>(ctx.ext[kFzPart].ptr),
+                          static_cast<double*>(ctx.ext[kFzOut].ptr), ctx.stream);
+    if (e != cudaSuccess) return ctx.cuda_fail(e, "frozen launch");
+    rc = ctx.record_stop(ctx.stream, pair);
+    if (rc) return rc;
+    out.assign(static_cast<size_t>(3) * nw * n, 0.0);
+    e = cudaMemcpyAsync(out.data(), ctx.ext[kFzOut].ptr, sizeof(double) * out.size(), cudaMemcpyDeviceToHost, ctx.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx.stream);
+    if (e != cudaSuccess) return ctx.cuda_fail(e, "frozen execution");
+    ctx.collect_timing(false);
+    return MCD_OK;
+}
+
+// The policy table of one contract from the ABI's coefficient layout.
+std::vector<LsmReg> policy_table(const LsmPlan& p, int monitoring_points, const double* coefficients,
+                                 const uint8_t* has) {
+    std::vector<LsmReg> reg(p.reg_rows);
+    std::memset(reg.data(), 0, sizeof(LsmReg) * reg.size());
+    for (int d = 1; d < monitoring_points; ++d) {
+        if (!has[d]) continue;
+        reg[d].has = 1;
+        for (int b = 0; b < 4; ++b) {
+            reg[d].gamma[b] = coefficients[4 * d + b];
+            reg[d].gamma_f[b] = static_cast<float>(coefficients[4 * d + b]);
+        }
+    }
+    return reg;
+}
+
+double intrinsic_host(double s, double k, int type) {
+    const double x = (type == 0 ? 1.0 : -1.0) * (s - k);
+    return x > 0.0 ? x : 0.0;
+}
+
+// Greeks of contract i from the five-scenario results (frozen inception
+// decision applied as src/pricers/lsm.cpp:206-212 does per replay).
+void assemble_greeks(const mcd_lsm_contract& c, double hs, double hv, bool inception, const double* r,
+                     mcd_american_greeks& g) {
+    double price[kFrozenScenarios];
+    const double spots[kFrozenScenarios] = {c.spot, c.spot + hs, c.spot - hs, c.spot, c.spot};
+    for (int q = 0; q < kFrozenScenarios; ++q)
+        price[q] = inception ? intrinsic_host(spots[q], c.strike, c.type) : r[3 * q];
+    std::memset(&g, 0, sizeof g);
+    g.price = {price[0], inception ? 0.0 : r[1]};
+    g.delta = {(price[1] - price[2]) / (2.0 * hs), inception ? 0.0 : r[3 * 5 + 1]};
+    g.gamma = {(price[1] - 2.0 * price[0] + price[2]) / (hs * hs), inception ? 0.0 : r[3 * 6 + 1]};
+    g.vega = {(price[3] - price[4]) / (2.0 * hv), inception ? 0.0 : r[3 * 7 + 1]};
+    for (int q = 0; q < 4; ++q) g.scenario[q] = price[q + 1];
+    g.spot_bump = hs;
+    g.vol_bump = hv;
+    g.path_count = static_cast<uint64_t>(r[2]);
+    g.exercise_at_inception = inception ? 1 : 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -327,28 +439,65 @@ int mcd_lsm_reprice_frozen(mcd_ctx* handle, double spot, double strike, double r
     LsmPlan p;
     int rc = plan_lsm(*ctx, &c, 1, p);
     if (rc) return rc;
-    std::vector<LsmReg> reg(p.reg_rows);
-    std::memset(reg.data(), 0, sizeof(LsmReg) * reg.size());
-    for (int d = 1; d < monitoring_points; ++d) {
-        if (!has_coefficients[d]) continue;
-        reg[d].has = 1;
-        for (int b = 0; b < 4; ++b) {
-            reg[d].gamma[b] = coefficients[4 * d + b];
-            reg[d].gamma_f[b] = static_cast<float>(coefficients[4 * d + b]);
-        }
-    }
+    const std::vector<LsmReg> reg = policy_table(p, monitoring_points, coefficients, has_coefficients);
+    const std::vector<FrozenDev> fz{frozen_dev(c, 0.0, 0.0)};
     std::vector<double> out;
-    rc = upload_and_run(*ctx, p, precision, true, &reg, out);
+    rc = frozen_run(*ctx, p, fz, precision, 1, &reg, out);
     if (rc) return rc;
     // Frozen inception decision (src/pricers/lsm.cpp:206-212): the base run's
     // choice is replayed; otherwise the price is the path average itself.
-    if (exercise_at_inception) {
-        const double phi = type == 0 ? 1.0 : -1.0;
-        const double x = phi * (spot - strike);
-        *price = x > 0.0 ? x : 0.0;
-    } else {
-        *price = out[4];
-    }
+    *price = exercise_at_inception ? intrinsic_host(spot, strike, type) : out[0];
+    return MCD_OK;
+}
+
+int mcd_lsm_frozen_greeks(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield,
+                          double vol, double time, int type, int monitoring_points, uint64_t path_count,
+                          uint64_t seed, const double* coefficients, const uint8_t* has_coefficients,
+                          int exercise_at_inception, double spot_bump, double vol_bump, int precision,
+                          mcd_american_greeks* out) {
+    MCD_CTX_OR_FAIL(handle, ctx);
+    if (!coefficients || !has_coefficients || !out) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
+    if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
+    if (!(spot_bump > 0.0 && spot_bump < spot) || !(vol_bump > 0.0 && vol_bump < vol))
+        return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "bumps must satisfy 0 < spot_bump < spot and 0 < vol_bump < vol");
+    const mcd_lsm_contract c{spot, strike, rate, carry_yield, vol, time, type, monitoring_points,
+                             path_count, seed};
+    LsmPlan p;
+    int rc = plan_lsm(*ctx, &c, 1, p);
+    if (rc) return rc;
+    const std::vector<LsmReg> reg = policy_table(p, monitoring_points, coefficients, has_coefficients);
+    const std::vector<FrozenDev> fz{frozen_dev(c, spot_bump, vol_bump)};
+    std::vector<double> res;
+    rc = frozen_run(*ctx, p, fz, precision, kFrozenScenarios, &reg, res);
+    if (rc) return rc;
+    assemble_greeks(c, spot_bump, vol_bump, exercise_at_inception != 0, res.data(), *out);
+    return MCD_OK;
+}
+
+int mcd_lsm_greeks_batch(mcd_ctx* handle, const mcd_lsm_contract* contracts, size_t n, double spot_bump_rel,
+                         double vol_bump_rel, int precision, mcd_american_greeks* results) {
+    MCD_CTX_OR_FAIL(handle, ctx);
+    if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
+    if (!(spot_bump_rel > 0.0 && spot_bump_rel < 1.0) || !(vol_bump_rel > 0.0 && vol_bump_rel < 1.0))
+        return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "relative bumps must lie in (0, 1)");
+    if (n == 0) return MCD_OK;
+    if (!contracts || !results) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null array");
+    LsmPlan p;
+    int rc = plan_lsm(*ctx, contracts, n, p);
+    if (rc) return rc;
+    // fit every policy (stored paths, QR); the table stays on the device
+    std::vector<double> fit;
+    rc = upload_and_run(*ctx, p, precision, false, fit);
+    if (rc) return rc;
+    std::vector<FrozenDev> fz(n);
+    for (size_t i = 0; i < n; ++i)
+        fz[i] = frozen_dev(contracts[i], spot_bump_rel * contracts[i].spot, vol_bump_rel * contracts[i].vol);
+    std::vector<double> res;
+    rc = frozen_run(*ctx, p, fz, precision, kFrozenScenarios, nullptr, res);
+    if (rc) return rc;
+    for (size_t i = 0; i < n; ++i)
+        assemble_greeks(contracts[i], spot_bump_rel * contracts[i].spot, vol_bump_rel * contracts[i].vol,
+                        fit[6 * i + 3] != 0.0, res.data() + 3 * kFrozenOutputs * i, results[i]);
     return MCD_OK;
 }
 
@@ -410,7 +559,7 @@ int mcd_lsm_reprice_mlp(mcd_ctx* handle, double spot, double strike, double rate
             nets[static_cast<size_t>(d) * mlp::kParamStride + q] = weights[static_cast<size_t>(d) * mlp::kParams + q];
     }
     std::vector<double> res;
-    rc = upload_and_run(*ctx, p, precision, true, nullptr, res, true, &nets, &ok);
+    rc = upload_and_run(*ctx, p, precision, true, res, true, &nets, &ok);
     if (rc) return rc;
     out->price = res[0];
     out->standard_error = res[1];

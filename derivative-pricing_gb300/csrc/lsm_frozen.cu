@@ -1,0 +1,296 @@
+// lsm_frozen.cu -- replay of a frozen Longstaff-Schwartz exercise policy,
+// streamed: no path storage, one pass, several scenarios per path.
+//
+// Reference: reprice_against_frozen_policy (src/pricers/lsm.cpp:151-213)
+// simulates the paths, seeds the cash flows with the terminal intrinsic and
+// walks dates n-1..1 backwards: discount, then exercise where the frozen
+// coefficients say so.  With the coefficients fixed, the cash flow a path ends
+// with is the exercise value at the EARLIEST date whose test passes (later
+// overwrites are earlier dates), or the terminal intrinsic, multiplied by the
+// one-date discount once per date before it.  So a path can be priced
+// forwards, stopping at its first exercise: the same multiplications in the
+// same order give the same bits, and nothing is stored.  Frozen-boundary
+// Greeks need the same replay at bumped inputs on the same draws (the
+// reference's tests/lsm_test.cpp:138-185 calls the replay at S +/- h): each
+// thread carries every scenario's state along one path, sharing the draws.
+//
+// Work layout, reductions and per-chunk partials are those of the backward
+// pass (lsm.cu): chunks of 1024 paths, 256 threads, a fixed Welford tree per
+// chunk, chunks merged in order per contract -- the base scenario reproduces
+// the stored-path replay's price bit for bit.
+//
+// nvcc-flags: --fmad=false
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+#include "lsm.hpp"
+
+namespace mcdg {
+
+namespace {
+
+__device__ __forceinline__ double intrinsic(double s, double k, int type) {
+    const double x = (type == 0 ? 1.0 : -1.0) * (s - k);
+    return (x < 0.0) ? 0.0 : x;
+}
+
+// Weighted Laguerre basis (src/pricers/lsm.cpp:21-25), FP64, and the FP32
+// path's version; both as in the backward pass, so decisions agree with it.
+__device__ __forceinline__ double continuation64(double s, double strike, const double g[4]) {
+    const double x = s / strike;
+    const double e = exp(-x / 2.0);
+    double cont = 0.0;
+    cont += g[0] * e;
+    cont += g[1] * (e * (1.0 - x));
+    cont += g[2] * (e * (1.0 - 2.0 * x + 0.5 * x * x));
+    cont += g[3] * (e * (1.0 - 3.0 * x + 1.5 * x * x - x * x * x / 6.0));
+    return cont;
+}
+
+__device__ __forceinline__ float continuation32(float s, float inv_strike, const float g[4]) {
+    const float x = s * inv_strike;
+    const float e = __expf(-0.5f * x);
+    const float b0 = e;
+    const float b1 = e * (1.0f - x);
+    const float b2 = e * __fmaf_rn(0.5f * x, x, __fmaf_rn(-2.0f, x, 1.0f));
+    const float b3 = e * __fmaf_rn(__fmaf_rn(-x / 6.0f, x, 1.5f * x), x, __fmaf_rn(-3.0f, x, 1.0f));
+    return __fmaf_rn(g[3], b3, __fmaf_rn(g[2], b2, __fmaf_rn(g[1], b1, g[0] * b0)));
+}
+
+// One path, NS scenarios: cash flow of each scenario, discounted to t = 0.
+template <int NS>
+__device__ void replay64(const LsmDev& c, const FrozenDev& f, const LsmReg* __restrict__ rg, const PhiloxPath& pp,
+                         const PhiloxKeys& k, double (&v)[NS]) {
+    double s[NS];
+    int stop[NS];
+    bool live[NS];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+        s[q] = f.sc[q].spot;
+        stop[q] = c.n_steps;
+        live[q] = true;
+        v[q] = 0.0;
+    }
+    int n_live = NS;
+    for (int d = 0; d < c.n_steps && n_live > 0; ++d) {
+        const double z = normal_from_bits_f64(philox_word0(pp, static_cast<uint32_t>(d), k));
+        const int date = d + 1;
+        const bool test = date < c.n_steps && rg[date].has == 1;
+        double g[4] = {0.0, 0.0, 0.0, 0.0};
+        if (test) {
+            g[0] = rg[date].gamma[0];
+            g[1] = rg[date].gamma[1];
+            g[2] = rg[date].gamma[2];
+            g[3] = rg[date].gamma[3];
+        }
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            if (!live[q]) continue;
+            s[q] = s[q] * exp(f.sc[q].drift + f.sc[q].vs * z);  // src/models/gbm.cpp:7-12
+            if (test) {
+                const double ex = intrinsic(s[q], c.strike, c.type);
+                if (ex > 0.0 && ex > continuation64(s[q], c.strike, g)) {
+                    v[q] = ex;
+                    stop[q] = date;
+                    live[q] = false;
+                    --n_live;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+        if (live[q]) v[q] = intrinsic(s[q], c.strike, c.type);
+        for (int t = 0; t < stop[q]; ++t) v[q] *= c.disc;
+    }
+}
+
+template <int NS>
+__device__ void replay32(const LsmDev& c, const FrozenDev& f, const LsmReg* __restrict__ rg, const PhiloxPath& pp,
+                         const PhiloxKeys& k, float (&v)[NS]) {
+    float x[NS], s[NS];
+    int stop[NS];
+    bool live[NS];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+        x[q] = 0.0f;
+        s[q] = f.sc[q].spot_f;
+        stop[q] = c.n_steps;
+        live[q] = true;
+        v[q] = 0.0f;
+    }
+    const float phi = c.phi_f, strike = c.strike_f, inv_k = c.inv_strike_f;
+    int n_live = NS;
+    for (int d = 0; d < c.n_steps && n_live > 0; ++d) {
+        const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(d), k));
+        const int date = d + 1;
+        const bool test = date < c.n_steps && rg[date].has == 1;
+        float g[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (test) {
+            g[0] = rg[date].gamma_f[0];
+            g[1] = rg[date].gamma_f[1];
+            g[2] = rg[date].gamma_f[2];
+            g[3] = rg[date].gamma_f[3];
+        }
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            if (!live[q]) continue;
+            // the FP32 forward pass's log-space step (lsm.cu, lsm_forward)
+            x[q] = __fmaf_rn(f.sc[q].sg_f, z, x[q] + f.sc[q].mu_f);
+            s[q] = f.sc[q].spot_f * __expf(x[q]);
+            if (test) {
+                const float ex = phi * (s[q] - strike);
+                if (ex > 0.0f && ex > continuation32(s[q], inv_k, g)) {
+                    v[q] = ex;
+                    stop[q] = date;
+                    live[q] = false;
+                    --n_live;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+        if (live[q]) v[q] = fmaxf(phi * (s[q] - strike), 0.0f);
+        for (int t = 0; t < stop[q]; ++t) v[q] *= c.disc_f;
+    }
+}
+
+// Per chunk: NS scenario averages (and, for the five-scenario form, the
+// per-path central differences of delta, gamma and vega) as Welford partials.
+// The FP32 five-scenario form runs 3 CTAs per SM (80 registers; measured
+// 1.3x faster than 2 CTAs at 106 registers on the 20-put grid: paths that
+// exercise early leave the pass latency-bound).
+template <int PREC, int NS>
+__global__ void __launch_bounds__(kLsmThreads, (PREC == 1 && NS > 1) ? 3 : 2)
+    lsm_frozen_stream(const LsmDev* __restrict__ cs, const FrozenDev* __restrict__ fz,
+                      const uint32_t* __restrict__ chunk_contract, uint32_t total_chunks,
+                      const LsmReg* __restrict__ reg, Welford* __restrict__ part) {
+    constexpr int NW = NS == 1 ? 1 : kFrozenOutputs;
+    __shared__ Welford swf[kLsmThreads / 32][NW];
+    const uint32_t chunk = blockIdx.x;
+    if (chunk >= total_chunks) return;
+    const uint32_t ci = chunk_contract[chunk];
+    const LsmDev c = cs[ci];
+    const FrozenDev& f = fz[ci];
+    const LsmReg* rg = reg + c.reg_offset;
+    const PhiloxKeys k = philox_keys(c.seed);
+    const uint32_t local = chunk - c.chunk_begin;
+    Welford w[NW];
+    if constexpr (PREC == 0) {
+#pragma unroll
+        for (int q = 0; q < NW; ++q) w[q] = Welford{0ull, 0.0, 0.0};
+        for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+            const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
+            if (i >= c.path_count) break;
+            double v[NS];
+            replay64<NS>(c, f, rg, philox_path(i, 0u, k), k, v);
+#pragma unroll
+            for (int q = 0; q < NS; ++q) welford_add(w[q], v[q]);
+            if constexpr (NS == kFrozenScenarios) {
+                welford_add(w[5], (v[1] - v[2]) * f.inv_2hs);
+                welford_add(w[6], ((v[1] - v[0]) - (v[0] - v[2])) * f.inv_hs2);
+                welford_add(w[7], (v[3] - v[4]) * f.inv_2hv);
+            }
+        }
+    } else {
+        // FP32 cash flows; the scenario sums are FP64 per path (the backward
+        // pass's final form, so the base scenario keeps its bits).  The three
+        // differences only feed standard errors: FP32 over a thread's four
+        // paths, FP64 from there on (FP64 work is costly on this GPU).
+        unsigned count = 0;
+        double s1[NS], s2[NS];
+        float d1[3] = {0.0f, 0.0f, 0.0f}, d2[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int q = 0; q < NS; ++q) s1[q] = s2[q] = 0.0;
+        for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
+            const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
+            if (i >= c.path_count) break;
+            float v[NS];
+            replay32<NS>(c, f, rg, philox_path(i, 0u, k), k, v);
+            ++count;
+#pragma unroll
+            for (int q = 0; q < NS; ++q) {
+                const double vd = static_cast<double>(v[q]);
+                s1[q] += vd;
+                s2[q] = fma(vd, vd, s2[q]);
+            }
+            if constexpr (NS == kFrozenScenarios) {
+                const float dd[3] = {(v[1] - v[2]) * f.inv_2hs_f, ((v[1] - v[0]) - (v[0] - v[2])) * f.inv_hs2_f,
+                                     (v[3] - v[4]) * f.inv_2hv_f};
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    d1[q] += dd[q];
+                    d2[q] = __fmaf_rn(dd[q], dd[q], d2[q]);
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NS; ++q) w[q] = welford_from_sums(count, s1[q], s2[q]);
+        if constexpr (NS == kFrozenScenarios) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+                w[NS + q] = welford_from_sums(count, static_cast<double>(d1[q]), static_cast<double>(d2[q]));
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NW; ++q) {
+        const Welford r = welford_warp_reduce(w[q]);
+        if ((threadIdx.x & 31) == 0) swf[threadIdx.x >> 5][q] = r;
+    }
+    __syncthreads();
+    if (threadIdx.x < NW) {
+        const int q = threadIdx.x;
+        Welford m = swf[0][q];
+        for (int wi = 1; wi < kLsmThreads / 32; ++wi) m = welford_merge(m, swf[wi][q]);
+        part[static_cast<uint64_t>(chunk) * NW + q] = m;
+    }
+}
+
+// Per (contract, output): chunk partials merged in chunk order (lane-strided,
+// then the fixed warp tree, as lsm_finish), mean, standard error, count.
+__global__ void lsm_frozen_finish(const LsmDev* __restrict__ cs, int n_contracts, int nw,
+                                  const Welford* __restrict__ part, double* __restrict__ out) {
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (wid >= n_contracts * nw) return;
+    const int ci = wid / nw, q = wid % nw;
+    const LsmDev c = cs[ci];
+    Welford w{0ull, 0.0, 0.0};
+    for (uint32_t ch = lane; ch < c.n_chunks; ch += 32)
+        w = welford_merge(w, part[static_cast<uint64_t>(c.chunk_begin + ch) * nw + q]);
+    w = welford_warp_reduce(w);
+    if (lane != 0) return;
+    const double var = w.count < 2 ? 0.0 : w.m2 / static_cast<double>(w.count - 1);
+    double* o = out + (static_cast<size_t>(ci) * nw + q) * 3;
+    o[0] = w.mean;
+    o[1] = w.count == 0 ? 0.0 : sqrt(var / static_cast<double>(w.count));
+    o[2] = static_cast<double>(w.count);
+}
+
+}  // namespace
+
+cudaError_t launch_lsm_frozen(int precision, int n_scenarios, const LsmDev* c, const FrozenDev* f,
+                              int n_contracts, const uint32_t* chunk_contract, uint32_t total_chunks,
+                              const LsmReg* reg, Welford* partials, double* out, cudaStream_t stream) {
+    cudaGetLastError();
+    if (n_scenarios != 1 && n_scenarios != kFrozenScenarios) return cudaErrorInvalidValue;
+    if (total_chunks) {
+        const bool five = n_scenarios == kFrozenScenarios;
+        if (precision == 0) {
+            if (five) lsm_frozen_stream<0, kFrozenScenarios><<<total_chunks, kLsmThreads, 0, stream>>>(c, f, chunk_contract, total_chunks, reg, partials);
+            else lsm_frozen_stream<0, 1><<<total_chunks, kLsmThreads, 0, stream>>>(c, f, chunk_contract, total_chunks, reg, partials);
+        } else {
+            if (five) lsm_frozen_stream<1, kFrozenScenarios><<<total_chunks, kLsmThreads, 0, stream>>>(c, f, chunk_contract, total_chunks, reg, partials);
+            else lsm_frozen_stream<1, 1><<<total_chunks, kLsmThreads, 0, stream>>>(c, f, chunk_contract, total_chunks, reg, partials);
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    const int nw = n_scenarios == 1 ? 1 : kFrozenOutputs;
+    const int warps = n_contracts * nw;
+    lsm_frozen_finish<<<(warps * 32 + 127) / 128, 128, 0, stream>>>(c, n_contracts, nw, partials, out);
+    return cudaGetLastError();
+}
+
+}  // namespace mcdg

@@ -62,6 +62,13 @@ LSM_CONTRACT_DTYPE = np.dtype([(n, "<f8") for n in ("spot", "strike", "rate", "c
 LSM_RESULT_DTYPE = np.dtype([("price", "<f8"), ("standard_error", "<f8"), ("path_count", "<u8"),
                              ("exercise_at_inception", "<i4"), ("reserved", "<i4")])
 LSM_QR, LSM_MLP = 0, 1
+# mcd_american_greeks: price, delta, gamma, vega as (value, standard error), the
+# four bumped frozen prices, the bumps, the path count and the inception flag.
+AMERICAN_GREEKS_DTYPE = np.dtype([(n, "<f8", (2,)) for n in ("price", "delta", "gamma", "vega")] +
+                                 [("scenario", "<f8", (4,)), ("spot_bump", "<f8"), ("vol_bump", "<f8"),
+                                  ("path_count", "<u8"), ("exercise_at_inception", "<i4"),
+                                  ("reserved", "<i4")])
+assert AMERICAN_GREEKS_DTYPE.itemsize == 128
 MLP_PARAMS = 4417  # W1[64][2], b1[64], W2[64][64], b2[64], W3[64], b3
 
 
@@ -188,6 +195,8 @@ def lib():
     sig("mcd_lsm_american", vp, *D6, i32, i32, u64, u64, i32, i32, P(LsmResult), P(dbl), P(u8))
     sig("mcd_lsm_reprice_frozen", vp, *D6, i32, i32, u64, u64, P(dbl), P(u8), i32, i32, P(dbl))
     sig("mcd_lsm_batch", vp, vp, C.c_size_t, i32, i32, vp)
+    sig("mcd_lsm_frozen_greeks", vp, *D6, i32, i32, u64, u64, P(dbl), P(u8), i32, dbl, dbl, i32, vp)
+    sig("mcd_lsm_greeks_batch", vp, vp, C.c_size_t, dbl, dbl, i32, vp)
     F = P(C.c_float)
     sig("mcd_lsm_set_mlp_config", vp, i32, i32, dbl, dbl)
     sig("mcd_lsm_mlp_policy", vp, C.c_size_t, F, P(u8))
@@ -394,6 +403,32 @@ class Engine:
         self._check(self._lib.mcd_lsm_batch(self.handle, contracts.ctypes.data, len(contracts),
                                             _prec(precision), _regression(regression),
                                             out.ctypes.data))
+        return out
+
+    def lsm_frozen_greeks(self, spot, strike, rate, carry_yield, vol, time, type, monitoring_points,
+                          path_count, seed, coefficients, has, exercise_at_inception=False,
+                          spot_bump=None, vol_bump=None, precision="fp64") -> np.record:
+        """Delta, gamma and vega of an American option against its frozen QR policy
+        (mcd_lsm_frozen_greeks); bumps default to 1% of spot and of vol."""
+        co = np.ascontiguousarray(coefficients, dtype=np.float64)
+        ha = np.ascontiguousarray(has, dtype=np.uint8)
+        out = np.zeros(1, dtype=AMERICAN_GREEKS_DTYPE)
+        self._check(self._lib.mcd_lsm_frozen_greeks(
+            self.handle, spot, strike, rate, carry_yield, vol, time, type, monitoring_points, path_count,
+            seed, co.ctypes.data_as(P(dbl)), ha.ctypes.data_as(P(u8)), int(bool(exercise_at_inception)),
+            0.01 * spot if spot_bump is None else spot_bump, 0.01 * vol if vol_bump is None else vol_bump,
+            _prec(precision), out.ctypes.data))
+        return out[0]
+
+    def lsm_greeks_batch(self, contracts, spot_bump_rel=0.01, vol_bump_rel=0.01,
+                         precision="fp32") -> np.ndarray:
+        """Fits every contract's policy and returns its frozen-boundary Greeks
+        (mcd_lsm_greeks_batch) as an AMERICAN_GREEKS_DTYPE array."""
+        contracts = np.ascontiguousarray(contracts, dtype=LSM_CONTRACT_DTYPE)
+        out = np.zeros(len(contracts), dtype=AMERICAN_GREEKS_DTYPE)
+        self._check(self._lib.mcd_lsm_greeks_batch(self.handle, contracts.ctypes.data, len(contracts),
+                                                   spot_bump_rel, vol_bump_rel, _prec(precision),
+                                                   out.ctypes.data))
         return out
 
     # -- learned regression ----------------------------------------------------------------

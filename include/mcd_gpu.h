@@ -399,6 +399,40 @@ int mcd_pathwise_asian(mcd_ctx* ctx, double spot, double strike, double rate, do
                        int monitoring_points, uint64_t path_count, uint64_t seed, int precision,
                        mcd_pathwise_greeks* out);
 
+/* ---- frozen-boundary American Greeks --------------------------------------- */
+/* The reference's recipe for American sensitivities (tests/lsm_test.cpp:138-185):
+ * fit the Longstaff-Schwartz policy once, then reprice against that frozen
+ * policy (src/pricers/lsm.cpp:151-213) at bumped inputs on the same paths, so
+ * the exercise boundary does not jump between the bumped prices.  Here every
+ * scenario runs in one streaming pass (no path storage): each path carries
+ * the base state and the states at spot +/- spot_bump and vol +/- vol_bump.
+ * Values are central differences of the scenario prices, exactly as calling
+ * the replay once per scenario; standard errors are those of the per-path
+ * differences (common random numbers).  With exercise at inception every
+ * scenario price is the intrinsic value at its spot (the frozen decision). */
+typedef struct {
+    mcd_greek price;           /* frozen replay at the inputs (= the fitted price) */
+    mcd_greek delta, gamma, vega;
+    double scenario[4];        /* frozen prices at spot+h, spot-h, vol+h_v, vol-h_v */
+    double spot_bump, vol_bump;
+    uint64_t path_count;
+    int32_t exercise_at_inception;
+    int32_t reserved;
+} mcd_american_greeks;
+/* Against a given QR policy (as returned by mcd_lsm_american).  Bumps are
+ * absolute: 0 < spot_bump < spot, 0 < vol_bump < vol. */
+int mcd_lsm_frozen_greeks(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
+                          double vol, double time, int type, int monitoring_points, uint64_t path_count,
+                          uint64_t seed, const double* coefficients, const uint8_t* has_coefficients,
+                          int exercise_at_inception, double spot_bump, double vol_bump, int precision,
+                          mcd_american_greeks* out);
+/* Many contracts: fits every policy by the QR regression (as mcd_lsm_batch),
+ * then replays all scenarios of all contracts against the device-resident
+ * policies in one launch.  Bumps relative: h = spot_bump_rel * spot,
+ * h_v = vol_bump_rel * vol, each in (0, 1). */
+int mcd_lsm_greeks_batch(mcd_ctx* ctx, const mcd_lsm_contract* contracts, size_t n, double spot_bump_rel,
+                         double vol_bump_rel, int precision, mcd_american_greeks* results);
+
 /* ---- Sobol quasi-Monte Carlo ----------------------------------------------- */
 /* Dimensions of the Sobol generator: the reference's seven
  * (src/core/sobol.cpp:22-30) followed by every further primitive polynomial
