@@ -38,6 +38,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "device_common.cuh"
 #include "lsm.hpp"
 #include "lsm_mlp_dev.hpp"
@@ -718,8 +720,10 @@ struct __align__(1024) WideSmem {
     uint32_t tmem_base;
 };
 
+// Two CTAs per SM at most (256 tensor-memory columns and ~107 KB of shared
+// memory each), so up to 128 registers per thread cost no residency.
 template <int PREC>
-__global__ void __launch_bounds__(kWideThreads)
+__global__ void __launch_bounds__(kWideThreads, 2)
     lsm_mlp_pass_wide(int k, int mode, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
                       uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
                       const float* __restrict__ nets, const float* __restrict__ snaps,
@@ -743,8 +747,17 @@ __global__ void __launch_bounds__(kWideThreads)
     const bool fill = (mode & kFill) != 0;
     if (!step && !gram) return;
     const int s = threadIdx.x, warp = s >> 5, half = s >> 7, row = s & 127;
-    const double phi = c.type == 0 ? 1.0 : -1.0;
-    const double inv_k = 1.0 / c.strike;
+    // Per-path arithmetic in the path precision: FP64 on the FP64 path, FP32
+    // (paths, cash flows, exercise values, targets) on the FP32 path, where
+    // FP64 work would otherwise occupy the FP64 pipe (a small fraction of
+    // the FP32 rate on this GPU); the final payoff sums stay FP64.
+    using T = typename std::conditional<PREC == 0, double, float>::type;
+    const T phi = PREC == 0 ? T(c.type == 0 ? 1.0 : -1.0) : T(c.phi_f);
+    const T strike = PREC == 0 ? T(c.strike) : T(c.strike_f);
+    const T inv_k = PREC == 0 ? T(1.0 / c.strike) : T(c.inv_strike_f);
+    const T disc = PREC == 0 ? T(c.disc) : T(c.disc_f);
+    const T* S_path = static_cast<const T*>(store) + c.s_offset;
+    T* cft = reinterpret_cast<T*>(cf) + c.cf_offset;
     if (exercise) {
         const float* net = snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride;
         for (int i = s; i < kParams - kB2; i += kWideThreads) S.pd[kW2 + i] = net[kB2 + i];
@@ -774,25 +787,27 @@ __global__ void __launch_bounds__(kWideThreads)
     const uint32_t chunk0 = gl * c.group_chunks;
     const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
     Welford w{0ull, 0.0, 0.0};
+    unsigned n_sum = 0;  // FP32 path: per-thread FP64 sums of the last date's payoffs
+    double s1 = 0.0, s2 = 0.0;
     for (uint32_t ch = chunk0; ch < chunk1; ++ch) {
         for (int tile = 0; tile < kLsmChunk / kWideThreads; ++tile) {
             const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + tile * kWideThreads + s;
             const bool live = i < c.path_count;
-            double v = 0.0, ex_e = 0.0, ex_d = 0.0;
+            T v = T(0), ex_e = T(0), ex_d = T(0);
             if (live) {
                 if (init) {
-                    const double sT = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(n - 1) * c.path_count + i);
-                    const double x = phi * (sT - c.strike);
-                    v = x > 0.0 ? x : 0.0;
+                    const T sT = S_path[static_cast<uint64_t>(n - 1) * c.path_count + i];
+                    const T x = phi * (sT - strike);
+                    v = x > T(0) ? x : T(0);
                 } else {
-                    v = cf_load<PREC>(cf, c.cf_offset + i);
+                    v = cft[i];
                 }
             }
             if (exercise && live) {
-                const double se = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 1) * c.path_count + i);
-                const double xx = phi * (se - c.strike);
-                ex_e = xx > 0.0 ? xx : 0.0;
-                if (ex_e > 0.0) {
+                const T se = S_path[static_cast<uint64_t>(e - 1) * c.path_count + i];
+                const T xx = phi * (se - strike);
+                ex_e = xx > T(0) ? xx : T(0);
+                if (ex_e > T(0)) {
                     const uint4* src = feat_cache + (c.cf_offset + i) * 8;
                     float yh = S.pd[sB3];
 #pragma unroll
@@ -810,17 +825,28 @@ __global__ void __launch_bounds__(kWideThreads)
                 }
             }
             if (live && step) {
-                v *= c.disc;
-                if (last) welford_add(w, v);
-                else cf_store<PREC>(cf, c.cf_offset + i, v);
+                v *= disc;
+                if (last) {
+                    if constexpr (PREC == 0) {
+                        welford_add(w, v);
+                    } else {
+                        const double vd = static_cast<double>(v);
+                        ++n_sum;
+                        s1 += vd;
+                        s2 = fma(vd, vd, s2);
+                    }
+                } else {
+                    cft[i] = v;
+                }
             }
             if (gram) {
                 float x0 = 0.0f;
                 if (live) {
-                    const double s_d = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 2) * c.path_count + i);
-                    const double xx = phi * (s_d - c.strike);
-                    ex_d = xx > 0.0 ? xx : 0.0;
-                    x0 = static_cast<float>(4.0 * (s_d * inv_k - 1.0));
+                    const T s_d = S_path[static_cast<uint64_t>(e - 2) * c.path_count + i];
+                    const T xx = phi * (s_d - strike);
+                    ex_d = xx > T(0) ? xx : T(0);
+                    if constexpr (PREC == 0) x0 = static_cast<float>(4.0 * (s_d * inv_k - 1.0));
+                    else x0 = 4.0f * (s_d * inv_k - 1.0f);
                 }
                 layer1_row(S.pc, x0, x1d, S.h1c[half], row);
                 umma::fence_smem_to_async();
@@ -838,7 +864,7 @@ __global__ void __launch_bounds__(kWideThreads)
                 phase ^= 1u;
                 gram_pending = false;
                 umma::fence_after_sync();
-                const bool itm = live && ex_d > 0.0;
+                const bool itm = live && ex_d > T(0);
                 const float y = itm ? static_cast<float>((v - ex_d) * inv_k) : 0.0f;
                 uint4* dst = fill && itm ? feat_cache + (c.cf_offset + i) * 8 : nullptr;
                 for (int cc = 0; cc < 4; ++cc) {
@@ -877,6 +903,11 @@ __global__ void __launch_bounds__(kWideThreads)
             }
         }
         if (last) {  // one final partial per chunk, fixed tree
+            if constexpr (PREC == 1) {
+                w = welford_from_sums(n_sum, s1, s2);
+                n_sum = 0;
+                s1 = s2 = 0.0;
+            }
             Welford r = welford_warp_reduce(w);
             if ((s & 31) == 0) swf[warp] = r;
             __syncthreads();
