@@ -286,4 +286,71 @@ __device__ __forceinline__ Welford welford_from_sums(unsigned count, double s1, 
     return w;
 }
 
+// Payoff sums of the FP32 Longstaff-Schwartz kernels, whose threads price
+// only a few cash flows each: compensated FP32 sums (Knuth's TwoSum; hi + lo
+// carries ~2^-44 relative) of the values and of their squares (each square's
+// rounding error recovered exactly by an FMA), added up per thread and over
+// the warp tree in FP32, converted to FP64 once per warp and folded in FP64
+// above that.  Converting, adding or Welford-merging every cash flow in FP64
+// would occupy the FP64 pipe, a small fraction of the FP32 rate on this GPU.
+// Needs --fmad=false (TwoSum must not be contracted).
+struct Sum32 {
+    unsigned n;
+    float hi, lo, qhi, qlo;
+};
+struct Sum64 {
+    unsigned n;
+    double s1, s2;
+};
+
+__device__ __forceinline__ void two_sum_add(float& hi, float& lo, float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+}
+
+__device__ __forceinline__ void sum32_add(Sum32& a, float v) {
+    ++a.n;
+    two_sum_add(a.hi, a.lo, v);
+    const float p = v * v;
+    two_sum_add(a.qhi, a.qlo, p);
+    a.qlo += __fmaf_rn(v, v, -p);
+}
+
+__device__ __forceinline__ Sum32 sum32_warp_reduce(Sum32 a) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const unsigned n = __shfl_down_sync(0xffffffffu, a.n, off);
+        const float hi = __shfl_down_sync(0xffffffffu, a.hi, off);
+        const float lo = __shfl_down_sync(0xffffffffu, a.lo, off);
+        const float qhi = __shfl_down_sync(0xffffffffu, a.qhi, off);
+        const float qlo = __shfl_down_sync(0xffffffffu, a.qlo, off);
+        a.n += n;
+        two_sum_add(a.hi, a.lo, hi);
+        a.lo += lo;
+        two_sum_add(a.qhi, a.qlo, qhi);
+        a.qlo += qlo;
+    }
+    return a;
+}
+
+__device__ __forceinline__ Sum64 sum32_wide(const Sum32& a) {
+    return Sum64{a.n, static_cast<double>(a.hi) + static_cast<double>(a.lo),
+                 static_cast<double>(a.qhi) + static_cast<double>(a.qlo)};
+}
+
+// Warp sums folded in warp order (one thread), as a Welford triple.
+template <int W>
+__device__ __forceinline__ Welford sum64_fold(const Sum64* s) {
+    unsigned n = 0;
+    double s1 = 0.0, s2 = 0.0;
+    for (int w = 0; w < W; ++w) {
+        n += s[w].n;
+        s1 += s[w].s1;
+        s2 += s[w].s2;
+    }
+    return welford_from_sums(n, s1, s2);
+}
+
 }  // namespace mcdg

@@ -34,8 +34,9 @@
 // FP32 path evaluates the basis, the exercise tests and the Gram products in
 // FP32 (FP64 runs at a small fraction of the FP32 rate here), keeps the cash
 // flows and continuation values in FP32 and accumulates the Gram products
-// with compensated FP32 sums per chunk; chunk partials, the Cholesky-QR2
-// solves and the final payoff sums stay FP64.  (The FP32 discount factor
+// with compensated FP32 sums per chunk; the final payoffs are summed in
+// compensated FP32 per thread and over the warp tree (Sum32), warp sums,
+// chunk partials and the Cholesky-QR2 solves in FP64.  (The FP32 discount factor
 // carries a relative error below 3e-8 per date, a bias under 2e-6 of the
 // price after 50 dates.)
 //
@@ -218,6 +219,7 @@ __global__ void __launch_bounds__(kLsmThreads)
     __shared__ double smem[kLsmThreads / 32][11];
     __shared__ __align__(8) float smem_f[kLsmThreads / 32][11][2];
     __shared__ Welford swf[kLsmThreads / 32];
+    __shared__ Sum64 s64[kLsmThreads / 32];
     const uint32_t chunk = blockIdx.x;
     if (chunk >= total_chunks) return;
     const LsmDev c = cs[chunk_contract[chunk]];
@@ -301,7 +303,8 @@ __global__ void __launch_bounds__(kLsmThreads)
     } else {
         // FP32 paths: FP32 cash flows (stored in the FP64 buffer's space),
         // basis, continuation value, exercise tests and Gram products; the
-        // Gram sums are compensated, the final payoff sums FP64.
+        // Gram sums and the final payoff sums up to the warp are
+        // compensated FP32, everything above FP64.
         const float phi = c.phi_f, strike = c.strike_f, inv_kf = c.inv_strike_f, disc = c.disc_f;
         const float g0f = exercise ? re->gamma_f[0] : 0.0f, g1f = exercise ? re->gamma_f[1] : 0.0f,
                     g2f = exercise ? re->gamma_f[2] : 0.0f, g3f = exercise ? re->gamma_f[3] : 0.0f;
@@ -310,8 +313,7 @@ __global__ void __launch_bounds__(kLsmThreads)
         float hi[11], lo[11];
 #pragma unroll
         for (int q = 0; q < 11; ++q) hi[q] = lo[q] = 0.0f;
-        unsigned count = 0;
-        double s1 = 0.0, s2 = 0.0;
+        Sum32 fin{0u, 0.0f, 0.0f, 0.0f, 0.0f};  // final payoffs (last date)
         constexpr int kPer = kLsmChunk / kLsmThreads;
         // all loads of this thread's paths first (independent, in flight together)
         float vv[kPer], se[kPer], sd[kPer];
@@ -346,10 +348,7 @@ __global__ void __launch_bounds__(kLsmThreads)
             }
             v *= disc;
             if (last) {
-                const double vd = static_cast<double>(v);
-                ++count;
-                s1 += vd;
-                s2 = fma(vd, vd, s2);
+                sum32_add(fin, v);
             } else {
                 cff[i] = v;
                 if (gram && phi * (sd[j] - strike) > 0.0f) {
@@ -369,7 +368,10 @@ __global__ void __launch_bounds__(kLsmThreads)
                 }
             }
         }
-        if (last) w = welford_from_sums(count, s1, s2);
+        if (last) {
+            const Sum32 r = sum32_warp_reduce(fin);
+            if ((threadIdx.x & 31) == 0) s64[threadIdx.x >> 5] = sum32_wide(r);
+        }
         if (gram) {
             double acc[11];
             block_sum_df<11>(hi, lo, smem_f, acc);
@@ -380,13 +382,18 @@ __global__ void __launch_bounds__(kLsmThreads)
         }
     }
     if (last) {
-        w = welford_warp_reduce(w);
-        if ((threadIdx.x & 31) == 0) swf[threadIdx.x >> 5] = w;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            Welford m = swf[0];
-            for (int q = 1; q < kLsmThreads / 32; ++q) m = welford_merge(m, swf[q]);
-            final_part[chunk] = m;
+        if constexpr (PREC == 0) {
+            w = welford_warp_reduce(w);
+            if ((threadIdx.x & 31) == 0) swf[threadIdx.x >> 5] = w;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                Welford m = swf[0];
+                for (int q = 1; q < kLsmThreads / 32; ++q) m = welford_merge(m, swf[q]);
+                final_part[chunk] = m;
+            }
+        } else {
+            __syncthreads();
+            if (threadIdx.x == 0) final_part[chunk] = sum64_fold<kLsmThreads / 32>(s64);
         }
     }
 }

@@ -15,9 +15,10 @@
 // thread carries every scenario's state along one path, sharing the draws.
 //
 // Work layout, reductions and per-chunk partials are those of the backward
-// pass (lsm.cu): chunks of 1024 paths, 256 threads, a fixed Welford tree per
-// chunk, chunks merged in order per contract -- the base scenario reproduces
-// the stored-path replay's price bit for bit.
+// pass's last date (lsm.cu): chunks of 1024 paths, 256 threads, a fixed
+// reduction tree per chunk (FP64 Welford on the FP64 path, compensated FP32
+// sums up to the warp on the FP32 path), chunks merged in order per contract
+// -- the base scenario reproduces the fitted price bit for bit.
 //
 // nvcc-flags: --fmad=false
 #include <cuda_runtime.h>
@@ -168,6 +169,7 @@ __global__ void __launch_bounds__(kLsmThreads, (PREC == 1 && NS > 1) ? 3 : 2)
                       const LsmReg* __restrict__ reg, Welford* __restrict__ part) {
     constexpr int NW = NS == 1 ? 1 : kFrozenOutputs;
     __shared__ Welford swf[kLsmThreads / 32][NW];
+    __shared__ Sum64 s64[NW][kLsmThreads / 32];
     const uint32_t chunk = blockIdx.x;
     if (chunk >= total_chunks) return;
     const uint32_t ci = chunk_contract[chunk];
@@ -176,8 +178,8 @@ __global__ void __launch_bounds__(kLsmThreads, (PREC == 1 && NS > 1) ? 3 : 2)
     const LsmReg* rg = reg + c.reg_offset;
     const PhiloxKeys k = philox_keys(c.seed);
     const uint32_t local = chunk - c.chunk_begin;
-    Welford w[NW];
     if constexpr (PREC == 0) {
+        Welford w[NW];
 #pragma unroll
         for (int q = 0; q < NW; ++q) w[q] = Welford{0ull, 0.0, 0.0};
         for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
@@ -193,57 +195,46 @@ __global__ void __launch_bounds__(kLsmThreads, (PREC == 1 && NS > 1) ? 3 : 2)
                 welford_add(w[7], (v[3] - v[4]) * f.inv_2hv);
             }
         }
-    } else {
-        // FP32 cash flows; the scenario sums are FP64 per path (the backward
-        // pass's final form, so the base scenario keeps its bits).  The three
-        // differences only feed standard errors: FP32 over a thread's four
-        // paths, FP64 from there on (FP64 work is costly on this GPU).
-        unsigned count = 0;
-        double s1[NS], s2[NS];
-        float d1[3] = {0.0f, 0.0f, 0.0f}, d2[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-        for (int q = 0; q < NS; ++q) s1[q] = s2[q] = 0.0;
+        for (int q = 0; q < NW; ++q) {
+            const Welford r = welford_warp_reduce(w[q]);
+            if ((threadIdx.x & 31) == 0) swf[threadIdx.x >> 5][q] = r;
+        }
+        __syncthreads();
+        if (threadIdx.x < NW) {
+            const int q = threadIdx.x;
+            Welford m = swf[0][q];
+            for (int wi = 1; wi < kLsmThreads / 32; ++wi) m = welford_merge(m, swf[wi][q]);
+            part[static_cast<uint64_t>(chunk) * NW + q] = m;
+        }
+    } else {
+        // FP32 cash flows; compensated FP32 sums per thread and over the
+        // warp tree (Sum32, as the backward pass's last date, so the base
+        // scenario keeps its bits), FP64 from the warp sums on.
+        Sum32 acc[NW];
+#pragma unroll
+        for (int q = 0; q < NW; ++q) acc[q] = Sum32{0u, 0.0f, 0.0f, 0.0f, 0.0f};
         for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
             const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
             if (i >= c.path_count) break;
             float v[NS];
             replay32<NS>(c, f, rg, philox_path(i, 0u, k), k, v);
-            ++count;
 #pragma unroll
-            for (int q = 0; q < NS; ++q) {
-                const double vd = static_cast<double>(v[q]);
-                s1[q] += vd;
-                s2[q] = fma(vd, vd, s2[q]);
-            }
+            for (int q = 0; q < NS; ++q) sum32_add(acc[q], v[q]);
             if constexpr (NS == kFrozenScenarios) {
-                const float dd[3] = {(v[1] - v[2]) * f.inv_2hs_f, ((v[1] - v[0]) - (v[0] - v[2])) * f.inv_hs2_f,
-                                     (v[3] - v[4]) * f.inv_2hv_f};
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    d1[q] += dd[q];
-                    d2[q] = __fmaf_rn(dd[q], dd[q], d2[q]);
-                }
+                sum32_add(acc[5], (v[1] - v[2]) * f.inv_2hs_f);
+                sum32_add(acc[6], ((v[1] - v[0]) - (v[0] - v[2])) * f.inv_hs2_f);
+                sum32_add(acc[7], (v[3] - v[4]) * f.inv_2hv_f);
             }
         }
 #pragma unroll
-        for (int q = 0; q < NS; ++q) w[q] = welford_from_sums(count, s1[q], s2[q]);
-        if constexpr (NS == kFrozenScenarios) {
-#pragma unroll
-            for (int q = 0; q < 3; ++q)
-                w[NS + q] = welford_from_sums(count, static_cast<double>(d1[q]), static_cast<double>(d2[q]));
+        for (int q = 0; q < NW; ++q) {
+            const Sum32 r = sum32_warp_reduce(acc[q]);
+            if ((threadIdx.x & 31) == 0) s64[q][threadIdx.x >> 5] = sum32_wide(r);
         }
-    }
-#pragma unroll
-    for (int q = 0; q < NW; ++q) {
-        const Welford r = welford_warp_reduce(w[q]);
-        if ((threadIdx.x & 31) == 0) swf[threadIdx.x >> 5][q] = r;
-    }
-    __syncthreads();
-    if (threadIdx.x < NW) {
-        const int q = threadIdx.x;
-        Welford m = swf[0][q];
-        for (int wi = 1; wi < kLsmThreads / 32; ++wi) m = welford_merge(m, swf[wi][q]);
-        part[static_cast<uint64_t>(chunk) * NW + q] = m;
+        __syncthreads();
+        if (threadIdx.x < NW)
+            part[static_cast<uint64_t>(chunk) * NW + threadIdx.x] = sum64_fold<kLsmThreads / 32>(s64[threadIdx.x]);
     }
 }
 

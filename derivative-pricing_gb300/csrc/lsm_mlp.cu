@@ -732,6 +732,7 @@ __global__ void __launch_bounds__(kWideThreads, 2)
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     WideSmem& S = *reinterpret_cast<WideSmem*>(smem_raw);
     __shared__ Welford swf[kWideThreads / 32];
+    __shared__ Sum64 s64[kWideThreads / 32];
     const uint32_t g = blockIdx.x;
     if (g >= total_groups) return;
     const uint32_t ci = group_contract[g];
@@ -787,8 +788,7 @@ __global__ void __launch_bounds__(kWideThreads, 2)
     const uint32_t chunk0 = gl * c.group_chunks;
     const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
     Welford w{0ull, 0.0, 0.0};
-    unsigned n_sum = 0;  // FP32 path: per-thread FP64 sums of the last date's payoffs
-    double s1 = 0.0, s2 = 0.0;
+    Sum32 fin{0u, 0.0f, 0.0f, 0.0f, 0.0f};  // FP32 path: the last date's payoffs
     for (uint32_t ch = chunk0; ch < chunk1; ++ch) {
         for (int tile = 0; tile < kLsmChunk / kWideThreads; ++tile) {
             const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + tile * kWideThreads + s;
@@ -830,10 +830,7 @@ __global__ void __launch_bounds__(kWideThreads, 2)
                     if constexpr (PREC == 0) {
                         welford_add(w, v);
                     } else {
-                        const double vd = static_cast<double>(v);
-                        ++n_sum;
-                        s1 += vd;
-                        s2 = fma(vd, vd, s2);
+                        sum32_add(fin, v);
                     }
                 } else {
                     cft[i] = v;
@@ -903,21 +900,24 @@ __global__ void __launch_bounds__(kWideThreads, 2)
             }
         }
         if (last) {  // one final partial per chunk, fixed tree
-            if constexpr (PREC == 1) {
-                w = welford_from_sums(n_sum, s1, s2);
-                n_sum = 0;
-                s1 = s2 = 0.0;
+            if constexpr (PREC == 0) {
+                Welford r = welford_warp_reduce(w);
+                if ((s & 31) == 0) swf[warp] = r;
+                __syncthreads();
+                if (s == 0) {
+                    Welford m = swf[0];
+                    for (int q = 1; q < kWideThreads / 32; ++q) m = welford_merge(m, swf[q]);
+                    final_part[c.chunk_begin + ch] = m;
+                }
+                w = Welford{0ull, 0.0, 0.0};
+            } else {
+                const Sum32 r = sum32_warp_reduce(fin);
+                if ((s & 31) == 0) s64[warp] = sum32_wide(r);
+                __syncthreads();
+                if (s == 0) final_part[c.chunk_begin + ch] = sum64_fold<kWideThreads / 32>(s64);
+                fin = Sum32{0u, 0.0f, 0.0f, 0.0f, 0.0f};
             }
-            Welford r = welford_warp_reduce(w);
-            if ((s & 31) == 0) swf[warp] = r;
             __syncthreads();
-            if (s == 0) {
-                Welford m = swf[0];
-                for (int q = 1; q < kWideThreads / 32; ++q) m = welford_merge(m, swf[q]);
-                final_part[c.chunk_begin + ch] = m;
-            }
-            __syncthreads();
-            w = Welford{0ull, 0.0, 0.0};
         }
     }
     if (gram) {
