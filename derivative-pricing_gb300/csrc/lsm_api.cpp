@@ -298,6 +298,8 @@ FrozenScenario scenario(double spot, const mcd_lsm_contract& c, double vol) {
 }
 
 // Scenarios base, spot +/- hs, vol +/- hv (hs = hv = 0: the base alone).
+// The kernel shares the base's growth factors with the two spot scenarios,
+// so those must keep the base volatility.
 FrozenDev frozen_dev(const mcd_lsm_contract& c, double hs, double hv) {
     FrozenDev f{};
     f.sc[0] = scenario(c.spot, c, c.vol);

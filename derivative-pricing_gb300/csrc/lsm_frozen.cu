@@ -58,6 +58,20 @@ __device__ __forceinline__ float continuation32(float s, float inv_strike, const
     return __fmaf_rn(g[3], b3, __fmaf_rn(g[2], b2, __fmaf_rn(g[1], b1, g[0] * b0)));
 }
 
+// Scenarios by volatility: {base, spot+h, spot-h} share the base's GBM step
+// constants (and so its growth factors), vol+h and vol-h have their own.
+template <int NS>
+constexpr int kGroups = NS == 1 ? 1 : 3;
+__device__ __forceinline__ constexpr int group_of(int q) { return q < 3 ? 0 : q - 2; }
+__device__ __forceinline__ constexpr int group_lead(int gi) { return gi == 0 ? 0 : gi + 2; }
+template <int NS>
+__device__ __forceinline__ bool group_live(const bool (&live)[NS], int gi) {
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < NS; ++q) any = any || (group_of(q) == gi && live[q]);
+    return any;
+}
+
 // One path, NS scenarios: cash flow of each scenario, discounted to t = 0.
 template <int NS>
 __device__ void replay64(const LsmDev& c, const FrozenDev& f, const LsmReg* __restrict__ rg, const PhiloxPath& pp,
@@ -84,10 +98,19 @@ __device__ void replay64(const LsmDev& c, const FrozenDev& f, const LsmReg* __re
             g[2] = rg[date].gamma[2];
             g[3] = rg[date].gamma[3];
         }
+        // one growth factor per volatility group (src/models/gbm.cpp:7-12):
+        // the spot scenarios share the base's, bit for bit
+        double gr[kGroups<NS>];
+#pragma unroll
+        for (int gi = 0; gi < kGroups<NS>; ++gi) {
+            gr[gi] = 1.0;
+            if (group_live<NS>(live, gi))
+                gr[gi] = exp(f.sc[group_lead(gi)].drift + f.sc[group_lead(gi)].vs * z);
+        }
 #pragma unroll
         for (int q = 0; q < NS; ++q) {
             if (!live[q]) continue;
-            s[q] = s[q] * exp(f.sc[q].drift + f.sc[q].vs * z);  // src/models/gbm.cpp:7-12
+            s[q] = s[q] * gr[group_of(q)];
             if (test) {
                 const double ex = intrinsic(s[q], c.strike, c.type);
                 if (ex > 0.0 && ex > continuation64(s[q], c.strike, g)) {
@@ -109,12 +132,13 @@ __device__ void replay64(const LsmDev& c, const FrozenDev& f, const LsmReg* __re
 template <int NS>
 __device__ void replay32(const LsmDev& c, const FrozenDev& f, const LsmReg* __restrict__ rg, const PhiloxPath& pp,
                          const PhiloxKeys& k, float (&v)[NS]) {
-    float x[NS], s[NS];
+    float x[kGroups<NS>], s[NS];
     int stop[NS];
     bool live[NS];
 #pragma unroll
+    for (int gi = 0; gi < kGroups<NS>; ++gi) x[gi] = 0.0f;
+#pragma unroll
     for (int q = 0; q < NS; ++q) {
-        x[q] = 0.0f;
         s[q] = f.sc[q].spot_f;
         stop[q] = c.n_steps;
         live[q] = true;
@@ -133,12 +157,22 @@ __device__ void replay32(const LsmDev& c, const FrozenDev& f, const LsmReg* __re
             g[2] = rg[date].gamma_f[2];
             g[3] = rg[date].gamma_f[3];
         }
+        // the FP32 forward pass's log-space step (lsm.cu, lsm_forward), one
+        // log path per volatility group
+        float e[kGroups<NS>];
+#pragma unroll
+        for (int gi = 0; gi < kGroups<NS>; ++gi) {
+            e[gi] = 1.0f;
+            if (group_live<NS>(live, gi)) {
+                const FrozenScenario& g0 = f.sc[group_lead(gi)];
+                x[gi] = __fmaf_rn(g0.sg_f, z, x[gi] + g0.mu_f);
+                e[gi] = __expf(x[gi]);
+            }
+        }
 #pragma unroll
         for (int q = 0; q < NS; ++q) {
             if (!live[q]) continue;
-            // the FP32 forward pass's log-space step (lsm.cu, lsm_forward)
-            x[q] = __fmaf_rn(f.sc[q].sg_f, z, x[q] + f.sc[q].mu_f);
-            s[q] = f.sc[q].spot_f * __expf(x[q]);
+            s[q] = f.sc[q].spot_f * e[group_of(q)];
             if (test) {
                 const float ex = phi * (s[q] - strike);
                 if (ex > 0.0f && ex > continuation32(s[q], inv_k, g)) {
