@@ -709,6 +709,8 @@ __global__ void __launch_bounds__(128)
 // the cached modes only (no decision network to evaluate).
 // ---------------------------------------------------------------------------
 constexpr int kWideThreads = 256;
+constexpr uint32_t kRing = 512;           // ring slots (two tiles)
+constexpr int kRingOffset = 10 * 4096;    // byte offset of xt row 80 (core-matrix row group 10)
 
 struct __align__(1024) WideSmem {
     __nv_bfloat16 h1c[2][128 * 64];  // current network input, one 128-path half each
@@ -733,6 +735,7 @@ __global__ void __launch_bounds__(kWideThreads, 2)
     WideSmem& S = *reinterpret_cast<WideSmem*>(smem_raw);
     __shared__ Welford swf[kWideThreads / 32];
     __shared__ Sum64 s64[kWideThreads / 32];
+    __shared__ uint32_t warp_cnt[kWideThreads / 32];
     const uint32_t g = blockIdx.x;
     if (g >= total_groups) return;
     const uint32_t ci = group_contract[g];
@@ -789,11 +792,84 @@ __global__ void __launch_bounds__(kWideThreads, 2)
     const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
     Welford w{0ull, 0.0, 0.0};
     Sum32 fin{0u, 0.0f, 0.0f, 0.0f, 0.0f};  // FP32 path: the last date's payoffs
+    // Ring of in-the-money paths of date e-1 awaiting a 256-path feature tile
+    // (path index within the group, network input, target): the fit only
+    // uses those paths, so tiles carry no out-of-the-money rows.  It lives in
+    // rows 80..127 of xt: the Gram MMA reads those rows only into output
+    // rows that are never read (row i of D depends on row i of A alone; B is
+    // rows 0..79), so they are free for scratch.
+    uint32_t* q_idx = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(S.xt) + kRingOffset);
+    float* q_x0 = reinterpret_cast<float*>(q_idx + kRing);
+    float* q_y = q_x0 + kRing;
+    uint32_t q_head = 0, q_len = 0;  // uniform over the CTA
+    const uint64_t first_path = static_cast<uint64_t>(chunk0) * kLsmChunk;
+    // One tile: the n_valid ring entries from q_head (the rest of the rows
+    // zero): layer 1 on CUDA cores, Z2 = H1 W2^T (two 128-row halves), the
+    // GELU features (cached for the next date's decisions), then the Gram
+    // MMA over the tile's 256 columns.
+    auto feature_tile = [&](uint32_t n_valid) {
+        const uint32_t slot = (q_head + s) & (kRing - 1);
+        const bool valid = static_cast<uint32_t>(s) < n_valid;
+        const uint32_t local = valid ? q_idx[slot] : 0u;
+        const float x0 = valid ? q_x0[slot] : 0.0f;
+        const float y = valid ? q_y[slot] : 0.0f;
+        layer1_row(S.pc, x0, x1d, S.h1c[half], row);
+        umma::fence_smem_to_async();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (s == 0) {
+            umma::fence_after_sync();
+            for (int hh = 0; hh < 2; ++hh)
+                for (int kk = 0; kk < 4; ++kk)
+                    umma::mma_bf16(tm + 64 * hh, desc(S.h1c[hh], 1024, kk), desc(S.w2c, 1024, kk), kIdesc, kk > 0);
+            umma::mma_commit(&S.mbar);  // also covers the previous tile's Gram MMA
+        }
+        ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 21));
+        phase ^= 1u;
+        gram_pending = false;
+        umma::fence_after_sync();
+        uint4* dst = fill && valid ? feat_cache + (c.cf_offset + first_path + local) * 8 : nullptr;
+        for (int cc = 0; cc < 4; ++cc) {
+            float zz[16];
+            umma::tmem_ld16(umma::tmem_addr(tm, 32 * (warp & 3), 64 * half + cc * 16), zz);
+            uint32_t packed[8];
+#pragma unroll
+            for (int q = 0; q < 16; q += 2) {
+                float t;
+                const float ha = valid ? gelu(zz[q] + S.pc[sB2 + cc * 16 + q], t) : 0.0f;
+                const float hb = valid ? gelu(zz[q + 1] + S.pc[sB2 + cc * 16 + q + 1], t) : 0.0f;
+                const __nv_bfloat162 hp = __floats2bfloat162_rn(ha, hb);
+                *at(S.xt, cc * 16 + q, s, 256) = hp.x;
+                *at(S.xt, cc * 16 + q + 1, s, 256) = hp.y;
+                packed[q / 2] = *reinterpret_cast<const uint32_t*>(&hp);
+            }
+            if (dst) {
+                dst[2 * cc] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                dst[2 * cc + 1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+            }
+        }
+        *at(S.xt, 64, s, 256) = __float2bfloat16_rn(valid ? 1.0f : 0.0f);
+        *at(S.xt, 65, s, 256) = __float2bfloat16_rn(y);
+        umma::fence_smem_to_async();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (s == 0) {
+            umma::fence_after_sync();
+            // D[i][j] += sum over the tile's 256 columns of xt[i][p] xt[j][p]  (M = 128, N = 80, K = 256)
+            for (int kk = 0; kk < 16; ++kk)
+                umma::mma_bf16(tm + 128, desc(S.xt, 4096, kk), desc(S.xt, 4096, kk), umma::idesc_bf16(128, kGramN),
+                               gram_started || kk > 0);
+        }
+        gram_started = true;
+        gram_pending = true;
+        q_head = (q_head + n_valid) & (kRing - 1);
+        q_len -= n_valid;
+    };
     for (uint32_t ch = chunk0; ch < chunk1; ++ch) {
         for (int tile = 0; tile < kLsmChunk / kWideThreads; ++tile) {
             const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + tile * kWideThreads + s;
             const bool live = i < c.path_count;
-            T v = T(0), ex_e = T(0), ex_d = T(0);
+            T v = T(0), ex_e = T(0);
             if (live) {
                 if (init) {
                     const T sT = S_path[static_cast<uint64_t>(n - 1) * c.path_count + i];
@@ -837,66 +913,38 @@ __global__ void __launch_bounds__(kWideThreads, 2)
                 }
             }
             if (gram) {
-                float x0 = 0.0f;
+                // the paths in the money at date e-1 join the ring of paths
+                // awaiting a feature tile; the others take no part in the fit
+                bool itm = false;
+                float x0 = 0.0f, y = 0.0f;
                 if (live) {
                     const T s_d = S_path[static_cast<uint64_t>(e - 2) * c.path_count + i];
                     const T xx = phi * (s_d - strike);
-                    ex_d = xx > T(0) ? xx : T(0);
+                    const T ex_d = xx > T(0) ? xx : T(0);
+                    itm = ex_d > T(0);
                     if constexpr (PREC == 0) x0 = static_cast<float>(4.0 * (s_d * inv_k - 1.0));
                     else x0 = 4.0f * (s_d * inv_k - 1.0f);
+                    y = static_cast<float>((v - ex_d) * inv_k);
                 }
-                layer1_row(S.pc, x0, x1d, S.h1c[half], row);
-                umma::fence_smem_to_async();
-                umma::fence_before_sync();
+                const unsigned bal = __ballot_sync(0xffffffffu, itm);
+                if ((s & 31) == 0) warp_cnt[warp] = __popc(bal);
                 __syncthreads();
-                if (s == 0) {
-                    umma::fence_after_sync();
-                    for (int hh = 0; hh < 2; ++hh)
-                        for (int kk = 0; kk < 4; ++kk)
-                            umma::mma_bf16(tm + 64 * hh, desc(S.h1c[hh], 1024, kk), desc(S.w2c, 1024, kk), kIdesc,
-                                           kk > 0);
-                    umma::mma_commit(&S.mbar);  // also covers the previous tile's Gram MMA
+                uint32_t before = 0, total = 0;
+                for (int wi = 0; wi < kWideThreads / 32; ++wi) {
+                    const uint32_t cw = warp_cnt[wi];
+                    before += wi < warp ? cw : 0u;
+                    total += cw;
                 }
-                ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 21));
-                phase ^= 1u;
-                gram_pending = false;
-                umma::fence_after_sync();
-                const bool itm = live && ex_d > T(0);
-                const float y = itm ? static_cast<float>((v - ex_d) * inv_k) : 0.0f;
-                uint4* dst = fill && itm ? feat_cache + (c.cf_offset + i) * 8 : nullptr;
-                for (int cc = 0; cc < 4; ++cc) {
-                    float zz[16];
-                    umma::tmem_ld16(umma::tmem_addr(tm, 32 * (warp & 3), 64 * half + cc * 16), zz);
-                    uint32_t packed[8];
-#pragma unroll
-                    for (int q = 0; q < 16; q += 2) {
-                        float t;
-                        const float ha = itm ? gelu(zz[q] + S.pc[sB2 + cc * 16 + q], t) : 0.0f;
-                        const float hb = itm ? gelu(zz[q + 1] + S.pc[sB2 + cc * 16 + q + 1], t) : 0.0f;
-                        const __nv_bfloat162 hp = __floats2bfloat162_rn(ha, hb);
-                        *at(S.xt, cc * 16 + q, s, 256) = hp.x;
-                        *at(S.xt, cc * 16 + q + 1, s, 256) = hp.y;
-                        packed[q / 2] = *reinterpret_cast<const uint32_t*>(&hp);
-                    }
-                    if (dst) {
-                        dst[2 * cc] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                        dst[2 * cc + 1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-                    }
+                if (itm) {
+                    const uint32_t pos =
+                        (q_head + q_len + before + __popc(bal & ((1u << (s & 31)) - 1u))) & (kRing - 1);
+                    q_idx[pos] = static_cast<uint32_t>(i - first_path);
+                    q_x0[pos] = x0;
+                    q_y[pos] = y;
                 }
-                *at(S.xt, 64, s, 256) = __float2bfloat16_rn(itm ? 1.0f : 0.0f);
-                *at(S.xt, 65, s, 256) = __float2bfloat16_rn(y);
-                umma::fence_smem_to_async();
-                umma::fence_before_sync();
+                q_len += total;
                 __syncthreads();
-                if (s == 0) {
-                    umma::fence_after_sync();
-                    // D[i][j] += sum over the 256 paths of xt[i][p] xt[j][p]  (M = 128, N = 80, K = 256)
-                    for (int kk = 0; kk < 16; ++kk)
-                        umma::mma_bf16(tm + 128, desc(S.xt, 4096, kk), desc(S.xt, 4096, kk),
-                                       umma::idesc_bf16(128, kGramN), gram_started || kk > 0);
-                }
-                gram_started = true;
-                gram_pending = true;
+                if (q_len >= static_cast<uint32_t>(kWideThreads)) feature_tile(kWideThreads);
             }
         }
         if (last) {  // one final partial per chunk, fixed tree
@@ -920,6 +968,7 @@ __global__ void __launch_bounds__(kWideThreads, 2)
             __syncthreads();
         }
     }
+    if (gram && q_len > 0) feature_tile(q_len);  // the remainder (< 256 paths)
     if (gram) {
         if (gram_pending) {
             if (s == 0) umma::mma_commit(&S.mbar);
@@ -936,7 +985,8 @@ __global__ void __launch_bounds__(kWideThreads, 2)
                 if (s < kGramDim)
                     for (int q = 0; q < 16; ++q) {
                         const int col = cc * 16 + q;
-                        if (col >= s && col < kGramDim) out[row0 + col - s] = ok ? dd[q] : 0.0f;
+                        // no in-the-money path in this group: no MMA wrote the accumulator
+                        if (col >= s && col < kGramDim) out[row0 + col - s] = ok && gram_started ? dd[q] : 0.0f;
                     }
             }
         }
