@@ -169,13 +169,13 @@ void escaped(std::string& out, const std::string& s) {
     out += '"';
 }
 
-void write(std::string& out, const Value& v) {
+void write(std::string& out, const Value& v, int digits) {
     switch (v.type) {
         case Value::Type::Null: out += "null"; break;
         case Value::Type::Bool: out += v.b ? "true" : "false"; break;
         case Value::Type::Number: {
             char buf[64];
-            const int n = std::snprintf(buf, sizeof buf, "%.10g", v.num);
+            const int n = std::snprintf(buf, sizeof buf, "%.*g", digits, v.num);
             out.append(buf, static_cast<size_t>(n));
             break;
         }
@@ -184,7 +184,7 @@ void write(std::string& out, const Value& v) {
             out += '[';
             for (size_t i = 0; i < v.items.size(); ++i) {
                 if (i) out += ',';
-                write(out, v.items[i]);
+                write(out, v.items[i], digits);
             }
             out += ']';
             break;
@@ -196,13 +196,13 @@ void write(std::string& out, const Value& v) {
 
 Object parse_object(std::string_view text) { return Reader(text).top_level(); }
 
-std::string serialize(const Object& obj) {
+std::string serialize(const Object& obj, int digits) {
     std::string out = "{";
     for (size_t i = 0; i < obj.size(); ++i) {
         if (i) out += ',';
         escaped(out, obj[i].first);
         out += ':';
-        write(out, obj[i].second);
+        write(out, obj[i].second, digits);
     }
     out += '}';
     return out;

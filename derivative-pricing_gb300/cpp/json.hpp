@@ -1,7 +1,8 @@
 // json.hpp -- the JSON subset of the CLI schema: one flat object of null,
 // bool, number, string and (for the batch request only) arrays of numbers or
-// strings.  Numbers are written with "%.10g" and objects keep insertion
-// order, as the reference CLI prints them (src/core/json.cpp:276-321).
+// strings.  Numbers are written with "%.10g" by default and objects keep
+// insertion order, as the reference CLI prints them (src/core/json.cpp:276-321);
+// 17 digits round-trip a double exactly.
 #pragma once
 
 #include <stdexcept>
@@ -54,7 +55,7 @@ struct ParseError : std::runtime_error {
 };
 
 Object parse_object(std::string_view text);
-std::string serialize(const Object& obj);
+std::string serialize(const Object& obj, int digits = 10);
 const Value* find(const Object& obj, std::string_view key);
 
 }  // namespace mcdjson

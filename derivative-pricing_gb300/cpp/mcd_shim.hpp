@@ -225,3 +225,18 @@ PathwiseGreeks pathwise_asian(double spot, double strike, double rate, double ca
 }  // namespace greeks
 
 }  // namespace mcd
+
+// ---- the JSON request handler (request.cpp), C linkage -------------------
+// One JSON request object in, one JSON object out (the result, or
+// {"error": message}); the returned string is released with mcd_shim_free.
+// dialect: MCD_SHIM_DIALECT_CLI (the reference CLI's messages) or
+// MCD_SHIM_DIALECT_LAMBDA (the reference Lambda layer's messages, its
+// variance-reduction toggles and max_path_count, 0 = no cap).
+// status: MCD_SHIM_OK, MCD_SHIM_REQUEST_ERROR (bad request) or
+// MCD_SHIM_INTERNAL_ERROR (the device failed).
+extern "C" {
+enum { MCD_SHIM_DIALECT_CLI = 0, MCD_SHIM_DIALECT_LAMBDA = 1 };
+enum { MCD_SHIM_OK = 0, MCD_SHIM_REQUEST_ERROR = 1, MCD_SHIM_INTERNAL_ERROR = 2 };
+char* mcd_shim_handle_request(const char* request, int dialect, uint64_t max_path_count, int* status);
+void mcd_shim_free(char* response);
+}
