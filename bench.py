@@ -42,8 +42,10 @@ UNIT = "paths/s"
 WORKLOAD = "batch of 4096 path-dependent GBM contracts (asian/barrier/lookback/digital), FP32 paths"
 
 
-def make_batch(n=4096, seed=42):
-    """The configuration's contract list (mcd_contract records)."""
+def make_batch(n=4096, seed=42, rank=0):
+    """The configuration's contract list (mcd_contract records).  Replica `rank`
+    of a multi-GPU run prices the same contract terms on its own pricing seeds
+    (42 + rank n + i), so N ranks price a book N times the size (weak scaling)."""
     import mcd_gpu as M
     rng = np.random.default_rng(seed)
     c = M.contracts(n)
@@ -76,8 +78,19 @@ def make_batch(n=4096, seed=42):
     c["barrier"] = np.where(c["direction"] == 0, 100.0 * (1 + h), 100.0 * (1 - h))
     c["rebate"] = 0.0
     c["cash_amount"] = 1.0
-    c["seed"] = 42 + np.arange(n, dtype=np.uint64)
+    c["seed"] = 42 + np.uint64(rank * n) + np.arange(n, dtype=np.uint64)
     return c
+
+
+def max_over_ranks(x, device="cpu"):
+    """The largest of every rank's x (the job's time is its slowest rank's)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def path_steps(c):
@@ -404,9 +417,9 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    # Replicas: every rank prices its own copy of the batch (the path does not
-    # need a collective, multi-GPU).
-    c = make_batch(args.contracts)
+    # Replicas: every rank prices its own batch (same terms, its own seeds); the
+    # path has no exchange step, so no collective touches the data.
+    c = make_batch(args.contracts, rank=rank)
     n = len(c)
     total_paths = float(c["path_count"].astype(np.float64).sum())
     total_steps = path_steps(c)
@@ -453,10 +466,7 @@ def main():
         torch.distributed.barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = sum(step_ms) / len(step_ms)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, device="cuda")
     kernel_ms, launches = eng.kernel_timing(reset=True)
     if not kernel_ms > 0:
         raise RuntimeError("no kernel timing was collected")
@@ -474,7 +484,7 @@ def main():
         t1 = time.perf_counter()
         if i >= args.warmup:
             e2e_ms.append((t1 - t0) * 1e3)
-    e2e = sum(e2e_ms) / len(e2e_ms)
+    e2e = max_over_ranks(sum(e2e_ms) / len(e2e_ms), device="cuda")
     assert host_out.tobytes() == results.tobytes(), "device-resident and host paths disagree"
 
     line = {
