@@ -177,39 +177,56 @@ __device__ __forceinline__ float fast_rcp(float x) {
 // Standard normal of the reference's u = (bits+0.5)/2^32, in FP32.
 //
 // q = min(u, 1-u) is formed from the bits (for bits >= 2^31 the mirror
-// 1-u = (~bits + 0.5)/2^32), so the tails keep full relative precision.  The
-// transform is Wichura's AS241 single-precision form (PPND7, Applied
-// Statistics 37:477-484, 1988; relative accuracy ~1e-7): a 3/3 rational in
-// r = 0.180625 - (q-1/2)^2 for |q-1/2| <= 0.425, else a 3/2 rational in
-// sqrt(-ln q) - 1.6.  (Its third branch, sqrt(-ln q) > 5, needs q < 1.4e-11,
-// which 32-bit inputs never reach: q >= 2^-33.)  Acklam's central rational,
-// used by the FP64 path, nearly cancels in both numerator and denominator near
-// its break point and loses ~4 digits in FP32, which is why it is not used
-// here.  Both branches are evaluated as one Horner chain with per-lane
-// coefficient selects, so a warp never diverges.
-// Lower-half deviate Phi^-1(q) for q in (0, 1/2] (AS241 PPND7, see above).
-__device__ __forceinline__ float ppnd7_lower(float q) {
-    const float t = q - 0.5f;                      // in [-0.5, 0]
-    const bool central = t >= -0.425f;
-    const float s = fast_sqrt(-__logf(q)) - 1.6f;  // tail variable (unused when central)
-    const float v = central ? __fmaf_rn(-t, t, 0.180625f) : s;
-    float num = central ? 5.9109374720e+01f : 1.7023821103e-01f;
-    num = __fmaf_rn(num, v, central ? 1.5929113202e+02f : 1.3067284816e+00f);
-    num = __fmaf_rn(num, v, central ? 5.0434271938e+01f : 2.7568153900e+00f);
-    num = __fmaf_rn(num, v, central ? 3.3871327179e+00f : 1.4234372777e+00f);
-    float den = central ? 6.7187563600e+01f : 0.0f;
-    den = __fmaf_rn(den, v, central ? 7.8757757664e+01f : 1.2021132975e-01f);
-    den = __fmaf_rn(den, v, central ? 1.7895169469e+01f : 7.3700164250e-01f);
-    den = __fmaf_rn(den, v, 1.0f);
-    return num * fast_rcp(den) * (central ? t : -1.0f);
+// 1-u = (~bits + 0.5)/2^32), so the tails keep full relative precision.
+// With x = 1 - 2q and w = -ln(4 q (1 - q)) = -ln(1 - x^2), Phi^-1(1 - q) =
+// x P(w) for a P that is smooth in w (M. Giles' change of variable for erfinv,
+// "Approximating the erfinv function", GPU Computing Gems Jade, 2011).  P is a
+// polynomial of degree 8 in w - 2.5 for w < 5 (q > 0.0017, 99.66 % of the
+// draws) and of degree 9 in sqrt(w) - 3 above (32-bit inputs give q >= 2^-33,
+// so w <= 21.5); the coefficients are this project's own least-squares fits to
+// the double-precision quantile (csrc/fit_inverse_normal.py), with relative fit
+// errors of 9.4e-8 and 1.2e-7.  One MUFU log2, eight or nine FMAs and the
+// product: about half the instructions of a rational with per-lane branch
+// selects, which every warp would pay for both branches.  Only warps holding a
+// tail draw (about one in ten) also run the second polynomial.
+__device__ __forceinline__ float inv_normal_upper(float q) {  // Phi^-1(1 - q) >= 0, q in (0, 1/2]
+    const float y = __fmaf_rn(-q, q, q);                                   // q (1 - q)
+    const float w = __fmaf_rn(__log2f(y), -0.693147181f, -1.386294361f);   // -ln(4 y)
+    const float x = __fmaf_rn(-2.0f, q, 1.0f);                             // 1 - 2q
+    float p;
+    if (w < 5.0f) {
+        const float t = w - 2.5f;
+        p = 4.035420447e-08f;
+        p = __fmaf_rn(p, t, 4.861469141e-07f);
+        p = __fmaf_rn(p, t, -4.990533717e-06f);
+        p = __fmaf_rn(p, t, -6.218398536e-06f);
+        p = __fmaf_rn(p, t, 3.091499728e-04f);
+        p = __fmaf_rn(p, t, -1.773009095e-03f);
+        p = __fmaf_rn(p, t, -5.908170540e-03f);
+        p = __fmaf_rn(p, t, 3.488026592e-01f);
+        p = __fmaf_rn(p, t, 2.123313567e+00f);
+    } else {
+        const float t = fast_sqrt(w) - 3.0f;
+        p = 5.067717386e-05f;
+        p = __fmaf_rn(p, t, -2.118356777e-04f);
+        p = __fmaf_rn(p, t, -3.360669450e-05f);
+        p = __fmaf_rn(p, t, 1.810359006e-03f);
+        p = __fmaf_rn(p, t, -5.043195909e-03f);
+        p = __fmaf_rn(p, t, 8.166690883e-03f);
+        p = __fmaf_rn(p, t, -1.082257433e-02f);
+        p = __fmaf_rn(p, t, 1.333906298e-02f);
+        p = __fmaf_rn(p, t, 1.416583983e+00f);
+        p = __fmaf_rn(p, t, 4.006434684e+00f);
+    }
+    return p * x;
 }
 
 __device__ __forceinline__ float normal_from_bits_f32(uint32_t bits) {
     const bool upper = (bits >> 31) != 0u;
     const uint32_t m = upper ? ~bits : bits;
     const float q = __fmaf_rn(__uint2float_rn(m), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
-    const float z = ppnd7_lower(q);
-    return upper ? -z : z;
+    const float z = inv_normal_upper(q);
+    return upper ? z : -z;
 }
 
 // Standard normal of a Sobol coordinate u = x / 2^32 (x > 0), in FP32: the
@@ -217,8 +234,8 @@ __device__ __forceinline__ float normal_from_bits_f32(uint32_t bits) {
 __device__ __forceinline__ float normal_from_sobol_f32(uint32_t x) {
     const bool upper = x > 0x80000000u;
     const uint32_t m = upper ? (0u - x) : x;
-    const float z = ppnd7_lower(__uint2float_rn(m) * 2.3283064365386963e-10f);
-    return upper ? -z : z;
+    const float z = inv_normal_upper(__uint2float_rn(m) * 2.3283064365386963e-10f);
+    return upper ? z : -z;
 }
 
 // Uniform (bits+0.5)/2^32 in FP32 (for comparisons against probabilities).
