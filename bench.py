@@ -506,8 +506,8 @@ def main():
     # Roofline of the persistent path kernel.  It is ALU-bound (no path data in
     # memory), so the bound is instruction issue: 4 SMSPs x 1 warp-instruction
     # per clock per SM.  Instructions per path-step are measured by ncu on the
-    # same kernel (profiles/path_kernel_fp32_batch.md: 1.9196e10 warp
-    # instructions for 6.807e9 path-steps = 90.2 thread-instructions each).
+    # same kernel (profiles/path_kernel_fp32_batch.md: 1.6964e10 warp
+    # instructions for 6.807e9 path-steps = 79.7 thread-instructions each).
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -517,19 +517,19 @@ def main():
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     clk = clocks.summary()
     mhz = clk["sm_mhz"] or peaks.get("sm_max_mhz", 2070.0)
-    inst_per_step = 90.2
+    inst_per_step = 79.7
     achieved = total_steps * inst_per_step / 32.0 / (kernel_ms / 1e3) / 1e12
     peak = sm_count * 4 * mhz * 1e6 / 1e12
     line["roofline"] = {
         "bound": "alu", "achieved": achieved, "peak": peak, "unit": "Twarp-inst/s",
         "frac": achieved / peak,
-        # DRAM bytes of the 256-contract ncu capture (167,424 B) scaled by contracts
+        # DRAM bytes of the 256-contract ncu capture (127,744 B) scaled by contracts
         # (the kernel reads contract records and writes slab partials only).
-        "traffic": 167424.0 * n / 256.0,
+        "traffic": 127744.0 * n / 256.0,
         "kernel_ms": kernel_ms, "launches": launches,
         "path_steps_per_second_kernel": total_steps / (kernel_ms / 1e3),
         "note": "issue-slot roofline (4 warp-inst/clk/SM at the sampled SM clock); "
-                "90.2 thread-instructions per path-step measured by ncu; "
+                "79.7 thread-instructions per path-step measured by ncu; "
                 "no HBM or tensor-core bound applies to this kernel"}
     line["clocks"] = clk
 

@@ -150,6 +150,78 @@ __device__ __forceinline__ float draw32(const PhiloxPath& pp, uint32_t step, con
     return neg ? -z : z;
 }
 
+// Path-dependent products (Asians, discrete barrier, lookbacks), NP paths
+// (or antithetic halves) at once: their draws are independent dependency
+// chains, so interleaving them gives every warp NP-fold instruction-level
+// parallelism.  Each path's arithmetic is the single-path one, so the samples
+// do not depend on NP.
+template <int KIND, int NP>
+__device__ __forceinline__ void path_dependent32(const DevContract& c, const PhiloxKeys& k,
+                                                 const PhiloxPath (&pp)[NP], const bool (&neg)[NP],
+                                                 double (&out)[NP]) {
+    const float phi = c.type == 0 ? 1.0f : -1.0f;
+    const float mu = static_cast<float>(c.drift);
+    const float sg = static_cast<float>(c.vs);
+    const float s0 = static_cast<float>(c.spot);
+    const float strike = static_cast<float>(c.strike);
+    const float lnh = static_cast<float>(c.log_h_rel);
+    float x[NP], acc[NP], acc2[NP], xmax[NP], xmin[NP];  // log path, sum of S/S0, sum of x, extrema
+    bool breached[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        x[p] = acc[p] = acc2[p] = xmax[p] = xmin[p] = 0.0f;
+        breached[p] = false;
+    }
+    for (int step = 0; step < c.n_steps; ++step) {
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const float z = draw32(pp[p], static_cast<uint32_t>(step), k, neg[p]);
+            x[p] = __fmaf_rn(sg, z, x[p] + mu);
+            if constexpr (KIND == kAsianArith) {
+                acc[p] += __expf(x[p]);
+            } else if constexpr (KIND == kAsianGeo) {
+                acc2[p] += x[p];
+            } else if constexpr (KIND == kAsianCv) {
+                acc[p] += __expf(x[p]);
+                acc2[p] += x[p];
+            } else if constexpr (KIND == kBarrier) {
+                const bool crossed = c.up ? x[p] >= lnh : x[p] <= lnh;
+                breached[p] = breached[p] || crossed;
+            } else {
+                xmax[p] = fmaxf(xmax[p], x[p]);
+                xmin[p] = fminf(xmin[p], x[p]);
+            }
+        }
+    }
+    const float inv_n = 1.0f / static_cast<float>(c.n_steps);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const float last = s0 * __expf(x[p]);
+        if constexpr (KIND == kAsianArith || KIND == kAsianGeo) {
+            const float avg = KIND == kAsianArith ? s0 * (acc[p] * inv_n) : s0 * __expf(acc2[p] * inv_n);
+            const float ref = c.floating ? (last - avg) : (avg - strike);
+            out[p] = c.discount * static_cast<double>(fmaxf(phi * ref, 0.0f));
+        } else if constexpr (KIND == kAsianCv) {
+            const float a = s0 * (acc[p] * inv_n);
+            const float g = s0 * __expf(acc2[p] * inv_n);
+            const double ap = c.discount * static_cast<double>(fmaxf(phi * (a - strike), 0.0f));
+            const double gp = c.discount * static_cast<double>(fmaxf(phi * (g - strike), 0.0f));
+            out[p] = ap - (gp - c.kv_anchor);
+        } else if constexpr (KIND == kBarrier) {
+            const float vanilla = fmaxf(phi * (last - strike), 0.0f);
+            const bool pays = c.out ? !breached[p] : breached[p];
+            out[p] = c.discount * static_cast<double>(pays ? vanilla : static_cast<float>(c.rebate));
+        } else if constexpr (KIND == kLookbackFixed) {
+            const float v = c.type == 0 ? fmaxf(s0 * __expf(xmax[p]) - strike, 0.0f)
+                                        : fmaxf(strike - s0 * __expf(xmin[p]), 0.0f);
+            out[p] = c.discount * static_cast<double>(v);
+        } else {
+            const float v = c.type == 0 ? (last - s0 * __expf(xmin[p])) : (s0 * __expf(xmax[p]) - last);
+            out[p] = c.discount * static_cast<double>(v);
+        }
+    }
+}
+
 // Returns the discounted sample in FP64 (the payoff itself is FP32).
 template <int KIND>
 __device__ double sample32(const DevContract& c, const PhiloxKeys& k, uint64_t path, bool neg) {
@@ -193,53 +265,11 @@ __device__ double sample32(const DevContract& c, const PhiloxKeys& k, uint64_t p
         const bool pays = c.out ? !breached : breached;
         return c.discount * static_cast<double>(pays ? vanilla : static_cast<float>(c.rebate));
     } else {
-        float x = 0.0f;
-        float acc = 0.0f, acc2 = 0.0f;      // arithmetic sum of S/S0, sum of x
-        float xmax = 0.0f, xmin = 0.0f;
-        bool breached = false;
-        const float lnh = static_cast<float>(c.log_h_rel);
-        for (int step = 0; step < c.n_steps; ++step) {
-            const float z = draw32(pp, static_cast<uint32_t>(step), k, neg);
-            x = __fmaf_rn(sg, z, x + mu);
-            if constexpr (KIND == kAsianArith) {
-                acc += __expf(x);
-            } else if constexpr (KIND == kAsianGeo) {
-                acc2 += x;
-            } else if constexpr (KIND == kAsianCv) {
-                acc += __expf(x);
-                acc2 += x;
-            } else if constexpr (KIND == kBarrier) {
-                const bool crossed = c.up ? x >= lnh : x <= lnh;
-                breached = breached || crossed;
-            } else {
-                xmax = fmaxf(xmax, x);
-                xmin = fminf(xmin, x);
-            }
-        }
-        const float inv_n = 1.0f / static_cast<float>(c.n_steps);
-        const float last = s0 * __expf(x);
-        if constexpr (KIND == kAsianArith || KIND == kAsianGeo) {
-            const float avg = KIND == kAsianArith ? s0 * (acc * inv_n) : s0 * __expf(acc2 * inv_n);
-            const float ref = c.floating ? (last - avg) : (avg - strike);
-            return c.discount * static_cast<double>(fmaxf(phi * ref, 0.0f));
-        } else if constexpr (KIND == kAsianCv) {
-            const float a = s0 * (acc * inv_n);
-            const float g = s0 * __expf(acc2 * inv_n);
-            const double ap = c.discount * static_cast<double>(fmaxf(phi * (a - strike), 0.0f));
-            const double gp = c.discount * static_cast<double>(fmaxf(phi * (g - strike), 0.0f));
-            return ap - (gp - c.kv_anchor);
-        } else if constexpr (KIND == kBarrier) {
-            const float vanilla = fmaxf(phi * (last - strike), 0.0f);
-            const bool pays = c.out ? !breached : breached;
-            return c.discount * static_cast<double>(pays ? vanilla : static_cast<float>(c.rebate));
-        } else if constexpr (KIND == kLookbackFixed) {
-            const float v = c.type == 0 ? fmaxf(s0 * __expf(xmax) - strike, 0.0f)
-                                        : fmaxf(strike - s0 * __expf(xmin), 0.0f);
-            return c.discount * static_cast<double>(v);
-        } else {
-            const float v = c.type == 0 ? (last - s0 * __expf(xmin)) : (s0 * __expf(xmax) - last);
-            return c.discount * static_cast<double>(v);
-        }
+        const PhiloxPath pps[1] = {pp};
+        const bool negs[1] = {neg};
+        double out[1];
+        path_dependent32<KIND, 1>(c, k, pps, negs, out);
+        return out[0];
     }
 }
 
@@ -247,6 +277,49 @@ template <int KIND>
 __device__ Welford slab32(const DevContract& c, const PhiloxKeys& k, uint64_t base) {
     unsigned count = 0;
     double s1 = 0.0, s2 = 0.0;
+    constexpr bool kPathDependent = KIND != kEuropean && KIND != kDigital && KIND != kBarrierBridge;
+    if constexpr (kPathDependent) {
+        if (c.antithetic) {  // the two halves of an antithetic sample share their draws
+            for (int j = 0; j < kPathsPerThread; ++j) {
+                const uint64_t path = base + static_cast<uint64_t>(j * kSlabThreads) + threadIdx.x;
+                if (path >= c.path_count) break;
+                const PhiloxPath pp = philox_path(path, 0u, k);
+                const PhiloxPath pps[2] = {pp, pp};
+                const bool negs[2] = {false, true};
+                double out[2];
+                path_dependent32<KIND, 2>(c, k, pps, negs, out);
+                const double sample = 0.5 * (out[0] + out[1]);
+                ++count;
+                s1 += sample;
+                s2 = fma(sample, sample, s2);
+            }
+        } else {  // two paths at a time, in path order
+            for (int j = 0; j < kPathsPerThread; j += 2) {
+                const uint64_t path = base + static_cast<uint64_t>(j * kSlabThreads) + threadIdx.x;
+                if (path >= c.path_count) break;
+                const uint64_t path2 = path + kSlabThreads;
+                double out[2];
+                if (path2 < c.path_count) {
+                    const PhiloxPath pps[2] = {philox_path(path, 0u, k), philox_path(path2, 0u, k)};
+                    const bool negs[2] = {false, false};
+                    path_dependent32<KIND, 2>(c, k, pps, negs, out);
+                } else {
+                    const PhiloxPath pps[1] = {philox_path(path, 0u, k)};
+                    const bool negs[1] = {false};
+                    double one[1];
+                    path_dependent32<KIND, 1>(c, k, pps, negs, one);
+                    out[0] = one[0];
+                }
+                const int n_here = path2 < c.path_count ? 2 : 1;
+                for (int p = 0; p < n_here; ++p) {
+                    ++count;
+                    s1 += out[p];
+                    s2 = fma(out[p], out[p], s2);
+                }
+            }
+        }
+        return welford_from_sums(count, s1, s2);
+    }
     for (int j = 0; j < kPathsPerThread; ++j) {
         const uint64_t path = base + static_cast<uint64_t>(j * kSlabThreads) + threadIdx.x;
         if (path >= c.path_count) break;
