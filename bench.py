@@ -395,6 +395,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--launch-shape", metavar="VARIANT,CTAS_PER_SM",
+                    help="use this launch shape of the path kernel instead of autotuning")
     ap.add_argument("--case", choices=PROFILE_CASES,
                     help="run one small profiling workload (see run_case) instead of the benchmark")
     ap.add_argument("--no-extra", action="store_true",
@@ -428,7 +430,11 @@ def main():
     # Autotune the launch shape on a cost-stratified subset.
     order = np.argsort(c["monitoring_points"] * c["path_count"].astype(np.float64))
     tune = c[order[::16]]
-    if args.no_tune:
+    if args.launch_shape:
+        v, cps = (int(x) for x in args.launch_shape.split(","))
+        eng.set_launch_shape("fp32", v, cps)
+        variant, ctas = eng.launch_shape("fp32")
+    elif args.no_tune:
         variant, ctas = eng.launch_shape("fp32")
     else:
         variant, ctas, _ = eng.autotune(tune, "fp32")
@@ -506,8 +512,9 @@ def main():
     # Roofline of the persistent path kernel.  It is ALU-bound (no path data in
     # memory), so the bound is instruction issue: 4 SMSPs x 1 warp-instruction
     # per clock per SM.  Instructions per path-step are measured by ncu on the
-    # same kernel (profiles/path_kernel_fp32_batch.md: 1.6964e10 warp
-    # instructions for 6.807e9 path-steps = 79.7 thread-instructions each).
+    # same kernel without register spills (profiles/path_kernel_fp32_batch.md:
+    # 1.5677e10 warp instructions for 6.807e9 path-steps = 73.7 thread-instructions
+    # each; the spilling variants issue ~1 % more).
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -517,19 +524,20 @@ def main():
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     clk = clocks.summary()
     mhz = clk["sm_mhz"] or peaks.get("sm_max_mhz", 2070.0)
-    inst_per_step = 79.7
+    inst_per_step = 73.7
     achieved = total_steps * inst_per_step / 32.0 / (kernel_ms / 1e3) / 1e12
     peak = sm_count * 4 * mhz * 1e6 / 1e12
     line["roofline"] = {
         "bound": "alu", "achieved": achieved, "peak": peak, "unit": "Twarp-inst/s",
         "frac": achieved / peak,
-        # DRAM bytes of the 256-contract ncu capture (127,744 B) scaled by contracts
-        # (the kernel reads contract records and writes slab partials only).
-        "traffic": 127744.0 * n / 256.0,
+        # DRAM bytes of the 256-contract ncu capture at the tuned launch shape
+        # (2,798,336 B: contract records, slab partials and register spills of the
+        # 32-register variant), scaled by contracts.
+        "traffic": 2798336.0 * n / 256.0,
         "kernel_ms": kernel_ms, "launches": launches,
         "path_steps_per_second_kernel": total_steps / (kernel_ms / 1e3),
         "note": "issue-slot roofline (4 warp-inst/clk/SM at the sampled SM clock); "
-                "79.7 thread-instructions per path-step measured by ncu; "
+                "73.7 thread-instructions per path-step measured by ncu; "
                 "no HBM or tensor-core bound applies to this kernel"}
     line["clocks"] = clk
 

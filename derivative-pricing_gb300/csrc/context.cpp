@@ -481,7 +481,7 @@ int mcd_batch_invalidate(mcd_ctx* handle) {
 int mcd_set_launch_shape(mcd_ctx* handle, int precision, int variant, int ctas_per_sm) {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "bad precision");
-    if (variant < 0 || variant >= kNumVariants) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "variant must be 0..3");
+    if (variant < 0 || variant >= kNumVariants) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "variant must be 0..4");
     if (ctas_per_sm < 0 || ctas_per_sm > 64) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "ctas_per_sm must be 0..64");
     ctx->shape[precision].variant = variant;
     ctx->shape[precision].ctas_per_sm = ctas_per_sm;

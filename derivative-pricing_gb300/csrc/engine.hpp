@@ -17,7 +17,7 @@ struct Welford {
 constexpr int kSlabPaths = 4096;       // MCD_SLAB_PATHS
 constexpr int kSlabThreads = 128;      // one CTA = one slab lane group
 constexpr int kPathsPerThread = kSlabPaths / kSlabThreads;
-constexpr int kNumVariants = 4;        // __launch_bounds__ min-blocks 4, 8, 12, 16
+constexpr int kNumVariants = 5;        // __launch_bounds__ min-blocks 4, 8, 12, 16, 6
 
 // Internal product kinds: one loop body per kind (the switch is outside the
 // step loop and uniform over a CTA).

@@ -479,7 +479,8 @@ cudaError_t launch_prec(int variant, int grid, const DevContract* c, int n, cons
         case 0: return launch_one<PREC, 4>(grid, c, n, prefix, total, ticket, partials, err, stream);
         case 1: return launch_one<PREC, 8>(grid, c, n, prefix, total, ticket, partials, err, stream);
         case 2: return launch_one<PREC, 12>(grid, c, n, prefix, total, ticket, partials, err, stream);
-        default: return launch_one<PREC, 16>(grid, c, n, prefix, total, ticket, partials, err, stream);
+        case 3: return launch_one<PREC, 16>(grid, c, n, prefix, total, ticket, partials, err, stream);
+        default: return launch_one<PREC, 6>(grid, c, n, prefix, total, ticket, partials, err, stream);
     }
 }
 
@@ -489,7 +490,8 @@ cudaError_t occupancy_prec(int variant, int* blocks) {
         case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, path_kernel<PREC, 4>, kSlabThreads, 0);
         case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, path_kernel<PREC, 8>, kSlabThreads, 0);
         case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, path_kernel<PREC, 12>, kSlabThreads, 0);
-        default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, path_kernel<PREC, 16>, kSlabThreads, 0);
+        case 3: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, path_kernel<PREC, 16>, kSlabThreads, 0);
+        default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, path_kernel<PREC, 6>, kSlabThreads, 0);
     }
 }
 

@@ -190,8 +190,8 @@ int mcd_price_batch_static(const mcd_contract* contracts, size_t n, int precisio
                            mcd_mc_result* results, void* stream, char* error_message,
                            size_t error_capacity);
 
-/* Launch shape of the persistent path kernel.  variant 0..3 selects the
- * register budget (__launch_bounds__ min blocks 4/8/12/16), ctas_per_sm the
+/* Launch shape of the persistent path kernel.  variant 0..4 selects the
+ * register budget (__launch_bounds__ min blocks 4/8/12/16/6), ctas_per_sm the
  * grid (SM count x ctas_per_sm).  0 restores the autotuned/default choice.
  * Results do not depend on either. */
 int mcd_set_launch_shape(mcd_ctx* ctx, int precision, int variant, int ctas_per_sm);

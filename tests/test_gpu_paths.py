@@ -191,7 +191,7 @@ def test_bitwise_identical_across_launch_shapes(engine, gpu_lib, precision):
     saved = engine.launch_shape(precision)
     outs = []
     try:
-        for variant, ctas in [(0, 1), (1, 0), (2, 3), (3, 0), (1, 16), (0, 7)]:
+        for variant, ctas in [(0, 1), (1, 0), (2, 3), (3, 0), (4, 5), (1, 16), (0, 7)]:
             engine.set_launch_shape(precision, variant, ctas)
             outs.append(engine.price_batch(c, precision).tobytes())
     finally:
