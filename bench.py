@@ -318,7 +318,7 @@ def run_case(case):
       path      256 contracts of the batch configuration (FP32)
       greeks    64 Asian/barrier contracts, 252 steps, 2^16 paths (FP32)
       qmc       256 contracts of the batch configuration under Sobol + bridge
-      heston    8 parameter sets x 64 strikes, 252 steps, 2^18 paths
+      heston    32 parameter sets x 64 strikes, 252 steps, 2^18 paths (8192 items: fills the GPU)
       lsm       4 puts of the American grid (2^20 paths, 50 dates), FP32 QR
       lsm_grid  the 20-put grid, FP32 QR
       mlp       4 puts of the grid, learned regression
@@ -337,7 +337,7 @@ def run_case(case):
             r = eng.qmc_batch(make_batch(256), "fp32")["price"]
         elif case == "heston":
             rng = np.random.default_rng(1)
-            n = 8
+            n = 32
             sets = np.zeros(n, dtype=M.HESTON_DTYPE)
             sets["spot"], sets["rate"], sets["time"] = 100.0, 0.03, 1.0
             sets["kappa"] = rng.uniform(0.5, 3.0, n)

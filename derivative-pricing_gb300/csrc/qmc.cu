@@ -24,6 +24,8 @@
 // nvcc-flags: --fmad=false
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "device_common.cuh"
 #include "engine.hpp"
 #include "qmc.hpp"
@@ -65,41 +67,67 @@ struct SobolLane {
 
 constexpr int kSxStride = kSobolDims + 1;  // +1 word: the last lane's row sits in another bank
 
-struct QmcTables {
+// Bridge coefficients of one contract in program order, FP64 kernel.
+struct QmcTables64 {
     BridgeNode node[kSobolDims];
     double a[kSobolDims], sd[kSobolDims], drift[kSobolDims];
-    float af[kSobolDims], sdf[kSobolDims], driftf[kSobolDims];  // FP32 copies (no conversion per path-step)
 };
+
+// FP32 kernel: one 16-byte record per node, read with one shared-memory load
+// (the same address across the warp): the FP32 coefficients and the node's
+// Sobol dimension and slots packed into the last word.
+struct QmcTables32 {
+    float4 node[kSobolDims];  // {a, sd, drift, bits(meta)}
+};
+constexpr uint32_t kMetaRoot = 1u << 20;  // the terminal point (no ancestors)
+__device__ __forceinline__ uint32_t meta_dim(uint32_t m) { return m & 0xFFu; }
+__device__ __forceinline__ uint32_t meta_left(uint32_t m) { return (m >> 8) & 0xFu; }
+__device__ __forceinline__ uint32_t meta_right(uint32_t m) { return (m >> 12) & 0xFu; }
+__device__ __forceinline__ uint32_t meta_out(uint32_t m) { return (m >> 16) & 0xFu; }
+
+template <int PREC>
+using QmcTables = typename std::conditional<PREC == 0, QmcTables64, QmcTables32>::type;
 
 // Bridge coefficients of one contract in program order, with the reference's
 // operations (brownian_bridge_path.cpp:29-31, :52-62, :71-74): t_i = i T / n.
+template <int PREC>
 __device__ void fill_tables(const DevContract& c, const DevQmc& q, const BridgeNode* __restrict__ programs,
-                            QmcTables& S) {
+                            QmcTables<PREC>& S) {
     const int n = c.n_steps;
     const double nd = static_cast<double>(n);
     auto t_of = [&](int i) { return static_cast<double>(i) * q.time / nd; };
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const BridgeNode b = programs[q.prog_offset + e];
-        S.node[e] = b;
         const double tm = t_of(b.t_mid + 1);
-        if (b.t_left < 0 && b.t_right < 0) {
-            S.a[e] = 0.0;
-            S.sd[e] = sqrt(t_of(n));
+        const bool root = b.t_left < 0 && b.t_right < 0;
+        double a, sd;
+        if (root) {
+            a = 0.0;
+            sd = sqrt(t_of(n));
         } else {
             const double tl = b.t_left < 0 ? 0.0 : t_of(b.t_left + 1);
             const double tr = t_of(b.t_right + 1);
-            S.a[e] = (tm - tl) / (tr - tl);
-            S.sd[e] = sqrt((tm - tl) * (tr - tm) / (tr - tl));
+            a = (tm - tl) / (tr - tl);
+            sd = sqrt((tm - tl) * (tr - tm) / (tr - tl));
         }
-        S.drift[e] = q.drift_rate * tm;
-        S.af[e] = static_cast<float>(S.a[e]);
-        S.sdf[e] = static_cast<float>(S.sd[e]);
-        S.driftf[e] = static_cast<float>(S.drift[e]);
+        const double drift = q.drift_rate * tm;
+        if constexpr (PREC == 0) {
+            S.node[e] = b;
+            S.a[e] = a;
+            S.sd[e] = sd;
+            S.drift[e] = drift;
+        } else {
+            const uint32_t meta = static_cast<uint32_t>(b.dim) | (static_cast<uint32_t>(b.slot_left) << 8) |
+                                  (static_cast<uint32_t>(b.slot_right) << 12) |
+                                  (static_cast<uint32_t>(b.slot_out) << 16) | (root ? kMetaRoot : 0u);
+            S.node[e] = make_float4(static_cast<float>(a), static_cast<float>(sd), static_cast<float>(drift),
+                                    __uint_as_float(meta));
+        }
     }
 }
 
 template <int KIND>
-__device__ double sample_qmc64(const DevContract& c, const DevQmc& q, const QmcTables& S, const SobolLane& sob) {
+__device__ double sample_qmc64(const DevContract& c, const DevQmc& q, const QmcTables64& S, const SobolLane& sob) {
     const double phi = c.type == 0 ? 1.0 : -1.0;
     if constexpr (KIND == kEuropean || KIND == kDigital) {  // qmc.cpp:20-27
         const double z = inv_normal_cdf_f64(static_cast<double>(sob(0u)) * (1.0 / 4294967296.0));
@@ -157,9 +185,13 @@ __device__ double sample_qmc64(const DevContract& c, const DevQmc& q, const QmcT
     }
 }
 
-// FP32: log-space spots x = ln(S/S0), FP32 payoff, FP64 accumulation.
+// FP32: log-space spots x = ln(S/S0), FP32 payoff, FP64 accumulation.  The
+// bridge values live in shared memory, one column per thread (w[slot * 128]):
+// a node's slots are known only at run time, so a register array would be
+// spilled to local memory.
 template <int KIND>
-__device__ double sample_qmc32(const DevContract& c, const DevQmc& q, const QmcTables& S, const SobolLane& sob) {
+__device__ double sample_qmc32(const DevContract& c, const DevQmc& q, const QmcTables32& S, const SobolLane& sob,
+                               float* __restrict__ w) {
     const float phi = c.type == 0 ? 1.0f : -1.0f;
     const float s0 = static_cast<float>(c.spot);
     const float strike = static_cast<float>(c.strike);
@@ -178,24 +210,24 @@ __device__ double sample_qmc32(const DevContract& c, const DevQmc& q, const QmcT
         const int n = c.n_steps;
         const float vol = static_cast<float>(q.vol);
         const float lnh = static_cast<float>(c.log_h_rel);
-        float w[kBridgeSlots];
         w[0] = 0.0f;
         float acc = 0.0f, acc2 = 0.0f, xlast = 0.0f, xmax = 0.0f, xmin = 0.0f;
         bool breached = false;
         for (int e = 0; e < n; ++e) {
-            const BridgeNode& b = S.node[e];
-            const float z = normal_from_sobol_f32(sob(b.dim));
-            const float sd = S.sdf[e];
+            const float4 nd = S.node[e];
+            const uint32_t meta = __float_as_uint(nd.w);
+            const float z = normal_from_sobol_f32(sob(meta_dim(meta)));
             float val;
-            if (b.t_left < 0 && b.t_right < 0) {
-                val = sd * z;
+            const bool root = (meta & kMetaRoot) != 0u;
+            if (root) {
+                val = nd.y * z;
             } else {
-                const float wl = w[b.slot_left], wr = w[b.slot_right];
-                val = __fmaf_rn(sd, z, __fmaf_rn(S.af[e], wr - wl, wl));
+                const float wl = w[meta_left(meta) * kSlabThreads], wr = w[meta_right(meta) * kSlabThreads];
+                val = __fmaf_rn(nd.y, z, __fmaf_rn(nd.x, wr - wl, wl));
             }
-            w[b.slot_out] = val;
-            const float x = __fmaf_rn(vol, val, S.driftf[e]);
-            if (b.t_mid == n - 1) xlast = x;
+            w[meta_out(meta) * kSlabThreads] = val;
+            const float x = __fmaf_rn(vol, val, nd.z);
+            if (root) xlast = x;  // the terminal point is the bridge's root
             if constexpr (KIND == kAsianArith) {
                 acc += __expf(x);
             } else if constexpr (KIND == kAsianGeo) {
@@ -229,9 +261,9 @@ __device__ double sample_qmc32(const DevContract& c, const DevQmc& q, const QmcT
 }
 
 template <int PREC, int KIND>
-__device__ Welford slab_qmc(const DevContract& c, const DevQmc& q, const QmcTables& S,
+__device__ Welford slab_qmc(const DevContract& c, const DevQmc& q, const QmcTables<PREC>& S,
                             const uint32_t* __restrict__ dirs, const uint32_t* __restrict__ ytab, uint32_t* sx,
-                            uint64_t base) {
+                            float* bridge_w, uint64_t base) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t ndims = (KIND == kEuropean || KIND == kDigital) ? 1u : static_cast<uint32_t>(c.n_steps);
     uint32_t* xw = sx + warp * 2 * kSxStride;
@@ -256,7 +288,7 @@ __device__ Welford slab_qmc(const DevContract& c, const DevQmc& q, const QmcTabl
         if constexpr (PREC == 0) {
             welford_add(w, sample_qmc64<KIND>(c, q, S, sob));
         } else {
-            const double v = sample_qmc32<KIND>(c, q, S, sob);
+            const double v = sample_qmc32<KIND>(c, q, S, sob, bridge_w + threadIdx.x);
             ++count;
             s1 += v;
             s2 = fma(v, v, s2);
@@ -267,17 +299,17 @@ __device__ Welford slab_qmc(const DevContract& c, const DevQmc& q, const QmcTabl
 }
 
 template <int PREC>
-__device__ Welford run_qmc_slab(const DevContract& c, const DevQmc& q, const QmcTables& S,
+__device__ Welford run_qmc_slab(const DevContract& c, const DevQmc& q, const QmcTables<PREC>& S,
                                 const uint32_t* __restrict__ dirs, const uint32_t* __restrict__ ytab, uint32_t* sx,
-                                uint64_t base) {
+                                float* bridge_w, uint64_t base) {
     switch (c.kind) {
-        case kEuropean: return slab_qmc<PREC, kEuropean>(c, q, S, dirs, ytab, sx, base);
-        case kDigital: return slab_qmc<PREC, kDigital>(c, q, S, dirs, ytab, sx, base);
-        case kAsianArith: return slab_qmc<PREC, kAsianArith>(c, q, S, dirs, ytab, sx, base);
-        case kAsianGeo: return slab_qmc<PREC, kAsianGeo>(c, q, S, dirs, ytab, sx, base);
-        case kBarrier: return slab_qmc<PREC, kBarrier>(c, q, S, dirs, ytab, sx, base);
-        case kLookbackFixed: return slab_qmc<PREC, kLookbackFixed>(c, q, S, dirs, ytab, sx, base);
-        default: return slab_qmc<PREC, kLookbackFloating>(c, q, S, dirs, ytab, sx, base);
+        case kEuropean: return slab_qmc<PREC, kEuropean>(c, q, S, dirs, ytab, sx, bridge_w, base);
+        case kDigital: return slab_qmc<PREC, kDigital>(c, q, S, dirs, ytab, sx, bridge_w, base);
+        case kAsianArith: return slab_qmc<PREC, kAsianArith>(c, q, S, dirs, ytab, sx, bridge_w, base);
+        case kAsianGeo: return slab_qmc<PREC, kAsianGeo>(c, q, S, dirs, ytab, sx, bridge_w, base);
+        case kBarrier: return slab_qmc<PREC, kBarrier>(c, q, S, dirs, ytab, sx, bridge_w, base);
+        case kLookbackFixed: return slab_qmc<PREC, kLookbackFixed>(c, q, S, dirs, ytab, sx, bridge_w, base);
+        default: return slab_qmc<PREC, kLookbackFloating>(c, q, S, dirs, ytab, sx, bridge_w, base);
     }
 }
 
@@ -293,7 +325,8 @@ __global__ void __launch_bounds__(kSlabThreads)
     __shared__ Welford s_warp[kSlabThreads / 32];
     __shared__ DevContract s_c;
     __shared__ DevQmc s_q;
-    __shared__ QmcTables S;
+    __shared__ QmcTables<PREC> S;
+    __shared__ float s_bridge[PREC == 0 ? 1 : kBridgeSlots * kSlabThreads];  // FP32 bridge values, per thread
     __shared__ int s_loaded;  // sorted index of the contract whose tables are in S
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -322,7 +355,7 @@ __global__ void __launch_bounds__(kSlabThreads)
                     if (threadIdx.x == 0) atomicOr(error_flag, 2u);
                     continue;
                 }
-                fill_tables(s_c, s_q, programs, S);
+                fill_tables<PREC>(s_c, s_q, programs, S);
             }
             if (threadIdx.x == 0) s_loaded = lo;
             __syncthreads();
@@ -332,7 +365,7 @@ __global__ void __launch_bounds__(kSlabThreads)
             if (threadIdx.x == 0) atomicOr(error_flag, 1u);
             continue;
         }
-        Welford w = run_qmc_slab<PREC>(s_c, s_q, S, dirs, ytab, s_sx, static_cast<uint64_t>(slab) * kSlabPaths);
+        Welford w = run_qmc_slab<PREC>(s_c, s_q, S, dirs, ytab, s_sx, s_bridge, static_cast<uint64_t>(slab) * kSlabPaths);
         w = welford_warp_reduce(w);
         if (lane == 0) s_warp[warp] = w;
         __syncthreads();
