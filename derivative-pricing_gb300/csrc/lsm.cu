@@ -1,8 +1,9 @@
 // lsm.cu -- batched Longstaff-Schwartz American pricing (QR regression).
 //
-// Reference: monte_carlo_lsm_american (src/pricers/lsm.cpp:62-149) and
-// reprice_against_frozen_policy (:151-213): forward-simulated GBM paths, cash
-// flows seeded with the terminal intrinsic, backward over dates n-1..1 (discount
+// Reference: monte_carlo_lsm_american (src/pricers/lsm.cpp:62-149; the frozen
+// replay of :151-213 is the streaming kernel of lsm_frozen.cu): forward-simulated
+// GBM paths, cash flows seeded with the terminal intrinsic, backward over dates
+// n-1..1 (discount
 // the cash flows, regress them on the weighted Laguerre basis of S/K over the
 // in-the-money paths -- skipped below 4 such paths --, exercise where
 // intrinsic > continuation), a final discount, Welford, and the inception check.
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(kLsmThreads)
 // ---------------------------------------------------------------------------
 template <int PREC>
 __global__ void __launch_bounds__(kLsmThreads)
-    lsm_exercise(int k, int frozen, const LsmDev* __restrict__ cs,
+    lsm_exercise(int k, const LsmDev* __restrict__ cs,
                  const uint32_t* __restrict__ chunk_contract, uint32_t total_chunks,
                  const void* __restrict__ store, double* __restrict__ cf,
                  const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_a,
@@ -228,7 +229,7 @@ __global__ void __launch_bounds__(kLsmThreads)
     if (e < 1) return;  // this contract has finished (uniform per CTA)
     const bool init = (k == 0);
     const bool last = (e == 1);
-    const bool gram = !frozen && !last;
+    const bool gram = !last;
     const LsmReg* re = (!init && e <= n - 1) ? &reg[c.reg_offset + e] : nullptr;
     const bool exercise = re != nullptr && re->has == 1;
     double g0 = 0, g1 = 0, g2 = 0, g3 = 0;
@@ -687,32 +688,27 @@ cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
     return cudaGetLastError();
 }
 
-cudaError_t launch_lsm_iteration(int precision, int k, bool frozen, const LsmDev* c,
-                                 int n_contracts, const uint32_t* chunk_contract,
-                                 uint32_t total_chunks, const void* s_store, double* cf,
-                                 LsmReg* reg, LsmPartial* part_a, LsmPartial* part_b,
+cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_contracts,
+                                 const uint32_t* chunk_contract, uint32_t total_chunks, const void* s_store,
+                                 double* cf, LsmReg* reg, LsmPartial* part_a, LsmPartial* part_b,
                                  Welford* final_part, cudaStream_t stream) {
     cudaGetLastError();
     if (total_chunks == 0) return cudaSuccess;
     const int solve_blocks = (n_contracts * 32 + 127) / 128;
     if (precision == 0)
-        lsm_exercise<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, frozen ? 1 : 0, c, chunk_contract,
-                                                                  total_chunks, s_store, cf, reg,
-                                                                  part_a, final_part);
+        lsm_exercise<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
+                                                                  reg, part_a, final_part);
     else
-        lsm_exercise<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, frozen ? 1 : 0, c, chunk_contract,
-                                                                  total_chunks, s_store, cf, reg,
-                                                                  part_a, final_part);
-    if (!frozen) {
-        lsm_solve_a<<<solve_blocks, 128, 0, stream>>>(k, c, n_contracts, part_a, reg);
-        if (precision == 0)
-            lsm_gram_b<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks,
-                                                                    s_store, cf, reg, part_b);
-        else
-            lsm_gram_b<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks,
-                                                                    s_store, cf, reg, part_b);
-        lsm_solve_b<<<solve_blocks, 128, 0, stream>>>(k, c, n_contracts, part_b, reg);
-    }
+        lsm_exercise<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
+                                                                  reg, part_a, final_part);
+    lsm_solve_a<<<solve_blocks, 128, 0, stream>>>(k, c, n_contracts, part_a, reg);
+    if (precision == 0)
+        lsm_gram_b<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf, reg,
+                                                                part_b);
+    else
+        lsm_gram_b<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf, reg,
+                                                                part_b);
+    lsm_solve_b<<<solve_blocks, 128, 0, stream>>>(k, c, n_contracts, part_b, reg);
     return cudaGetLastError();
 }
 

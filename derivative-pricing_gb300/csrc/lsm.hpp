@@ -71,10 +71,9 @@ struct FrozenDev {
 cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
                                const uint32_t* chunk_contract, uint32_t total_chunks, void* s_store,
                                cudaStream_t stream);
-cudaError_t launch_lsm_iteration(int precision, int k, bool frozen, const LsmDev* c,
-                                 int n_contracts, const uint32_t* chunk_contract,
-                                 uint32_t total_chunks, const void* s_store, double* cf,
-                                 LsmReg* reg, LsmPartial* part_a, LsmPartial* part_b,
+cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_contracts,
+                                 const uint32_t* chunk_contract, uint32_t total_chunks, const void* s_store,
+                                 double* cf, LsmReg* reg, LsmPartial* part_a, LsmPartial* part_b,
                                  Welford* final_part, cudaStream_t stream);
 cudaError_t launch_lsm_finish(const LsmDev* c, int n_contracts, const Welford* final_part,
                               double* out /* n x 6: price, se, count, inception, mean, se */,

@@ -177,7 +177,7 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
                                           static_cast<Welford*>(ctx.ext[kFinal].ptr),
                                           static_cast<uint32_t*>(ctx.ext[kErr].ptr), ctx.stream);
         else
-            le = launch_lsm_iteration(precision, k, frozen, d_dev, static_cast<int>(n), d_map, p.total_chunks,
+            le = launch_lsm_iteration(precision, k, d_dev, static_cast<int>(n), d_map, p.total_chunks,
                                       ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
                                       static_cast<LsmReg*>(ctx.ext[kReg].ptr),
                                       static_cast<LsmPartial*>(ctx.ext[kPartA].ptr),
