@@ -196,7 +196,24 @@ __global__ void __launch_bounds__(kLsmThreads)
                 S[static_cast<uint64_t>(d) * c.path_count + i] = s;
             }
         } else {
+            // two paths per iteration when both exist: independent Philox
+            // chains for instruction-level parallelism, the same values
             float* S = static_cast<float*>(store) + c.s_offset;
+            const uint64_t i2 = i + kLsmThreads;
+            if ((j & 1) == 0 && j + 1 < kLsmChunk / kLsmThreads && i2 < c.path_count) {
+                const PhiloxPath pp2 = philox_path(i2, 0u, k);
+                float x = 0.0f, x2 = 0.0f;
+                for (int d = 0; d < c.n_steps; ++d) {
+                    const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(d), k));
+                    const float z2 = normal_from_bits_f32(philox_word0(pp2, static_cast<uint32_t>(d), k));
+                    x = __fmaf_rn(sg, z, x + mu);
+                    x2 = __fmaf_rn(sg, z2, x2 + mu);
+                    S[static_cast<uint64_t>(d) * c.path_count + i] = s0 * __expf(x);
+                    S[static_cast<uint64_t>(d) * c.path_count + i2] = s0 * __expf(x2);
+                }
+                ++j;  // the partner path is done
+                continue;
+            }
             float x = 0.0f;
             for (int d = 0; d < c.n_steps; ++d) {
                 const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(d), k));
