@@ -88,14 +88,16 @@ struct KahanF {
     }
 };
 
+// FP32: two paths per thread in flight, so a larger register budget (6 CTAs
+// of 128 threads per SM) than the FP64 kernel's (8).
 template <int PREC>
-__global__ void __launch_bounds__(128, 8)
+__global__ void __launch_bounds__(128, PREC == 1 ? 6 : 8)
     heston_kernel(const HestonSet* __restrict__ sets, int n_sets, const double* __restrict__ strikes,
                   int n_strikes, int type, uint32_t items_per_set, uint32_t total_items,
                   uint32_t* __restrict__ ticket, Welford* __restrict__ partials) {
     __shared__ uint32_t s_item;
     __shared__ double s_terminal64[128];
-    __shared__ float s_terminal32[128];
+    __shared__ float s_terminal32[128], s_terminal32b[128];
     __shared__ Welford s_acc[256];
     __shared__ HestonSet s_set;
     const int t = threadIdx.x;
@@ -125,13 +127,12 @@ __global__ void __launch_bounds__(128, 8)
         double a0 = 0.0, q0 = 0.0, a1 = 0.0, q1 = 0.0;
         HestonSet32 h32;
         if (PREC == 1) h32 = make_set32(h);
-        for (int j = 0; j < 32; ++j) {
-            const uint64_t path = static_cast<uint64_t>(slab) * 4096 + static_cast<uint64_t>(j * 128 + t);
-            const bool live = path < h.path_count;
-            if (live) {
-                const PhiloxPath ps = philox_path(path, 0u, k);
-                const PhiloxPath pv = philox_path(path, 1u, k);
-                if (PREC == 0) {
+        if constexpr (PREC == 0) {
+            for (int j = 0; j < 32; ++j) {
+                const uint64_t path = static_cast<uint64_t>(slab) * 4096 + static_cast<uint64_t>(j * 128 + t);
+                if (path < h.path_count) {
+                    const PhiloxPath ps = philox_path(path, 0u, k);
+                    const PhiloxPath pv = philox_path(path, 1u, k);
                     double v = h.v0;
                     double log_s = h.log_s0;
                     for (int step = 0; step < h.n_steps; ++step) {
@@ -143,39 +144,34 @@ __global__ void __launch_bounds__(128, 8)
                         v = v_next;
                     }
                     s_terminal64[t] = exp(log_s);
-                } else {
-                    float v = h32.v0;
-                    float x = 0.0f;  // ln(S/S0)
-                    for (int step = 0; step < h.n_steps; ++step) {
-                        const uint32_t d = static_cast<uint32_t>(step);
-                        const float z_s = normal_from_bits_f32(philox_word0(ps, d, k));
-                        const float v_next = qe_step32(v, h32, philox_word0(pv, d, k));
-                        const float dv = fmaxf(__fmaf_rn(h32.k3, v, h32.k4 * v_next), 0.0f);
-                        const float incr = __fmaf_rn(h32.k1, v, __fmaf_rn(h32.k2, v_next, h32.c0));
-                        x = __fmaf_rn(fast_sqrt(dv), z_s, x + incr);
-                        v = v_next;
-                    }
-                    s_terminal32[t] = h32.s0 * __expf(x);
                 }
-            }
-            __syncthreads();
-            // Pay out the round's paths (paths of this round beyond path_count are skipped).
-            const uint64_t round_base = static_cast<uint64_t>(slab) * 4096 + static_cast<uint64_t>(j * 128);
-            const uint64_t left = round_base >= h.path_count ? 0 : h.path_count - round_base;
-            const int round_live = left > 128 ? 128 : static_cast<int>(left);
-            if (PREC == 0) {
+                __syncthreads();
+                // Pay out the round's paths (paths of this round beyond path_count are skipped).
+                const uint64_t round_base = static_cast<uint64_t>(slab) * 4096 + static_cast<uint64_t>(j * 128);
+                const uint64_t left = round_base >= h.path_count ? 0 : h.path_count - round_base;
+                const int round_live = left > 128 ? 128 : static_cast<int>(left);
                 for (int p = my_group; p < round_live; p += groups) {
                     const double s_t = s_terminal64[p];
                     if (serves0) welford_add(w0, h.discount * dmax(phi * (s_t - strike0), 0.0));
                     if (serves1) welford_add(w1, h.discount * dmax(phi * (s_t - strike1), 0.0));
                 }
-            } else {
-                const float fphi = static_cast<float>(phi);
-                const float fk0 = static_cast<float>(strike0), fk1 = static_cast<float>(strike1);
+                __syncthreads();
+            }
+        } else {
+            // Two rounds per pass: each thread simulates the paths of rounds j
+            // and j + 1 together (independent dependency chains), then both
+            // rounds are paid out in order, so the sums are those of one round
+            // at a time.
+            const float fphi = static_cast<float>(phi);
+            const float fk0 = static_cast<float>(strike0), fk1 = static_cast<float>(strike1);
+            auto payout = [&](int j, const float* terminal) {
+                const uint64_t round_base = static_cast<uint64_t>(slab) * 4096 + static_cast<uint64_t>(j * 128);
+                const uint64_t left = round_base >= h.path_count ? 0 : h.path_count - round_base;
+                const int round_live = left > 128 ? 128 : static_cast<int>(left);
                 KahanF s0a, s0b, s1a, s1b;
                 unsigned n_here = 0;
                 for (int p = my_group; p < round_live; p += groups) {
-                    const float s_t = s_terminal32[p];
+                    const float s_t = terminal[p];
                     const float y0 = fmaxf(fphi * (s_t - fk0), 0.0f);
                     s0a.add(y0);
                     s0b.add(y0 * y0);
@@ -196,8 +192,39 @@ __global__ void __launch_bounds__(128, 8)
                     a1 += static_cast<double>(s1a.s) + static_cast<double>(-s1a.c);
                     q1 += static_cast<double>(s1b.s) + static_cast<double>(-s1b.c);
                 }
+            };
+            for (int j = 0; j < 32; j += 2) {
+                const uint64_t path_a = static_cast<uint64_t>(slab) * 4096 + static_cast<uint64_t>(j * 128 + t);
+                const uint64_t path_b = path_a + 128;
+                if (path_a < h.path_count) {  // path_b exists only if path_a does
+                    const bool live_b = path_b < h.path_count;
+                    const PhiloxPath psa = philox_path(path_a, 0u, k), pva = philox_path(path_a, 1u, k);
+                    const PhiloxPath psb = philox_path(path_b, 0u, k), pvb = philox_path(path_b, 1u, k);
+                    float va = h32.v0, vb = h32.v0;
+                    float xa = 0.0f, xb = 0.0f;  // ln(S/S0)
+                    for (int step = 0; step < h.n_steps; ++step) {
+                        const uint32_t d = static_cast<uint32_t>(step);
+                        const float za = normal_from_bits_f32(philox_word0(psa, d, k));
+                        const float zb = normal_from_bits_f32(philox_word0(psb, d, k));
+                        const float va_next = qe_step32(va, h32, philox_word0(pva, d, k));
+                        const float vb_next = qe_step32(vb, h32, philox_word0(pvb, d, k));
+                        const float dva = fmaxf(__fmaf_rn(h32.k3, va, h32.k4 * va_next), 0.0f);
+                        const float dvb = fmaxf(__fmaf_rn(h32.k3, vb, h32.k4 * vb_next), 0.0f);
+                        const float ia = __fmaf_rn(h32.k1, va, __fmaf_rn(h32.k2, va_next, h32.c0));
+                        const float ib = __fmaf_rn(h32.k1, vb, __fmaf_rn(h32.k2, vb_next, h32.c0));
+                        xa = __fmaf_rn(fast_sqrt(dva), za, xa + ia);
+                        xb = __fmaf_rn(fast_sqrt(dvb), zb, xb + ib);
+                        va = va_next;
+                        vb = vb_next;
+                    }
+                    s_terminal32[t] = h32.s0 * __expf(xa);
+                    if (live_b) s_terminal32b[t] = h32.s0 * __expf(xb);
+                }
+                __syncthreads();
+                payout(j, s_terminal32);
+                payout(j + 1, s_terminal32b);
+                __syncthreads();
             }
-            __syncthreads();
         }
         if (PREC == 1) {
             // discount applied once: mean scales by D, M2 by D^2
