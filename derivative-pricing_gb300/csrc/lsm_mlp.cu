@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(128)
 // the cached modes only (no decision network to evaluate).
 // ---------------------------------------------------------------------------
 constexpr int kWideThreads = 256;
-constexpr uint32_t kRing = 512;           // ring slots (two tiles)
+constexpr uint32_t kRing = 2048;          // ring slots: a chunk (1024) plus a partial tile, rounded up
 constexpr int kRingOffset = 10 * 4096;    // byte offset of xt row 80 (core-matrix row group 10)
 
 struct __align__(1024) WideSmem {
@@ -865,42 +865,56 @@ __global__ void __launch_bounds__(kWideThreads, 2)
         q_head = (q_head + n_valid) & (kRing - 1);
         q_len -= n_valid;
     };
+    constexpr int kPer = kLsmChunk / kWideThreads;  // paths per thread and chunk
     for (uint32_t ch = chunk0; ch < chunk1; ++ch) {
-        for (int tile = 0; tile < kLsmChunk / kWideThreads; ++tile) {
-            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + tile * kWideThreads + s;
-            const bool live = i < c.path_count;
-            T v = T(0), ex_e = T(0);
-            if (live) {
-                if (init) {
-                    const T sT = S_path[static_cast<uint64_t>(n - 1) * c.path_count + i];
-                    const T x = phi * (sT - strike);
-                    v = x > T(0) ? x : T(0);
-                } else {
-                    v = cft[i];
-                }
+        // every path load of this thread's kPer paths first (independent, in flight together)
+        T vv[kPer], se[kPer], sd[kPer];
+        bool live[kPer];
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + q * kWideThreads + s;
+            live[q] = i < c.path_count;
+            vv[q] = se[q] = sd[q] = T(0);
+            if (live[q]) {
+                vv[q] = init ? S_path[static_cast<uint64_t>(n - 1) * c.path_count + i] : cft[i];
+                if (exercise) se[q] = S_path[static_cast<uint64_t>(e - 1) * c.path_count + i];
+                if (gram) sd[q] = S_path[static_cast<uint64_t>(e - 2) * c.path_count + i];
             }
-            if (exercise && live) {
-                const T se = S_path[static_cast<uint64_t>(e - 1) * c.path_count + i];
-                const T xx = phi * (se - strike);
-                ex_e = xx > T(0) ? xx : T(0);
+        }
+        bool itm[kPer];
+        float x0[kPer], y[kPer];
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + q * kWideThreads + s;
+            itm[q] = false;
+            x0[q] = y[q] = 0.0f;
+            if (!live[q]) continue;
+            T v = vv[q];
+            if (init) {
+                const T x = phi * (v - strike);
+                v = x > T(0) ? x : T(0);
+            }
+            if (exercise) {
+                const T xx = phi * (se[q] - strike);
+                const T ex_e = xx > T(0) ? xx : T(0);
                 if (ex_e > T(0)) {
                     const uint4* src = feat_cache + (c.cf_offset + i) * 8;
                     float yh = S.pd[sB3];
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        const uint4 u = src[q];
+                    for (int r = 0; r < 8; ++r) {
+                        const uint4 u = src[r];
                         const uint32_t words[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
                         for (int h = 0; h < 4; ++h) {
                             const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&words[h]));
-                            yh = __fmaf_rn(S.pd[sW3 + q * 8 + 2 * h], f.x, yh);
-                            yh = __fmaf_rn(S.pd[sW3 + q * 8 + 2 * h + 1], f.y, yh);
+                            yh = __fmaf_rn(S.pd[sW3 + r * 8 + 2 * h], f.x, yh);
+                            yh = __fmaf_rn(S.pd[sW3 + r * 8 + 2 * h + 1], f.y, yh);
                         }
                     }
                     if (yh < 0.0f) v = ex_e;  // predicted time value < 0: exercise
                 }
             }
-            if (live && step) {
+            if (step) {
                 v *= disc;
                 if (last) {
                     if constexpr (PREC == 0) {
@@ -913,39 +927,49 @@ __global__ void __launch_bounds__(kWideThreads, 2)
                 }
             }
             if (gram) {
-                // the paths in the money at date e-1 join the ring of paths
-                // awaiting a feature tile; the others take no part in the fit
-                bool itm = false;
-                float x0 = 0.0f, y = 0.0f;
-                if (live) {
-                    const T s_d = S_path[static_cast<uint64_t>(e - 2) * c.path_count + i];
-                    const T xx = phi * (s_d - strike);
-                    const T ex_d = xx > T(0) ? xx : T(0);
-                    itm = ex_d > T(0);
-                    if constexpr (PREC == 0) x0 = static_cast<float>(4.0 * (s_d * inv_k - 1.0));
-                    else x0 = 4.0f * (s_d * inv_k - 1.0f);
-                    y = static_cast<float>((v - ex_d) * inv_k);
-                }
-                const unsigned bal = __ballot_sync(0xffffffffu, itm);
-                if ((s & 31) == 0) warp_cnt[warp] = __popc(bal);
-                __syncthreads();
-                uint32_t before = 0, total = 0;
-                for (int wi = 0; wi < kWideThreads / 32; ++wi) {
-                    const uint32_t cw = warp_cnt[wi];
-                    before += wi < warp ? cw : 0u;
-                    total += cw;
-                }
-                if (itm) {
-                    const uint32_t pos =
-                        (q_head + q_len + before + __popc(bal & ((1u << (s & 31)) - 1u))) & (kRing - 1);
-                    q_idx[pos] = static_cast<uint32_t>(i - first_path);
-                    q_x0[pos] = x0;
-                    q_y[pos] = y;
-                }
-                q_len += total;
-                __syncthreads();
-                if (q_len >= static_cast<uint32_t>(kWideThreads)) feature_tile(kWideThreads);
+                const T xx = phi * (sd[q] - strike);
+                const T ex_d = xx > T(0) ? xx : T(0);
+                itm[q] = ex_d > T(0);
+                if constexpr (PREC == 0) x0[q] = static_cast<float>(4.0 * (sd[q] * inv_k - 1.0));
+                else x0[q] = 4.0f * (sd[q] * inv_k - 1.0f);
+                y[q] = static_cast<float>((v - ex_d) * inv_k);
             }
+        }
+        if (gram) {
+            // The chunk's paths in the money at date e-1 join the ring of
+            // paths awaiting a feature tile (the others take no part in the
+            // fit): a block-wide exclusive scan of the per-thread counts.
+            uint32_t mine = 0;
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) mine += itm[q] ? 1u : 0u;
+            uint32_t incl = mine;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+                if ((s & 31) >= off) incl += o;
+            }
+            if ((s & 31) == 31) warp_cnt[warp] = incl;
+            __syncthreads();
+            uint32_t before = incl - mine, total = 0;
+            for (int wi = 0; wi < kWideThreads / 32; ++wi) {
+                const uint32_t cw = warp_cnt[wi];
+                before += wi < warp ? cw : 0u;
+                total += cw;
+            }
+            uint32_t pos = q_head + q_len + before;
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                if (!itm[q]) continue;
+                const uint32_t slot = pos & (kRing - 1);
+                q_idx[slot] = static_cast<uint32_t>(static_cast<uint64_t>(ch) * kLsmChunk + q * kWideThreads + s -
+                                                    first_path);
+                q_x0[slot] = x0[q];
+                q_y[slot] = y[q];
+                ++pos;
+            }
+            q_len += total;
+            __syncthreads();
+            while (q_len >= static_cast<uint32_t>(kWideThreads)) feature_tile(kWideThreads);
         }
         if (last) {  // one final partial per chunk, fixed tree
             if constexpr (PREC == 0) {
