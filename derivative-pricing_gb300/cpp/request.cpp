@@ -587,6 +587,9 @@ extern "C" char* mcd_shim_handle_request(const char* request, int dialect, uint6
         Object err;
         err.emplace_back("error", Value::string(e.what()));
         body = mcdjson::serialize(err);
+    } catch (...) {  // nothing may unwind through the C boundary
+        st = MCD_SHIM_INTERNAL_ERROR;
+        body = "{\"error\":\"internal error\"}";
     }
     if (status) *status = st;
     char* out = static_cast<char*>(std::malloc(body.size() + 1));
