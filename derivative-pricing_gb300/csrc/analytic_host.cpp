@@ -256,22 +256,26 @@ void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
 extern "C" {
 
 double mcd_crr_binomial_american(double spot, double strike, double rate, double carry_yield, double vol,
-                                 double time, int steps, int type) {
+                                 double time, int steps, int type) try {
     if (steps < 1) return std::nan("");
     return lattice(spot, strike, rate, carry_yield, vol, time, steps, type, true, nullptr, nullptr, nullptr);
+} catch (...) {
+    return std::nan("");
 }
 
 int mcd_crr_binomial(double spot, double strike, double rate, double carry_yield, double vol, double time, int steps,
-                     int type, double* price_p_u_d) {
+                     int type, double* price_p_u_d) try {
     if (steps < 1 || !price_p_u_d) return MCD_ERR_INVALID_ARGUMENT;
     price_p_u_d[0] = lattice(spot, strike, rate, carry_yield, vol, time, steps, type, false, &price_p_u_d[1],
                              &price_p_u_d[2], &price_p_u_d[3]);
     return MCD_OK;
+} catch (...) {  // a lattice too large for host memory
+    return MCD_ERR_OUT_OF_MEMORY;
 }
 
 // heston.cpp:48-82: Heston (1993) P1/P2 as integrals over [0, 200] by
 // 128-point Gauss-Legendre; the put from parity.
-double mcd_heston_semi_analytic(const mcd_heston_params* params, double strike, int type) {
+double mcd_heston_semi_analytic(const mcd_heston_params* params, double strike, int type) try {
     if (!params) return std::nan("");
     static const auto rule = [] {
         std::vector<double> x, w;
@@ -295,6 +299,8 @@ double mcd_heston_semi_analytic(const mcd_heston_params* params, double strike, 
     const double dq = std::exp(-p.carry_yield * p.time), dr = std::exp(-p.rate * p.time);
     const double call = p.spot * dq * p1 - strike * dr * p2;
     return type == MCD_CALL ? call : call - p.spot * dq + strike * dr;
+} catch (...) {
+    return std::nan("");
 }
 
 }  // extern "C"

@@ -366,11 +366,31 @@ int price_batch_host(Ctx& ctx, const mcd_contract* contracts, size_t n, int prec
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
+int abi_exception(mcd_ctx* handle) noexcept {
+    int code = MCD_ERR_INVALID_ARGUMENT;
+    const char* msg = "internal error";
+    try {
+        throw;
+    } catch (const std::bad_alloc&) {
+        code = MCD_ERR_OUT_OF_MEMORY;
+        msg = "host out of memory";
+    } catch (const std::exception& e) {
+        msg = e.what();
+    } catch (...) {
+    }
+    try {
+        if (handle) reinterpret_cast<Ctx*>(handle)->error = std::string("internal error: ") + msg;
+        else g_create_error = std::string("internal error: ") + msg;
+    } catch (...) {
+    }
+    return code;
+}
+
 extern "C" {
 
 int mcd_abi_version(void) { return MCD_GPU_ABI_VERSION; }
 
-int mcd_create(int device, mcd_ctx** out) {
+int mcd_create(int device, mcd_ctx** out) try {
     if (!out) {
         g_create_error = "out must not be NULL";
         return MCD_ERR_INVALID_ARGUMENT;
@@ -415,6 +435,8 @@ int mcd_create(int device, mcd_ctx** out) {
     cudaMemset(ctx->d_flags, 0, 64);
     *out = reinterpret_cast<mcd_ctx*>(ctx);
     return MCD_OK;
+} catch (...) {
+    return abi_exception(nullptr);
 }
 
 void mcd_destroy(mcd_ctx* handle) {
@@ -430,23 +452,27 @@ const char* mcd_last_error(const mcd_ctx* handle) {
     return reinterpret_cast<const Ctx*>(handle)->error.c_str();
 }
 
-int mcd_synchronize(mcd_ctx* handle) {
+int mcd_synchronize(mcd_ctx* handle) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "synchronize");
     return collect_after_sync(*ctx);
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_price_batch(mcd_ctx* handle, const mcd_contract* contracts, size_t n, int precision,
-                    mcd_mc_result* results) {
+                    mcd_mc_result* results) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (n > 0 && (!contracts || !results)) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null array");
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
     return price_batch_host(*ctx, contracts, n, precision, results);
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_price_batch_device(mcd_ctx* handle, const mcd_contract* contracts, size_t n, int precision,
-                           mcd_mc_result* results, void* stream) {
+                           mcd_mc_result* results, void* stream) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (n > 0 && (!contracts || !results)) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null array");
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
@@ -470,15 +496,19 @@ int mcd_price_batch_device(mcd_ctx* handle, const mcd_contract* contracts, size_
     int rc = get_graph(*ctx, precision, ctx->device_plan, results, &exec);
     if (rc) return rc;
     return run_graph(*ctx, exec, s);
+} catch (...) {
+    return abi_exception(handle);
 }
 
-int mcd_batch_invalidate(mcd_ctx* handle) {
+int mcd_batch_invalidate(mcd_ctx* handle) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     ctx->device_plan_valid = false;
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
-int mcd_set_launch_shape(mcd_ctx* handle, int precision, int variant, int ctas_per_sm) {
+int mcd_set_launch_shape(mcd_ctx* handle, int precision, int variant, int ctas_per_sm) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "bad precision");
     if (variant < 0 || variant >= kNumVariants) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "variant must be 0..4");
@@ -486,9 +516,11 @@ int mcd_set_launch_shape(mcd_ctx* handle, int precision, int variant, int ctas_p
     ctx->shape[precision].variant = variant;
     ctx->shape[precision].ctas_per_sm = ctas_per_sm;
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
-int mcd_get_launch_shape(mcd_ctx* handle, int precision, int* variant, int* ctas_per_sm) {
+int mcd_get_launch_shape(mcd_ctx* handle, int precision, int* variant, int* ctas_per_sm) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "bad precision");
     int v = 0, grid = 0;
@@ -497,10 +529,12 @@ int mcd_get_launch_shape(mcd_ctx* handle, int precision, int* variant, int* ctas
     if (variant) *variant = v;
     if (ctas_per_sm) *ctas_per_sm = grid / ctx->sm_count;
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_autotune(mcd_ctx* handle, const mcd_contract* contracts, size_t n, int precision,
-                 int* variant_out, int* ctas_out, double* best_ms_out) {
+                 int* variant_out, int* ctas_out, double* best_ms_out) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "bad precision");
     if (n == 0 || !contracts) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "empty tuning batch");
@@ -546,9 +580,11 @@ int mcd_autotune(mcd_ctx* handle, const mcd_contract* contracts, size_t n, int p
     if (ctas_out) *ctas_out = best_shape.ctas_per_sm;
     if (best_ms_out) *best_ms_out = best;
     return collect_after_sync(*ctx);
+} catch (...) {
+    return abi_exception(handle);
 }
 
-int mcd_kernel_timing(mcd_ctx* handle, int reset, double* avg_ms, uint64_t* launches) {
+int mcd_kernel_timing(mcd_ctx* handle, int reset, double* avg_ms, uint64_t* launches) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     ctx->collect_timing(true);
     if (avg_ms) *avg_ms = ctx->kernel_launches ? ctx->kernel_ms_sum / ctx->kernel_launches : 0.0;
@@ -558,6 +594,8 @@ int mcd_kernel_timing(mcd_ctx* handle, int reset, double* avg_ms, uint64_t* laun
         ctx->kernel_launches = 0;
     }
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 // ---- single-contract entry points --------------------------------------------
@@ -595,40 +633,46 @@ static mcd_contract base_contract(int product, double spot, double strike, doubl
 
 int mcd_price_european(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
                        double vol, double time, int type, uint64_t path_count, uint64_t seed,
-                       const mcd_mc_options* options, int precision, mcd_mc_result* out) {
+                       const mcd_mc_options* options, int precision, mcd_mc_result* out) try {
     const mcd_contract c = base_contract(MCD_PRODUCT_EUROPEAN, spot, strike, rate, carry_yield, vol,
                                          time, type, path_count, seed, options);
     return price_one(ctx, c, precision, out);
+} catch (...) {
+    return abi_exception(ctx);
 }
 
 int mcd_price_digital(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
                       double vol, double time, int type, int digital_style, double cash_amount,
                       uint64_t path_count, uint64_t seed, const mcd_mc_options* options,
-                      int precision, mcd_mc_result* out) {
+                      int precision, mcd_mc_result* out) try {
     mcd_contract c = base_contract(MCD_PRODUCT_DIGITAL, spot, strike, rate, carry_yield, vol, time,
                                    type, path_count, seed, options);
     c.digital_style = digital_style;
     c.cash_amount = cash_amount;
     return price_one(ctx, c, precision, out);
+} catch (...) {
+    return abi_exception(ctx);
 }
 
 int mcd_price_asian(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
                     double vol, double time, int type, int strike_style, int average_style,
                     int monitoring_points, uint64_t path_count, uint64_t seed,
-                    const mcd_mc_options* options, int precision, mcd_mc_result* out) {
+                    const mcd_mc_options* options, int precision, mcd_mc_result* out) try {
     mcd_contract c = base_contract(MCD_PRODUCT_ASIAN, spot, strike, rate, carry_yield, vol, time,
                                    type, path_count, seed, options);
     c.strike_style = strike_style;
     c.average_style = average_style;
     c.monitoring_points = monitoring_points;
     return price_one(ctx, c, precision, out);
+} catch (...) {
+    return abi_exception(ctx);
 }
 
 int mcd_price_barrier(mcd_ctx* ctx, double spot, double strike, double barrier, double rate,
                       double carry_yield, double vol, double time, int type, int direction,
                       int knock, double rebate, int monitoring_points, uint64_t path_count,
                       uint64_t seed, const mcd_mc_options* options, int precision,
-                      mcd_mc_result* out) {
+                      mcd_mc_result* out) try {
     mcd_contract c = base_contract(MCD_PRODUCT_BARRIER, spot, strike, rate, carry_yield, vol, time,
                                    type, path_count, seed, options);
     c.barrier = barrier;
@@ -637,22 +681,26 @@ int mcd_price_barrier(mcd_ctx* ctx, double spot, double strike, double barrier, 
     c.rebate = rebate;
     c.monitoring_points = monitoring_points;
     return price_one(ctx, c, precision, out);
+} catch (...) {
+    return abi_exception(ctx);
 }
 
 int mcd_price_lookback(mcd_ctx* ctx, double spot, double strike, double rate, double carry_yield,
                        double vol, double time, int type, int strike_style, int monitoring_points,
                        uint64_t path_count, uint64_t seed, const mcd_mc_options* options,
-                       int precision, mcd_mc_result* out) {
+                       int precision, mcd_mc_result* out) try {
     mcd_contract c = base_contract(MCD_PRODUCT_LOOKBACK, spot, strike, rate, carry_yield, vol, time,
                                    type, path_count, seed, options);
     c.strike_style = strike_style;
     c.monitoring_points = monitoring_points;
     return price_one(ctx, c, precision, out);
+} catch (...) {
+    return abi_exception(ctx);
 }
 
 // ---- draws ---------------------------------------------------------------------
 int mcd_philox(mcd_ctx* handle, const uint32_t* counters, const uint32_t* keys, size_t n,
-               uint32_t* out) {
+               uint32_t* out) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (n == 0) return MCD_OK;
     if (!counters || !keys || !out) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null array");
@@ -674,10 +722,12 @@ int mcd_philox(mcd_ctx* handle, const uint32_t* counters, const uint32_t* keys, 
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "philox");
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_draws(mcd_ctx* handle, uint64_t seed, uint64_t path_begin, uint64_t n_paths,
-              uint32_t draw_begin, uint32_t n_draws, int stream_id, int precision, double* out) {
+              uint32_t draw_begin, uint32_t n_draws, int stream_id, int precision, double* out) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (stream_id != 0 && stream_id != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "stream_id must be 0 or 1");
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "bad precision");
@@ -695,6 +745,8 @@ int mcd_draws(mcd_ctx* handle, uint64_t seed, uint64_t path_begin, uint64_t n_pa
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "draws");
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 }  // extern "C"

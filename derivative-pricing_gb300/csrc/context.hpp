@@ -132,6 +132,11 @@ double mcd_host_bsm(double spot, double strike, double rate, double carry_yield,
 double mcd_host_kemna_vorst(double spot, double strike, double rate, double carry_yield,
                             double vol, double time, int type);
 
+// Status for an exception caught at the C ABI (nothing may unwind through
+// it): host out of memory, or an internal failure; the message goes to the
+// context when there is one.  Called from the entry points' catch handlers.
+int abi_exception(mcd_ctx* handle) noexcept;
+
 #define MCD_CTX_OR_FAIL(handle, var)                              \
     if (!(handle)) return MCD_ERR_INVALID_ARGUMENT;               \
     ::mcdg::Ctx* var = reinterpret_cast<::mcdg::Ctx*>(handle);    \

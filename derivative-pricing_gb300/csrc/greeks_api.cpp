@@ -267,22 +267,26 @@ void to_pw(const mcd_greeks_result& r, mcd_pathwise_greeks* out) {
 extern "C" {
 
 int mcd_greeks_batch(mcd_ctx* handle, const mcd_contract* contracts, size_t n, double spot_bump_rel,
-                     double vol_bump_rel, int precision, mcd_greeks_result* results) {
+                     double vol_bump_rel, int precision, mcd_greeks_result* results) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     return greeks_batch(*ctx, contracts, n, spot_bump_rel, vol_bump_rel, precision, results);
+} catch (...) {
+    return abi_exception(handle);
 }
 
-int mcd_greeks_set_launch_shape(mcd_ctx* handle, int precision, int variant, int ctas_per_sm) {
+int mcd_greeks_set_launch_shape(mcd_ctx* handle, int precision, int variant, int ctas_per_sm) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "bad precision");
     if (variant < 0 || variant >= kGreeksVariants) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "variant must be 0..2");
     if (ctas_per_sm < 0 || ctas_per_sm > 64) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "ctas_per_sm must be 0..64");
     ctx->greeks_shape[precision] = LaunchShape{variant, ctas_per_sm};
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_greeks_autotune(mcd_ctx* handle, const mcd_contract* contracts, size_t n, double spot_bump_rel,
-                        double vol_bump_rel, int precision, int* variant_out, int* ctas_out, double* best_ms_out) {
+                        double vol_bump_rel, int precision, int* variant_out, int* ctas_out, double* best_ms_out) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "bad precision");
     if (n == 0 || !contracts) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "empty tuning batch");
@@ -327,6 +331,8 @@ int mcd_greeks_autotune(mcd_ctx* handle, const mcd_contract* contracts, size_t n
     if (ctas_out) *ctas_out = best_shape.ctas_per_sm;
     if (best_ms_out) *best_ms_out = best;
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 mcd_bump_sizes mcd_default_bump_sizes(double spot, double vol, double time) {
@@ -340,7 +346,7 @@ mcd_bump_sizes mcd_default_bump_sizes(double spot, double vol, double time) {
 
 int mcd_fd_european(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield, double vol,
                     double time, int type, uint64_t path_count, uint64_t seed, mcd_bump_sizes bumps, int precision,
-                    mcd_european_greeks* out) {
+                    mcd_european_greeks* out) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (!out) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "out must not be NULL");
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
@@ -370,10 +376,12 @@ int mcd_fd_european(mcd_ctx* handle, double spot, double strike, double rate, do
     out->theta = -(r[7].price - r[8].price) / (2.0 * bumps.time);
     out->rho = (r[5].price - r[6].price) / (2.0 * bumps.rate);
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_lr_european(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield, double vol,
-                    double time, int type, uint64_t path_count, uint64_t seed, int precision, mcd_lr_greeks* out) {
+                    double time, int type, uint64_t path_count, uint64_t seed, int precision, mcd_lr_greeks* out) try {
     if (!out) return MCD_ERR_INVALID_ARGUMENT;
     mcd_greeks_result r;
     const int rc = greeks_one(handle, make_contract(MCD_PRODUCT_EUROPEAN, spot, strike, rate, carry_yield, vol, time,
@@ -381,11 +389,13 @@ int mcd_lr_european(mcd_ctx* handle, double spot, double strike, double rate, do
                               precision, &r);
     if (!rc) to_lr(r, true, out);
     return rc;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_lr_digital(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield, double vol,
                    double time, int type, int digital_style, double cash_amount, uint64_t path_count, uint64_t seed,
-                   int precision, mcd_lr_greeks* out) {
+                   int precision, mcd_lr_greeks* out) try {
     if (!out) return MCD_ERR_INVALID_ARGUMENT;
     mcd_contract c = make_contract(MCD_PRODUCT_DIGITAL, spot, strike, rate, carry_yield, vol, time, type, path_count,
                                    seed);
@@ -395,11 +405,13 @@ int mcd_lr_digital(mcd_ctx* handle, double spot, double strike, double rate, dou
     const int rc = greeks_one(handle, c, precision, &r);
     if (!rc) to_lr(r, true, out);
     return rc;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_lr_barrier(mcd_ctx* handle, double spot, double strike, double barrier, double rate, double carry_yield,
                    double vol, double time, int type, int direction, int knock, double rebate,
-                   int monitoring_points, uint64_t path_count, uint64_t seed, int precision, mcd_lr_greeks* out) {
+                   int monitoring_points, uint64_t path_count, uint64_t seed, int precision, mcd_lr_greeks* out) try {
     if (!out) return MCD_ERR_INVALID_ARGUMENT;
     mcd_contract c = make_contract(MCD_PRODUCT_BARRIER, spot, strike, rate, carry_yield, vol, time, type, path_count,
                                    seed);
@@ -412,11 +424,13 @@ int mcd_lr_barrier(mcd_ctx* handle, double spot, double strike, double barrier, 
     const int rc = greeks_one(handle, c, precision, &r);
     if (!rc) to_lr(r, false, out);
     return rc;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_pathwise_european(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield, double vol,
                           double time, int type, uint64_t path_count, uint64_t seed, int precision,
-                          mcd_pathwise_greeks* out) {
+                          mcd_pathwise_greeks* out) try {
     if (!out) return MCD_ERR_INVALID_ARGUMENT;
     mcd_greeks_result r;
     const int rc = greeks_one(handle, make_contract(MCD_PRODUCT_EUROPEAN, spot, strike, rate, carry_yield, vol, time,
@@ -424,11 +438,13 @@ int mcd_pathwise_european(mcd_ctx* handle, double spot, double strike, double ra
                               precision, &r);
     if (!rc) to_pw(r, out);
     return rc;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_pathwise_asian(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield, double vol,
                        double time, int type, int strike_style, int average_style, int monitoring_points,
-                       uint64_t path_count, uint64_t seed, int precision, mcd_pathwise_greeks* out) {
+                       uint64_t path_count, uint64_t seed, int precision, mcd_pathwise_greeks* out) try {
     if (!out) return MCD_ERR_INVALID_ARGUMENT;
     mcd_contract c = make_contract(MCD_PRODUCT_ASIAN, spot, strike, rate, carry_yield, vol, time, type, path_count,
                                    seed);
@@ -439,6 +455,8 @@ int mcd_pathwise_asian(mcd_ctx* handle, double spot, double strike, double rate,
     const int rc = greeks_one(handle, c, precision, &r);
     if (!rc) to_pw(r, out);
     return rc;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 }  // extern "C"

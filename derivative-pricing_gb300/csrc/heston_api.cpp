@@ -116,19 +116,23 @@ extern "C" {
 
 int mcd_heston_qe_european(mcd_ctx* handle, const mcd_heston_params* params, double strike,
                            int type, int monitoring_points, uint64_t path_count, uint64_t seed,
-                           int precision, mcd_mc_result* out) {
+                           int precision, mcd_mc_result* out) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (!params || !out) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
     return heston_run(*ctx, params, 1, &strike, 1, type, monitoring_points, path_count, seed,
                       precision, out);
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_heston_qe_batch(mcd_ctx* handle, const mcd_heston_params* sets, size_t n_sets,
                         const double* strikes, size_t n_strikes, int type, int monitoring_points,
-                        uint64_t path_count, uint64_t seed, int precision, mcd_mc_result* results) {
+                        uint64_t path_count, uint64_t seed, int precision, mcd_mc_result* results) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     return heston_run(*ctx, sets, n_sets, strikes, n_strikes, type, monitoring_points, path_count,
                       seed, precision, results);
+} catch (...) {
+    return abi_exception(handle);
 }
 
 }  // extern "C"

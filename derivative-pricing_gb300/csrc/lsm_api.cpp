@@ -407,7 +407,7 @@ extern "C" {
 int mcd_lsm_american(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield,
                      double vol, double time, int type, int monitoring_points,
                      uint64_t path_count, uint64_t seed, int precision, int regression,
-                     mcd_lsm_result* out, double* coefficients, uint8_t* has_coefficients) {
+                     mcd_lsm_result* out, double* coefficients, uint8_t* has_coefficients) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (!out) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "out must not be NULL");
     const mcd_lsm_contract c{spot, strike, rate, carry_yield, vol, time, type, monitoring_points,
@@ -426,13 +426,15 @@ int mcd_lsm_american(mcd_ctx* handle, double spot, double strike, double rate, d
         }
     }
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_lsm_reprice_frozen(mcd_ctx* handle, double spot, double strike, double rate,
                            double carry_yield, double vol, double time, int type,
                            int monitoring_points, uint64_t path_count, uint64_t seed,
                            const double* coefficients, const uint8_t* has_coefficients,
-                           int exercise_at_inception, int precision, double* price) {
+                           int exercise_at_inception, int precision, double* price) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (!coefficients || !has_coefficients || !price) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
@@ -450,13 +452,15 @@ int mcd_lsm_reprice_frozen(mcd_ctx* handle, double spot, double strike, double r
     // choice is replayed; otherwise the price is the path average itself.
     *price = exercise_at_inception ? intrinsic_host(spot, strike, type) : out[0];
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_lsm_frozen_greeks(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield,
                           double vol, double time, int type, int monitoring_points, uint64_t path_count,
                           uint64_t seed, const double* coefficients, const uint8_t* has_coefficients,
                           int exercise_at_inception, double spot_bump, double vol_bump, int precision,
-                          mcd_american_greeks* out) {
+                          mcd_american_greeks* out) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (!coefficients || !has_coefficients || !out) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
@@ -474,10 +478,12 @@ int mcd_lsm_frozen_greeks(mcd_ctx* handle, double spot, double strike, double ra
     if (rc) return rc;
     assemble_greeks(c, spot_bump, vol_bump, exercise_at_inception != 0, res.data(), *out);
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_lsm_greeks_batch(mcd_ctx* handle, const mcd_lsm_contract* contracts, size_t n, double spot_bump_rel,
-                         double vol_bump_rel, int precision, mcd_american_greeks* results) {
+                         double vol_bump_rel, int precision, mcd_american_greeks* results) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
     if (!(spot_bump_rel > 0.0 && spot_bump_rel < 1.0) || !(vol_bump_rel > 0.0 && vol_bump_rel < 1.0))
@@ -501,15 +507,19 @@ int mcd_lsm_greeks_batch(mcd_ctx* handle, const mcd_lsm_contract* contracts, siz
         assemble_greeks(contracts[i], spot_bump_rel * contracts[i].spot, vol_bump_rel * contracts[i].vol,
                         fit[6 * i + 3] != 0.0, res.data() + 3 * kFrozenOutputs * i, results[i]);
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_lsm_batch(mcd_ctx* handle, const mcd_lsm_contract* contracts, size_t n, int precision,
-                  int regression, mcd_lsm_result* results) {
+                  int regression, mcd_lsm_result* results) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     return lsm_batch(*ctx, contracts, n, precision, regression, results, nullptr);
+} catch (...) {
+    return abi_exception(handle);
 }
 
-int mcd_lsm_set_mlp_config(mcd_ctx* handle, int steps_first, int steps, double lr_first, double lr) {
+int mcd_lsm_set_mlp_config(mcd_ctx* handle, int steps_first, int steps, double lr_first, double lr) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (steps_first < 0 || steps < 0 || steps_first > 1000000 || steps > 1000000 || !(lr_first > 0) || !(lr > 0))
         return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "steps must be 0..1e6 and learning rates > 0");
@@ -518,9 +528,11 @@ int mcd_lsm_set_mlp_config(mcd_ctx* handle, int steps_first, int steps, double l
     ctx->mlp_lr_first = static_cast<float>(lr_first);
     ctx->mlp_lr = static_cast<float>(lr);
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
-int mcd_lsm_mlp_policy(mcd_ctx* handle, size_t contract, float* weights, uint8_t* has) {
+int mcd_lsm_mlp_policy(mcd_ctx* handle, size_t contract, float* weights, uint8_t* has) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (contract >= ctx->mlp_reg_offset.size()) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "no such contract in the last learned run");
     const uint32_t off = ctx->mlp_reg_offset[contract];
@@ -539,12 +551,14 @@ int mcd_lsm_mlp_policy(mcd_ctx* handle, size_t contract, float* weights, uint8_t
                 weights[static_cast<size_t>(d) * mlp::kParams + q] = ok[d] == 1 ? buf[static_cast<size_t>(d) * mlp::kParamStride + q] : 0.0f;
     }
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_lsm_reprice_mlp(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield,
                         double vol, double time, int type, int monitoring_points, uint64_t path_count,
                         uint64_t seed, const float* weights, const uint8_t* has, int precision,
-                        mcd_lsm_result* out) {
+                        mcd_lsm_result* out) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (!weights || !has || !out) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
@@ -569,9 +583,11 @@ int mcd_lsm_reprice_mlp(mcd_ctx* handle, double spot, double strike, double rate
     out->exercise_at_inception = res[3] != 0.0 ? 1 : 0;
     out->reserved = 0;
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
-int mcd_umma_selftest(mcd_ctx* handle, const float* a, const float* b, float* d) {
+int mcd_umma_selftest(mcd_ctx* handle, const float* a, const float* b, float* d) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (!a || !b || !d) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
     int rc = ctx->reserve(ctx->ext[kErr], 256, "error word");
@@ -591,10 +607,12 @@ int mcd_umma_selftest(mcd_ctx* handle, const float* a, const float* b, float* d)
     if (e != cudaSuccess) return ctx->cuda_fail(e, "umma selftest");
     if (werr) return ctx->fail(MCD_ERR_TIMEOUT, "tensor-core wait gave up");
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_mlp_gradients(mcd_ctx* handle, const float* params, const float* x0, const float* x1, const float* y,
-                      const float* w, int n, float* grad, float* loss) {
+                      const float* w, int n, float* grad, float* loss) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (n < 1 || n > 128) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "n must be 1..128");
     if (!params || !x0 || !x1 || !y || !w || !grad || !loss) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "null argument");
@@ -627,9 +645,11 @@ int mcd_mlp_gradients(mcd_ctx* handle, const float* params, const float* x0, con
     if (e != cudaSuccess) return ctx->cuda_fail(e, "mlp gradients");
     if (werr) return ctx->fail(MCD_ERR_TIMEOUT, "tensor-core wait gave up");
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
-int mcd_mlp_forward(mcd_ctx* handle, const float* params, const float* x0, const float* x1, size_t n, float* out) {
+int mcd_mlp_forward(mcd_ctx* handle, const float* params, const float* x0, const float* x1, size_t n, float* out) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (n == 0) return MCD_OK;
     if (n > (1u << 26)) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "at most 2^26 inputs per call");
@@ -656,6 +676,8 @@ int mcd_mlp_forward(mcd_ctx* handle, const float* params, const float* x0, const
     if (e != cudaSuccess) return ctx->cuda_fail(e, "mlp forward");
     if (werr) return ctx->fail(MCD_ERR_TIMEOUT, "tensor-core wait gave up");
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 }  // extern "C"

@@ -296,13 +296,15 @@ mcd_contract qmc_contract(int product, double spot, double strike, double rate, 
 
 extern "C" {
 
-int mcd_qmc_batch(mcd_ctx* handle, const mcd_contract* contracts, size_t n, int precision, mcd_mc_result* results) {
+int mcd_qmc_batch(mcd_ctx* handle, const mcd_contract* contracts, size_t n, int precision, mcd_mc_result* results) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     return qmc_batch(*ctx, contracts, n, precision, results);
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_qmc_sobol_european(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield, double vol,
-                           double time, int type, uint64_t path_count, int precision, double* price) {
+                           double time, int type, uint64_t path_count, int precision, double* price) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (!price) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "price must not be NULL");
     const mcd_contract c = qmc_contract(MCD_PRODUCT_EUROPEAN, spot, strike, rate, carry_yield, vol, time, type,
@@ -311,11 +313,13 @@ int mcd_qmc_sobol_european(mcd_ctx* handle, double spot, double strike, double r
     const int rc = qmc_batch(*ctx, &c, 1, precision, &r);
     if (!rc) *price = r.price;
     return rc;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_qmc_sobol_asian(mcd_ctx* handle, double spot, double strike, double rate, double carry_yield, double vol,
                         double time, int type, int strike_style, int monitoring_points, uint64_t path_count,
-                        int precision, double* price) {
+                        int precision, double* price) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (!price) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "price must not be NULL");
     mcd_contract c = qmc_contract(MCD_PRODUCT_ASIAN, spot, strike, rate, carry_yield, vol, time, type, path_count);
@@ -326,10 +330,12 @@ int mcd_qmc_sobol_asian(mcd_ctx* handle, double spot, double strike, double rate
     const int rc = qmc_batch(*ctx, &c, 1, precision, &r);
     if (!rc) *price = r.price;
     return rc;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 int mcd_sobol_points(mcd_ctx* handle, unsigned dim_begin, unsigned n_dims, uint64_t index_begin, uint64_t n_indices,
-                     double* out) {
+                     double* out) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (!out) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "out must not be NULL");
     if (dim_begin + static_cast<uint64_t>(n_dims) > static_cast<uint64_t>(kSobolDims))
@@ -353,6 +359,8 @@ int mcd_sobol_points(mcd_ctx* handle, unsigned dim_begin, unsigned n_dims, uint6
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "sobol points");
     return MCD_OK;
+} catch (...) {
+    return abi_exception(handle);
 }
 
 }  // extern "C"
