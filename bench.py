@@ -309,6 +309,22 @@ def bench_qmc(eng, c):
             "timing": "wall clock of one mcd_qmc_batch call (host arrays), best of 2 after a warm-up"}
 
 
+def bench_european_1e6(eng):
+    """The reference's CPU-runnable case: European call S0 = K = 100, r = 0.05,
+    q = 0, sigma = 0.2, T = 1, 1e6 paths, seed 42, the reference's FP64
+    arithmetic (its own output: price 10.463094885721839, SE 0.014739648351400047)
+    and the FP32 path beside it; one pricer call each, host arguments, wall clock."""
+    args = (100.0, 100.0, 0.05, 0.0, 0.2, 1.0, 0, 10**6, 42)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        r, t = _timed(lambda: eng.monte_carlo_european(*args, precision=prec), reps=5)
+        out[prec] = {"s": t, "paths_per_second": 1e6 / t, "price": r.price, "standard_error": r.standard_error}
+    out["reference_price"] = 10.463094885721839
+    out["black_scholes"] = 10.450583572185565
+    out["fp64_rel_diff_vs_reference"] = abs(out["fp64"]["price"] - 10.463094885721839) / 10.463094885721839
+    return out
+
+
 PROFILE_CASES = ("path", "greeks", "qmc", "heston", "lsm", "lsm_grid", "mlp", "mlp_grid", "american_greeks")
 
 
@@ -565,6 +581,7 @@ def main():
         line["risk"] = bench_risk(eng)
         line["heston"] = bench_heston(eng)
         line["qmc"] = bench_qmc(eng, c)
+        line["european_1e6"] = bench_european_1e6(eng)
     if not args.no_cpu and rank == 0:
         line["cpu_baseline"] = cpu_baseline_sample(c)
     if rank == 0:
