@@ -211,6 +211,21 @@ def bench_lsm(eng):
     eml = np.abs(rml["price"] - r64["price"]) / se
     tree = np.array([M.crr_binomial_american(r["spot"], r["strike"], r["rate"], r["carry_yield"], r["vol"],
                                              r["time"], 2000, 1) for r in g])
+    # Out of sample: both fitted policies replayed on the same fresh paths
+    # (seed + 10^7), so foresight bias is gone and the better policy earns more.
+    mlp_pol = [eng.mlp_policy(i, int(r["monitoring_points"])) for i, r in enumerate(g)]
+    oos_qr, oos_ml, oos_se = [], [], []
+    for r, (w, has) in zip(g, mlp_pol):
+        args = (r["spot"], r["strike"], r["rate"], r["carry_yield"], r["vol"], r["time"], int(r["type"]),
+                int(r["monitoring_points"]))
+        _, co, hq = eng.monte_carlo_lsm_american(*args, int(r["path_count"]), int(r["seed"]), precision="fp64",
+                                                 policy=True)
+        fresh = int(r["seed"]) + 10_000_000
+        oos_qr.append(eng.reprice_against_frozen_policy(*args, int(r["path_count"]), fresh, co, hq, False, "fp64"))
+        ml_oos = eng.reprice_mlp(*args, int(r["path_count"]), fresh, w, has, "fp32")
+        oos_ml.append(ml_oos.price)
+        oos_se.append(ml_oos.standard_error)
+    gain = (np.array(oos_ml) - np.array(oos_qr)) / np.array(oos_se)
     return {"workload": "20 American puts (S0 36..44, sigma .2/.4, T 1/2), 50 dates, 2^20 paths each",
             "fp64_qr_s": t64, "fp32_qr_s": t32, "learned_s": tml,
             "speedup_learned_over_fp64": t64 / tml, "speedup_fp32_qr_over_fp64": t64 / t32,
@@ -224,6 +239,13 @@ def bench_lsm(eng):
                 "fp32_qr_mean_abs_err": float(np.mean(np.abs(r32["price"] - tree))),
                 "learned_mean_abs_err": float(np.mean(np.abs(rml["price"] - tree))),
                 "mean_se": float(np.mean(se))},
+            "out_of_sample": {
+                "note": "the learned policy (FP32 replay) and the FP64 QR policy (FP64 replay) on the same "
+                        "fresh 2^20 paths per put; difference learned - QR in units of the replay's standard error",
+                "learned_minus_qr_min_se": float(gain.min()), "learned_minus_qr_mean_se": float(gain.mean()),
+                "learned_minus_qr_max_se": float(gain.max()),
+                "learned_mean_abs_err_vs_tree": float(np.mean(np.abs(np.array(oos_ml) - tree))),
+                "qr_mean_abs_err_vs_tree": float(np.mean(np.abs(np.array(oos_qr) - tree)))},
             "timing": "wall clock of one mcd_lsm_batch call (host arrays, graph capture and copies included), "
                       "best of 2 after a warm-up"}
 
