@@ -465,6 +465,26 @@ __device__ __forceinline__ void layer1_row(const float* small, float x0, float x
     }
 }
 
+// The same layer with the date's input folded in: the time input x1 is one
+// value per date, so c[j] = fma(W1[j][1], x1, b1[j]) is formed once per CTA and
+// z[j] = fma(W1[j][0], x0, c[j]) -- the same bits as layer1_row.  w0 and c are
+// 16-byte aligned; four hidden units per step, stored as 8 contiguous bytes.
+__device__ __forceinline__ void layer1_row_folded(const float* w0, const float* c, float x0, __nv_bfloat16* h1,
+                                                  int s) {
+#pragma unroll 4
+    for (int j = 0; j < 64; j += 4) {
+        const float4 w = *reinterpret_cast<const float4*>(w0 + j);
+        const float4 b = *reinterpret_cast<const float4*>(c + j);
+        float t;
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(gelu(__fmaf_rn(w.x, x0, b.x), t), gelu(__fmaf_rn(w.y, x0, b.y), t));
+        const __nv_bfloat162 hi = __floats2bfloat162_rn(gelu(__fmaf_rn(w.z, x0, b.z), t), gelu(__fmaf_rn(w.w, x0, b.w), t));
+        uint2 v;
+        v.x = *reinterpret_cast<const uint32_t*>(&lo);
+        v.y = *reinterpret_cast<const uint32_t*>(&hi);
+        *reinterpret_cast<uint2*>(at(h1, s, j, 64)) = v;  // units j..j+3: one 8-byte run (j % 8 is 0 or 4)
+    }
+}
+
 enum PassMode { kStep = 1, kGram = 2, kCache = 4, kFill = 8 };
 
 template <int PREC>
@@ -718,6 +738,8 @@ struct __align__(1024) WideSmem {
     __nv_bfloat16 w2c[64 * 64];
     float pc[kParamStride - 4096];   // current network without W2
     float pd[kParamStride - 4096];   // decision output layer (b2 W3 b3 at the small-layout slots)
+    __align__(16) float w0[64];      // W1[j][0] of the current network
+    __align__(16) float c1[64];      // fma(W1[j][1], x1, b1[j]) at this date's time input
     uint64_t mbar;
     uint32_t tmem_base;
 };
@@ -766,9 +788,14 @@ __global__ void __launch_bounds__(kWideThreads, 2)
         const float* net = snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride;
         for (int i = s; i < kParams - kB2; i += kWideThreads) S.pd[kW2 + i] = net[kB2 + i];
     }
+    const float x1d = static_cast<float>(n - (e - 1)) / static_cast<float>(n);
     if (gram) {
         const float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
         for (int i = s; i < kW2; i += kWideThreads) S.pc[i] = net[i];
+        if (s < 64) {
+            S.w0[s] = net[kW1 + 2 * s];
+            S.c1[s] = __fmaf_rn(net[kW1 + 2 * s + 1], x1d, net[kB1 + s]);
+        }
         for (int i = s; i < kParams - kB2; i += kWideThreads) S.pc[kW2 + i] = net[kB2 + i];
         if (s < 64)
             for (int j = 0; j < 64; j += 2)
@@ -786,7 +813,6 @@ __global__ void __launch_bounds__(kWideThreads, 2)
     uint32_t phase = 0;
     bool ok = true;
     bool gram_pending = false, gram_started = false;
-    const float x1d = static_cast<float>(n - (e - 1)) / static_cast<float>(n);
     const uint32_t gl = g - c.group_begin;
     const uint32_t chunk0 = gl * c.group_chunks;
     const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
@@ -813,7 +839,7 @@ __global__ void __launch_bounds__(kWideThreads, 2)
         const uint32_t local = valid ? q_idx[slot] : 0u;
         const float x0 = valid ? q_x0[slot] : 0.0f;
         const float y = valid ? q_y[slot] : 0.0f;
-        layer1_row(S.pc, x0, x1d, S.h1c[half], row);
+        layer1_row_folded(S.w0, S.c1, x0, S.h1c[half], row);
         umma::fence_smem_to_async();
         umma::fence_before_sync();
         __syncthreads();
