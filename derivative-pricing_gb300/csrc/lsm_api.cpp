@@ -20,8 +20,8 @@ namespace {
 // Extension slots of Ctx::ext used by this module (Heston uses 0..3).
 enum { kDev = 4, kChunkMap = 5, kStore = 6, kCf = 7, kReg = 8, kPartA = 9, kPartB = 10,
        kFinal = 11, kOut = 12, kNets = 13, kSnaps = 14, kSnapOk = 15, kAdamT = 16, kErr = 17,
-       kGroupMap = 18, kGramPart = 19, kGramSum = 20, kFeatCache = 35, kFzDev = 36, kFzPart = 37,
-       kFzOut = 38 };
+       kGroupMap = 18, kGramPart = 19, kFeats = 20, kMomPart = 35, kFzDev = 36, kFzPart = 37,
+       kFzOut = 38, kETab = 39 };
 
 struct LsmPlan {
     std::vector<LsmDev> dev;
@@ -121,16 +121,22 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
         if (!rc) rc = ctx.reserve(ctx.ext[kAdamT], sizeof(int) * n, "mlp adam steps");
         if (!rc) rc = ctx.reserve(ctx.ext[kErr], 256, "mlp error word");
         if (!rc) rc = ctx.reserve(ctx.ext[kGroupMap], sizeof(uint32_t) * std::max<uint32_t>(p.total_groups, 1), "mlp group map");
-        if (!rc) rc = ctx.reserve(ctx.ext[kGramPart], sizeof(float) * kGramPacked * std::max<uint32_t>(p.total_groups, 1), "mlp gram partials");
-        if (!rc) rc = ctx.reserve(ctx.ext[kGramSum], sizeof(double) * kGramPacked * n, "mlp gram sums");
-        if (!rc && !frozen)
-            rc = ctx.reserve(ctx.ext[kFeatCache], 128 * std::max<uint64_t>(p.cf_elems, 1), "mlp feature cache");
+        if (!rc) rc = ctx.reserve(ctx.ext[kGramPart], sizeof(float) * kGramPacked * kNodeSlices * n, "mlp gram partials");
+        if (!rc) rc = ctx.reserve(ctx.ext[kFeats], sizeof(float) * 64 * kNodes * n, "mlp feature tables");
+        if (!rc) rc = ctx.reserve(ctx.ext[kETab], sizeof(float) * kNodes * n, "mlp continuation tables");
+        if (!rc)
+            rc = ctx.reserve(ctx.ext[kMomPart], sizeof(unsigned long long) * kMoments * kNodes *
+                                                     std::max<uint32_t>(p.total_groups, 1), "mlp bin moments");
         if (!rc) {
             cudaError_t pe = mlp_prepare();
             if (pe != cudaSuccess) rc = ctx.cuda_fail(pe, "mlp shared memory opt-in");
         }
     }
     if (rc) return rc;
+    if (mlp && !frozen)  // the bin moments of one CTA are exact 64-bit integers up to 2^23 paths
+        for (const LsmDev& d : p.dev)
+            if (static_cast<uint64_t>(d.group_chunks) * kLsmChunk > (1ull << 23))
+                return ctx.fail(MCD_ERR_INVALID_ARGUMENT, "learned regression: path_count must be <= 2^31");
     cudaError_t e = cudaMemcpyAsync(ctx.ext[kDev].ptr, p.dev.data(), sizeof(LsmDev) * n, cudaMemcpyHostToDevice, ctx.stream);
     if (e == cudaSuccess && p.total_chunks)
         e = cudaMemcpyAsync(ctx.ext[kChunkMap].ptr, p.chunk_contract.data(), sizeof(uint32_t) * p.total_chunks,
@@ -175,8 +181,9 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
                                           static_cast<int*>(ctx.ext[kSnapOk].ptr),
                                           static_cast<int*>(ctx.ext[kAdamT].ptr),
                                           static_cast<float*>(ctx.ext[kGramPart].ptr),
-                                          static_cast<double*>(ctx.ext[kGramSum].ptr),
-                                          frozen ? nullptr : ctx.ext[kFeatCache].ptr, cfg,
+                                          static_cast<float*>(ctx.ext[kFeats].ptr),
+                                          static_cast<float*>(ctx.ext[kETab].ptr),
+                                          static_cast<unsigned long long*>(ctx.ext[kMomPart].ptr), cfg,
                                           static_cast<Welford*>(ctx.ext[kFinal].ptr),
                                           static_cast<uint32_t*>(ctx.ext[kErr].ptr), ctx.stream);
         else

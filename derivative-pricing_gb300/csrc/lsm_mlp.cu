@@ -465,28 +465,6 @@ __device__ __forceinline__ void layer1_row(const float* small, float x0, float x
     }
 }
 
-// The same layer with the date's input folded in: the time input x1 is one
-// value per date, so c[j] = fma(W1[j][1], x1, b1[j]) is formed once per CTA and
-// z[j] = fma(W1[j][0], x0, c[j]) -- the same bits as layer1_row.  w0 and c are
-// 16-byte aligned; four hidden units per step, stored as 8 contiguous bytes.
-__device__ __forceinline__ void layer1_row_folded(const float* w0, const float* c, float x0, __nv_bfloat16* h1,
-                                                  int s) {
-#pragma unroll 4
-    for (int j = 0; j < 64; j += 4) {
-        const float4 w = *reinterpret_cast<const float4*>(w0 + j);
-        const float4 b = *reinterpret_cast<const float4*>(c + j);
-        float t;
-        const __nv_bfloat162 lo = __floats2bfloat162_rn(gelu(__fmaf_rn(w.x, x0, b.x), t), gelu(__fmaf_rn(w.y, x0, b.y), t));
-        const __nv_bfloat162 hi = __floats2bfloat162_rn(gelu(__fmaf_rn(w.z, x0, b.z), t), gelu(__fmaf_rn(w.w, x0, b.w), t));
-        uint2 v;
-        v.x = *reinterpret_cast<const uint32_t*>(&lo);
-        v.y = *reinterpret_cast<const uint32_t*>(&hi);
-        *reinterpret_cast<uint2*>(at(h1, s, j, 64)) = v;  // units j..j+3: one 8-byte run (j % 8 is 0 or 4)
-    }
-}
-
-enum PassMode { kStep = 1, kGram = 2, kCache = 4, kFill = 8 };
-
 template <int PREC>
 __global__ void __launch_bounds__(128)
     lsm_mlp_pass(int k, int mode, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
@@ -721,333 +699,6 @@ __global__ void __launch_bounds__(128)
 }
 
 // ---------------------------------------------------------------------------
-// The same pass with cached decision features, two tiles per CTA: 256 threads
-// work on 256-path tiles; the two halves' Z2 = H1 W2^T go to tensor-memory
-// columns [0,64) and [64,128), and one Gram MMA with K = 256 paths
-// accumulates both halves into columns [128,208).  Twice the resident warps
-// of lsm_mlp_pass for the same 256 tensor-memory columns per CTA.  Used for
-// the cached modes only (no decision network to evaluate).
-// ---------------------------------------------------------------------------
-constexpr int kWideThreads = 256;
-constexpr uint32_t kRing = 2048;          // ring slots: a chunk (1024) plus a partial tile, rounded up
-constexpr int kRingOffset = 10 * 4096;    // byte offset of xt row 80 (core-matrix row group 10)
-
-struct __align__(1024) WideSmem {
-    __nv_bfloat16 h1c[2][128 * 64];  // current network input, one 128-path half each
-    __nv_bfloat16 xt[128 * 256];     // Gram operand [row][path]; rows 66..127 stay zero
-    __nv_bfloat16 w2c[64 * 64];
-    float pc[kParamStride - 4096];   // current network without W2
-    float pd[kParamStride - 4096];   // decision output layer (b2 W3 b3 at the small-layout slots)
-    __align__(16) float w0[64];      // W1[j][0] of the current network
-    __align__(16) float c1[64];      // fma(W1[j][1], x1, b1[j]) at this date's time input
-    uint64_t mbar;
-    uint32_t tmem_base;
-};
-
-// Two CTAs per SM at most (256 tensor-memory columns and ~107 KB of shared
-// memory each), so up to 128 registers per thread cost no residency.
-template <int PREC>
-__global__ void __launch_bounds__(kWideThreads, 2)
-    lsm_mlp_pass_wide(int k, int mode, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
-                      uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
-                      const float* __restrict__ nets, const float* __restrict__ snaps,
-                      const int* __restrict__ snap_ok, float* __restrict__ gram_part,
-                      Welford* __restrict__ final_part, uint4* __restrict__ feat_cache, uint32_t* __restrict__ err) {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    WideSmem& S = *reinterpret_cast<WideSmem*>(smem_raw);
-    __shared__ Welford swf[kWideThreads / 32];
-    __shared__ Sum64 s64[kWideThreads / 32];
-    __shared__ uint32_t warp_cnt[kWideThreads / 32];
-    const uint32_t g = blockIdx.x;
-    if (g >= total_groups) return;
-    const uint32_t ci = group_contract[g];
-    const LsmDev c = cs[ci];
-    const int n = c.n_steps;
-    const int e = n - k;
-    if (e < 1) return;
-    const bool step = (mode & kStep) != 0;
-    const bool init = step && k == 0;
-    const bool last = step && e == 1;
-    const bool exercise = step && k > 0 && e <= n - 1 && snap_ok[c.reg_offset + e] == 1;  // cached features
-    const bool gram = (mode & kGram) != 0 && e - 1 >= 1;
-    const bool fill = (mode & kFill) != 0;
-    if (!step && !gram) return;
-    const int s = threadIdx.x, warp = s >> 5, half = s >> 7, row = s & 127;
-    // Per-path arithmetic in the path precision: FP64 on the FP64 path, FP32
-    // (paths, cash flows, exercise values, targets) on the FP32 path, where
-    // FP64 work would otherwise occupy the FP64 pipe (a small fraction of
-    // the FP32 rate on this GPU); the final payoff sums stay FP64.
-    using T = typename std::conditional<PREC == 0, double, float>::type;
-    const T phi = PREC == 0 ? T(c.type == 0 ? 1.0 : -1.0) : T(c.phi_f);
-    const T strike = PREC == 0 ? T(c.strike) : T(c.strike_f);
-    const T inv_k = PREC == 0 ? T(1.0 / c.strike) : T(c.inv_strike_f);
-    const T disc = PREC == 0 ? T(c.disc) : T(c.disc_f);
-    const T* S_path = static_cast<const T*>(store) + c.s_offset;
-    T* cft = reinterpret_cast<T*>(cf) + c.cf_offset;
-    if (exercise) {
-        const float* net = snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride;
-        for (int i = s; i < kParams - kB2; i += kWideThreads) S.pd[kW2 + i] = net[kB2 + i];
-    }
-    const float x1d = static_cast<float>(n - (e - 1)) / static_cast<float>(n);
-    if (gram) {
-        const float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
-        for (int i = s; i < kW2; i += kWideThreads) S.pc[i] = net[i];
-        if (s < 64) {
-            S.w0[s] = net[kW1 + 2 * s];
-            S.c1[s] = __fmaf_rn(net[kW1 + 2 * s + 1], x1d, net[kB1 + s]);
-        }
-        for (int i = s; i < kParams - kB2; i += kWideThreads) S.pc[kW2 + i] = net[kB2 + i];
-        if (s < 64)
-            for (int j = 0; j < 64; j += 2)
-                *reinterpret_cast<__nv_bfloat162*>(at(S.w2c, s, j, 64)) =
-                    __floats2bfloat162_rn(net[kW2 + s * 64 + j], net[kW2 + s * 64 + j + 1]);
-        for (int i = s; i < 128 * 256 / 2; i += kWideThreads) reinterpret_cast<uint32_t*>(S.xt)[i] = 0u;
-        if (s == 0) umma::mbar_init(&S.mbar, 1);
-        if (warp == 0) umma::tmem_alloc(&S.tmem_base, 256);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        umma::fence_before_sync();
-    }
-    __syncthreads();
-    if (gram) umma::fence_after_sync();
-    const uint32_t tm = gram ? S.tmem_base : 0u;
-    uint32_t phase = 0;
-    bool ok = true;
-    bool gram_pending = false, gram_started = false;
-    const uint32_t gl = g - c.group_begin;
-    const uint32_t chunk0 = gl * c.group_chunks;
-    const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
-    Welford w{0ull, 0.0, 0.0};
-    Sum32 fin{0u, 0.0f, 0.0f, 0.0f, 0.0f};  // FP32 path: the last date's payoffs
-    // Ring of in-the-money paths of date e-1 awaiting a 256-path feature tile
-    // (path index within the group, network input, target): the fit only
-    // uses those paths, so tiles carry no out-of-the-money rows.  It lives in
-    // rows 80..127 of xt: the Gram MMA reads those rows only into output
-    // rows that are never read (row i of D depends on row i of A alone; B is
-    // rows 0..79), so they are free for scratch.
-    uint32_t* q_idx = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(S.xt) + kRingOffset);
-    float* q_x0 = reinterpret_cast<float*>(q_idx + kRing);
-    float* q_y = q_x0 + kRing;
-    uint32_t q_head = 0, q_len = 0;  // uniform over the CTA
-    const uint64_t first_path = static_cast<uint64_t>(chunk0) * kLsmChunk;
-    // One tile: the n_valid ring entries from q_head (the rest of the rows
-    // zero): layer 1 on CUDA cores, Z2 = H1 W2^T (two 128-row halves), the
-    // GELU features (cached for the next date's decisions), then the Gram
-    // MMA over the tile's 256 columns.
-    auto feature_tile = [&](uint32_t n_valid) {
-        const uint32_t slot = (q_head + s) & (kRing - 1);
-        const bool valid = static_cast<uint32_t>(s) < n_valid;
-        const uint32_t local = valid ? q_idx[slot] : 0u;
-        const float x0 = valid ? q_x0[slot] : 0.0f;
-        const float y = valid ? q_y[slot] : 0.0f;
-        layer1_row_folded(S.w0, S.c1, x0, S.h1c[half], row);
-        umma::fence_smem_to_async();
-        umma::fence_before_sync();
-        __syncthreads();
-        if (s == 0) {
-            umma::fence_after_sync();
-            for (int hh = 0; hh < 2; ++hh)
-                for (int kk = 0; kk < 4; ++kk)
-                    umma::mma_bf16(tm + 64 * hh, desc(S.h1c[hh], 1024, kk), desc(S.w2c, 1024, kk), kIdesc, kk > 0);
-            umma::mma_commit(&S.mbar);  // also covers the previous tile's Gram MMA
-        }
-        ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 21));
-        phase ^= 1u;
-        gram_pending = false;
-        umma::fence_after_sync();
-        uint4* dst = fill && valid ? feat_cache + (c.cf_offset + first_path + local) * 8 : nullptr;
-        for (int cc = 0; cc < 4; ++cc) {
-            float zz[16];
-            umma::tmem_ld16(umma::tmem_addr(tm, 32 * (warp & 3), 64 * half + cc * 16), zz);
-            uint32_t packed[8];
-#pragma unroll
-            for (int q = 0; q < 16; q += 2) {
-                float t;
-                const float ha = valid ? gelu(zz[q] + S.pc[sB2 + cc * 16 + q], t) : 0.0f;
-                const float hb = valid ? gelu(zz[q + 1] + S.pc[sB2 + cc * 16 + q + 1], t) : 0.0f;
-                const __nv_bfloat162 hp = __floats2bfloat162_rn(ha, hb);
-                *at(S.xt, cc * 16 + q, s, 256) = hp.x;
-                *at(S.xt, cc * 16 + q + 1, s, 256) = hp.y;
-                packed[q / 2] = *reinterpret_cast<const uint32_t*>(&hp);
-            }
-            if (dst) {
-                dst[2 * cc] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                dst[2 * cc + 1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-            }
-        }
-        *at(S.xt, 64, s, 256) = __float2bfloat16_rn(valid ? 1.0f : 0.0f);
-        *at(S.xt, 65, s, 256) = __float2bfloat16_rn(y);
-        umma::fence_smem_to_async();
-        umma::fence_before_sync();
-        __syncthreads();
-        if (s == 0) {
-            umma::fence_after_sync();
-            // D[i][j] += sum over the tile's 256 columns of xt[i][p] xt[j][p]  (M = 128, N = 80, K = 256)
-            for (int kk = 0; kk < 16; ++kk)
-                umma::mma_bf16(tm + 128, desc(S.xt, 4096, kk), desc(S.xt, 4096, kk), umma::idesc_bf16(128, kGramN),
-                               gram_started || kk > 0);
-        }
-        gram_started = true;
-        gram_pending = true;
-        q_head = (q_head + n_valid) & (kRing - 1);
-        q_len -= n_valid;
-    };
-    constexpr int kPer = kLsmChunk / kWideThreads;  // paths per thread and chunk
-    for (uint32_t ch = chunk0; ch < chunk1; ++ch) {
-        // every path load of this thread's kPer paths first (independent, in flight together)
-        T vv[kPer], se[kPer], sd[kPer];
-        bool live[kPer];
-#pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + q * kWideThreads + s;
-            live[q] = i < c.path_count;
-            vv[q] = se[q] = sd[q] = T(0);
-            if (live[q]) {
-                vv[q] = init ? S_path[static_cast<uint64_t>(n - 1) * c.path_count + i] : cft[i];
-                if (exercise) se[q] = S_path[static_cast<uint64_t>(e - 1) * c.path_count + i];
-                if (gram) sd[q] = S_path[static_cast<uint64_t>(e - 2) * c.path_count + i];
-            }
-        }
-        bool itm[kPer];
-        float x0[kPer], y[kPer];
-#pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + q * kWideThreads + s;
-            itm[q] = false;
-            x0[q] = y[q] = 0.0f;
-            if (!live[q]) continue;
-            T v = vv[q];
-            if (init) {
-                const T x = phi * (v - strike);
-                v = x > T(0) ? x : T(0);
-            }
-            if (exercise) {
-                const T xx = phi * (se[q] - strike);
-                const T ex_e = xx > T(0) ? xx : T(0);
-                if (ex_e > T(0)) {
-                    const uint4* src = feat_cache + (c.cf_offset + i) * 8;
-                    float yh = S.pd[sB3];
-#pragma unroll
-                    for (int r = 0; r < 8; ++r) {
-                        const uint4 u = src[r];
-                        const uint32_t words[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-                        for (int h = 0; h < 4; ++h) {
-                            const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&words[h]));
-                            yh = __fmaf_rn(S.pd[sW3 + r * 8 + 2 * h], f.x, yh);
-                            yh = __fmaf_rn(S.pd[sW3 + r * 8 + 2 * h + 1], f.y, yh);
-                        }
-                    }
-                    if (yh < 0.0f) v = ex_e;  // predicted time value < 0: exercise
-                }
-            }
-            if (step) {
-                v *= disc;
-                if (last) {
-                    if constexpr (PREC == 0) {
-                        welford_add(w, v);
-                    } else {
-                        sum32_add(fin, v);
-                    }
-                } else {
-                    cft[i] = v;
-                }
-            }
-            if (gram) {
-                const T xx = phi * (sd[q] - strike);
-                const T ex_d = xx > T(0) ? xx : T(0);
-                itm[q] = ex_d > T(0);
-                if constexpr (PREC == 0) x0[q] = static_cast<float>(4.0 * (sd[q] * inv_k - 1.0));
-                else x0[q] = 4.0f * (sd[q] * inv_k - 1.0f);
-                y[q] = static_cast<float>((v - ex_d) * inv_k);
-            }
-        }
-        if (gram) {
-            // The chunk's paths in the money at date e-1 join the ring of
-            // paths awaiting a feature tile (the others take no part in the
-            // fit): a block-wide exclusive scan of the per-thread counts.
-            uint32_t mine = 0;
-#pragma unroll
-            for (int q = 0; q < kPer; ++q) mine += itm[q] ? 1u : 0u;
-            uint32_t incl = mine;
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
-                if ((s & 31) >= off) incl += o;
-            }
-            if ((s & 31) == 31) warp_cnt[warp] = incl;
-            __syncthreads();
-            uint32_t before = incl - mine, total = 0;
-            for (int wi = 0; wi < kWideThreads / 32; ++wi) {
-                const uint32_t cw = warp_cnt[wi];
-                before += wi < warp ? cw : 0u;
-                total += cw;
-            }
-            uint32_t pos = q_head + q_len + before;
-#pragma unroll
-            for (int q = 0; q < kPer; ++q) {
-                if (!itm[q]) continue;
-                const uint32_t slot = pos & (kRing - 1);
-                q_idx[slot] = static_cast<uint32_t>(static_cast<uint64_t>(ch) * kLsmChunk + q * kWideThreads + s -
-                                                    first_path);
-                q_x0[slot] = x0[q];
-                q_y[slot] = y[q];
-                ++pos;
-            }
-            q_len += total;
-            __syncthreads();
-            while (q_len >= static_cast<uint32_t>(kWideThreads)) feature_tile(kWideThreads);
-        }
-        if (last) {  // one final partial per chunk, fixed tree
-            if constexpr (PREC == 0) {
-                Welford r = welford_warp_reduce(w);
-                if ((s & 31) == 0) swf[warp] = r;
-                __syncthreads();
-                if (s == 0) {
-                    Welford m = swf[0];
-                    for (int q = 1; q < kWideThreads / 32; ++q) m = welford_merge(m, swf[q]);
-                    final_part[c.chunk_begin + ch] = m;
-                }
-                w = Welford{0ull, 0.0, 0.0};
-            } else {
-                const Sum32 r = sum32_warp_reduce(fin);
-                if ((s & 31) == 0) s64[warp] = sum32_wide(r);
-                __syncthreads();
-                if (s == 0) final_part[c.chunk_begin + ch] = sum64_fold<kWideThreads / 32>(s64);
-                fin = Sum32{0u, 0.0f, 0.0f, 0.0f, 0.0f};
-            }
-            __syncthreads();
-        }
-    }
-    if (gram && q_len > 0) feature_tile(q_len);  // the remainder (< 256 paths)
-    if (gram) {
-        if (gram_pending) {
-            if (s == 0) umma::mma_commit(&S.mbar);
-            ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 22));
-            phase ^= 1u;
-            umma::fence_after_sync();
-        }
-        float* out = gram_part + static_cast<size_t>(g) * kGramPacked;
-        if (warp < 3) {  // lanes 0..95 hold rows 0..95; the upper triangle of rows 0..65 is kept
-            const int row0 = s * kGramDim - s * (s - 1) / 2;
-            for (int cc = 0; cc < 5; ++cc) {
-                float dd[16];
-                umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 128 + cc * 16), dd);
-                if (s < kGramDim)
-                    for (int q = 0; q < 16; ++q) {
-                        const int col = cc * 16 + q;
-                        // no in-the-money path in this group: no MMA wrote the accumulator
-                        if (col >= s && col < kGramDim) out[row0 + col - s] = ok && gram_started ? dd[q] : 0.0f;
-                    }
-            }
-        }
-        if (!ok) umma::mbar_wait(&S.mbar, phase, err, 23);
-        umma::fence_before_sync();
-        __syncthreads();
-        if (warp == 0) umma::tmem_dealloc(tm, 256);
-    }
-}
-
-// ---------------------------------------------------------------------------
 // output layer of date d = n - k - 1: ridge least squares on the Gram matrix
 //
 // The 64 GELU features are smooth functions of one state variable and are
@@ -1076,38 +727,6 @@ __device__ __forceinline__ int packed_index(int r, int q) {  // r <= q
     return r * kGramDim - r * (r - 1) / 2 + (q - r);
 }
 
-// Sum of the group partials of every contract: one thread per packed entry,
-// a fixed-order compensated (Kahan) FP32 sum over the groups (loads issued
-// eight at a time), stored as the FP64 value sum - compensation.
-__global__ void __launch_bounds__(128)
-    lsm_mlp_gram_reduce(int k, const LsmDev* __restrict__ cs, int n_contracts, const float* __restrict__ gram_part,
-                        double* __restrict__ gram_sum) {
-    const int idx = blockIdx.x * 128 + threadIdx.x;
-    if (idx >= kGramPacked) return;
-    for (int ci = blockIdx.y; ci < n_contracts; ci += gridDim.y) {
-        const LsmDev c = cs[ci];
-        if (c.n_steps - k - 1 < 1) continue;
-        const float* base = gram_part + static_cast<size_t>(c.group_begin) * kGramPacked + idx;
-        float sum = 0.0f, comp = 0.0f;
-        auto add = [&](float v) {
-            const float y = __fsub_rn(v, comp);
-            const float t = __fadd_rn(sum, y);
-            comp = __fsub_rn(__fsub_rn(t, sum), y);
-            sum = t;
-        };
-        uint32_t gg = 0;
-        for (; gg + 8 <= c.n_groups; gg += 8) {
-            float v[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = base[static_cast<size_t>(gg + u) * kGramPacked];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) add(v[u]);
-        }
-        for (; gg < c.n_groups; ++gg) add(base[static_cast<size_t>(gg) * kGramPacked]);
-        gram_sum[static_cast<size_t>(ci) * kGramPacked + idx] = static_cast<double>(sum) - static_cast<double>(comp);
-    }
-}
-
 // x = L^-T L^-1 b for the FP32 factor L (lower, row stride kGramDim,
 // reciprocal diagonal in inv_diag), by one warp on shared vectors: b is
 // overwritten, the solution lands in x.  Dropped regressors give 0 (their
@@ -1129,7 +748,7 @@ __device__ void chol_solve_warp(const float* L, const float* inv_diag, float* b,
 }
 
 __global__ void __launch_bounds__(kSolveThreads)
-    lsm_mlp_solve(int k, const LsmDev* __restrict__ cs, int n_contracts, const double* __restrict__ gram_sum,
+    lsm_mlp_solve(int k, const LsmDev* __restrict__ cs, int n_contracts, const float* __restrict__ gram_part,
                   float* __restrict__ nets, float* __restrict__ snaps, int* __restrict__ snap_ok) {
     __shared__ double G[kGramPacked];   // Gram matrix, packed upper triangle; standardised in place
     __shared__ float L[kM * kGramDim];  // FP32 Cholesky factor (lower)
@@ -1144,7 +763,12 @@ __global__ void __launch_bounds__(kSolveThreads)
     const int d = c.n_steps - k - 1;
     if (d < 1) return;
     const int s = threadIdx.x, lane = s & 31, warp = s >> 5;
-    for (int idx = s; idx < kGramPacked; idx += kSolveThreads) G[idx] = gram_sum[static_cast<size_t>(ci) * kGramPacked + idx];
+    for (int idx = s; idx < kGramPacked; idx += kSolveThreads) {  // the bin quarters' partials, in order
+        const float* p = gram_part + static_cast<size_t>(ci) * kNodeSlices * kGramPacked + idx;
+        double v = 0.0;
+        for (int sl = 0; sl < kNodeSlices; ++sl) v += static_cast<double>(p[static_cast<size_t>(sl) * kGramPacked]);
+        G[idx] = v;
+    }
     if (s == 0) bad = 0;
     __syncthreads();
     const double count = G[packed_index(64, 64)];
@@ -1391,8 +1015,6 @@ cudaError_t mlp_prepare() {
     if (e == cudaSuccess) e = set_smem(mlp_grad_kernel, sizeof(TrainSmem));
     if (e == cudaSuccess) e = set_smem(lsm_mlp_pass<0>, sizeof(PassSmem));
     if (e == cudaSuccess) e = set_smem(lsm_mlp_pass<1>, sizeof(PassSmem));
-    if (e == cudaSuccess) e = set_smem(lsm_mlp_pass_wide<0>, sizeof(WideSmem));
-    if (e == cudaSuccess) e = set_smem(lsm_mlp_pass_wide<1>, sizeof(WideSmem));
     if (e == cudaSuccess) e = set_smem(mlp_forward_kernel, sizeof(InferSmem));
     return e;
 }
@@ -1400,36 +1022,20 @@ cudaError_t mlp_prepare() {
 cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int n_contracts,
                                      const uint32_t* group_contract, uint32_t total_groups, const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
-                                     float* gram_part, double* gram_sum, void* feat_cache, const MlpConfig& cfg,
-                                     Welford* final_part, uint32_t* err, cudaStream_t stream) {
+                                     float* gram_part, float* feats, float* etab, unsigned long long* mom_part,
+                                     const MlpConfig& cfg, Welford* final_part, uint32_t* err, cudaStream_t stream) {
     cudaGetLastError();
     if (total_groups == 0) return cudaSuccess;
     const size_t pass_smem = sizeof(PassSmem);
-    uint4* cache = static_cast<uint4*>(feat_cache);
-    auto pass = [&](int mode) {
+    auto pass = [&](int mode) {  // the per-path network: terminal step, and replays of a given policy
         if (precision == 0)
             lsm_mlp_pass<0><<<total_groups, 128, pass_smem, stream>>>(k, mode, c, group_contract, total_groups, store,
                                                                       cf, nets, snaps, snap_ok, gram_part, final_part,
-                                                                      cache, err);
+                                                                      nullptr, err);
         else
             lsm_mlp_pass<1><<<total_groups, 128, pass_smem, stream>>>(k, mode, c, group_contract, total_groups, store,
                                                                       cf, nets, snaps, snap_ok, gram_part, final_part,
-                                                                      cache, err);
-    };
-    // With the features fixed after the first date (no fine-tuning), each
-    // pass reuses the previous pass's features for its decisions and runs as
-    // the two-tile kernel.
-    const int reuse = (cache != nullptr && cfg.steps == 0) ? (kCache | kFill) : 0;
-    auto pass_wide = [&](int mode) {
-        const size_t smem = sizeof(WideSmem);
-        if (precision == 0)
-            lsm_mlp_pass_wide<0><<<total_groups, kWideThreads, smem, stream>>>(
-                k, mode, c, group_contract, total_groups, store, cf, nets, snaps, snap_ok, gram_part, final_part,
-                cache, err);
-        else
-            lsm_mlp_pass_wide<1><<<total_groups, kWideThreads, smem, stream>>>(
-                k, mode, c, group_contract, total_groups, store, cf, nets, snaps, snap_ok, gram_part, final_part,
-                cache, err);
+                                                                      nullptr, err);
     };
     auto trainer = [&]() {
         if (precision == 0)
@@ -1443,19 +1049,17 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
         pass(kStep);
         return cudaGetLastError();
     }
+    int mode = kStep | kGram;  // exercise at date e, discount, regression data of date e-1
     if (k == 0) {
-        pass(kStep);                        // terminal cash flows, first discount
-        trainer();                          // learn the features on the latest date
-        if (reuse) pass_wide(kGram | kFill);  // Gram matrix of that date
-        else pass(kGram);
-    } else if (reuse) {
-        pass_wide(kStep | kGram | reuse);   // exercise at date e (cached features), discount, Gram of date e-1
-    } else {
-        pass(kStep | kGram);
+        pass(kStep);  // terminal cash flows, first discount
+        trainer();    // learn the features on the latest date
+        mode = kGram;
     }
-    const dim3 rgrid((kGramPacked + 127) / 128, static_cast<unsigned>(n_contracts < 65535 ? n_contracts : 65535));
-    lsm_mlp_gram_reduce<<<rgrid, 128, 0, stream>>>(k, c, n_contracts, gram_part, gram_sum);
-    lsm_mlp_solve<<<n_contracts, kSolveThreads, 0, stream>>>(k, c, n_contracts, gram_sum, nets, snaps, snap_ok);
+    cudaError_t e = launch_lsm_mlp_nodes(precision, k, mode, c, n_contracts, group_contract, total_groups, store, cf,
+                                         nets, snaps, snap_ok, feats, etab, mom_part, gram_part, final_part, err,
+                                         stream);
+    if (e != cudaSuccess) return e;
+    lsm_mlp_solve<<<n_contracts, kSolveThreads, 0, stream>>>(k, c, n_contracts, gram_part, nets, snaps, snap_ok);
     if (k > 0 && cfg.steps > 0) trainer();  // optional fine-tuning of the features
     return cudaGetLastError();
 }

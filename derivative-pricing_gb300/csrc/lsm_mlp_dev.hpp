@@ -1,6 +1,7 @@
 // lsm_mlp_dev.hpp -- launch interface of the learned-regression kernels.
 #pragma once
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -18,19 +19,83 @@ struct MlpConfig {
     float lr;
 };
 
+// Pass modes: kStep = exercise, discount and cash-flow update at date n-k;
+// kGram = regression data of date n-k-1; kCache / kFill: the per-path decision
+// kernel's feature reuse.
+enum PassMode { kStep = 1, kGram = 2, kCache = 4, kFill = 8 };
+
+// Node tables.  The network's inputs are x0 = 4 (S/K - 1) and the date's time
+// input, which is one value per date, so at a date every learned feature is a
+// function of u = ln(S/K) alone.  The features are evaluated (tcgen05) at
+// kNodes equally spaced values of u covering the in-the-money side of the
+// date's distribution, and every path uses their linear interpolation: as its
+// regression basis (the fit is exact least squares on the interpolated
+// features, built from per-bin moments of the paths) and for its exercise
+// decision (an interpolated continuation table).
+constexpr int kNodes = 512;
+constexpr int kNodeSlices = 4;                       // Gram CTAs per contract (bins split in four)
+constexpr int kMoments = 5;                          // per bin: n, sum t, sum t^2, sum y, sum t y
+constexpr double kTScale = 65536.0;                  // t in [0, 1] as an integer of 16 bits
+constexpr double kYScale = 16777216.0;               // |y| / y_bound as an integer of 24 bits
+constexpr double kGridSd = 7.0;                      // the grid covers the mean +/- 7 standard deviations
+
+struct NodeGrid {
+    float lo, h, inv_h;  // node i at u = lo + i h
+    float y_bound;       // |(cash flow - exercise value) / K| is at most this on the grid's paths
+};
+
+// ln(S_d/K) of the stored GBM paths is normal with mean ln(S0/K) + d drift and
+// standard deviation vs sqrt(d); the grid takes the in-the-money side of
+// +/- kGridSd of it (paths beyond use the end bins).  Every kernel derives
+// the grid from this function, so they agree on it bit for bit.
+__host__ __device__ inline NodeGrid node_grid(const LsmDev& c, int date) {
+    const double m = log(c.spot / c.strike) + static_cast<double>(date) * c.drift;
+    const double s = c.vs * sqrt(static_cast<double>(date));
+    double lo, hi;
+    if (c.type == 1) {  // put: in the money below the strike
+        lo = fmin(m - kGridSd * s, -1e-6);
+        hi = 0.0;
+    } else {
+        lo = 0.0;
+        hi = fmax(m + kGridSd * s, 1e-6);
+    }
+    const double h = (hi - lo) / static_cast<double>(kNodes - 1);
+    // cash flows and exercise values are at most max(S)/K over the remaining dates
+    const double n = static_cast<double>(c.n_steps);
+    const double top = log(c.spot / c.strike) + n * fmax(c.drift, 0.0) + kGridSd * c.vs * sqrt(n);
+    NodeGrid g;
+    g.lo = static_cast<float>(lo);
+    g.h = static_cast<float>(h);
+    g.inv_h = static_cast<float>(1.0 / h);
+    g.y_bound = static_cast<float>(c.type == 1 ? 1.0 : 2.0 * fmax(exp(top), 1.0));
+    return g;
+}
+
+// One backward iteration of the learned regression on node tables (k as in
+// launch_lsm_mlp_iteration): lsm_mlp_nodes (continuation table of date n-k from
+// its fitted output layer, then the feature table of date n-k-1), the binned
+// path pass (exercise, discount, moments of date n-k-1), and the sliced Gram
+// matrices the solve sums.
+cudaError_t launch_lsm_mlp_nodes(int precision, int k, int mode, const LsmDev* c, int n_contracts,
+                                 const uint32_t* group_contract, uint32_t total_groups, const void* store,
+                                 double* cf, const float* nets, const float* snaps, const int* snap_ok,
+                                 float* feats, float* etab, unsigned long long* mom_part, float* gram_part,
+                                 Welford* final_part, uint32_t* err, cudaStream_t stream);
+
 size_t mlp_train_smem_bytes();
 size_t mlp_infer_smem_bytes();
 cudaError_t mlp_prepare();  // opts the kernels into their dynamic shared memory
-// One backward iteration k: exercise at date n-k with that date's network,
-// discount, and (train = true) the Gram matrix and output-layer fit of date
-// n-k-1; at k = 0 the features are first trained on that date.  feat_cache
-// (128 B per path, or null) carries each date's BF16 features to the next
-// iteration's exercise decisions when the features are not fine-tuned.
+// One backward iteration k: exercise at date n-k, discount, and (train =
+// true) the Gram matrix and output-layer fit of date n-k-1 on node tables; at
+// k = 0 the features are first trained on that date.  train = false replays
+// given networks path by path (lsm_mlp_pass).  Buffers: gram_part
+// n x kNodeSlices x kGramPacked floats, feats n x kNodes x 64 floats, etab
+// n x kNodes floats, mom_part groups x kMoments x kNodes.
 cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int n_contracts,
                                      const uint32_t* group_contract, uint32_t total_groups, const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
-                                     float* gram_part, double* gram_sum, void* feat_cache, const MlpConfig& cfg,
-                                     Welford* final_part, uint32_t* err, cudaStream_t stream);
+                                     float* gram_part, float* feats, float* etab, unsigned long long* mom_part,
+                                     const MlpConfig& cfg, Welford* final_part, uint32_t* err, cudaStream_t stream);
 cudaError_t launch_mlp_grad(const float* params, const float* x0, const float* x1, const float* y, const float* w,
                             int n, float* grad, float* loss, uint32_t* err, cudaStream_t stream);
 cudaError_t launch_mlp_forward(const float* params, const float* x0, const float* x1, int n, float* out,

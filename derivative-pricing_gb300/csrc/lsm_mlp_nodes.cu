@@ -1,0 +1,505 @@
+// lsm_mlp_nodes.cu -- the learned regression on node tables.
+//
+// At an exercise date the continuation network (lsm_mlp.cu, mlp.cuh) sees
+// x0 = 4 (S/K - 1) and a time input that is one value per date, so each of its
+// 64 last-layer features is a function of u = ln(S/K) alone at that date.
+// Rather than evaluating the 2 -> 64 -> 64 network once per in-the-money path
+// and date, each (contract, date) evaluates it at kNodes = 512 equally spaced
+// values of u over the in-the-money side of the date's distribution (node_grid,
+// lsm_mlp_dev.hpp) and every path uses the linear interpolation of those
+// nodes, f(u) = (1 - t) F_i + t F_{i+1} with u in bin i at fraction t:
+//
+//   lsm_mlp_nodes        one CTA per contract: the continuation table of
+//                        date e (E_i = b3 + W3 . F_e,i from the output layer
+//                        fitted at e), then the feature table F of date e-1:
+//                        layer 1 on the CUDA cores, Z2 = H1 W2^T on the tensor
+//                        core (tcgen05, BF16 operands, FP32 accumulator in
+//                        tensor memory), GELU; four 128-node tiles.
+//   lsm_mlp_binned       one CTA per group of chunks: exercise at date e where
+//                        the interpolated continuation value is negative,
+//                        discount, cash-flow update, and for the paths in the
+//                        money at date e-1 the per-bin moments n, sum t,
+//                        sum t^2, sum y, sum t y (y = time value / K) as exact
+//                        integers (t to 16 bits, y to 24 bits of its bound)
+//                        with shared-memory atomics: the sums do not depend on
+//                        the order of the additions, so the result is
+//                        deterministic.
+//   lsm_mlp_gram_slices  kNodeSlices CTAs per contract: the Gram matrix of
+//                        [f | 1 | y] over the paths from the moments,
+//                        G = sum over bins of (1-t)^2 F_i F_i^T + t(1-t)
+//                        (F_i F_{i+1}^T + F_{i+1} F_i^T) + t^2 F_{i+1} F_{i+1}^T
+//                        (and the right-hand side likewise), one partial per
+//                        quarter of the bins; lsm_mlp_solve sums the four.
+//
+// The least-squares fit over the interpolated features is exact (no path is
+// left out and no feature rounded to BF16 on its way to the Gram matrix); the
+// interpolation moves a feature by ~h^2 f''/8 (h = 1/511 of the grid), far
+// below the BF16 rounding of the network's own hidden layer.  Every mbarrier
+// wait is bounded (umma.cuh).
+//
+// nvcc-flags: --fmad=false
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "device_common.cuh"
+#include "lsm.hpp"
+#include "lsm_mlp_dev.hpp"
+#include "mlp.cuh"
+#include "umma.cuh"
+
+namespace mcdg {
+
+using namespace mlp;
+
+namespace {
+
+constexpr int kGramDim = 66;   // 64 features, constant, target
+constexpr int kFStride = 68;   // feature-table row stride in shared memory (16-byte rows)
+constexpr int kBinsPerSlice = kNodes / kNodeSlices;
+constexpr uint32_t kNodeIdesc = umma::idesc_bf16(128, 64);
+static_assert(kNodes % 128 == 0 && kNodes % kNodeSlices == 0, "node tiles");
+
+__device__ __forceinline__ __nv_bfloat16* at(__nv_bfloat16* base, int r, int k, int kcols) {
+    return reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(base) + umma::kmajor_offset(r, k, kcols));
+}
+
+__device__ __forceinline__ uint64_t desc(const void* p, uint32_t sbo, int kstep) {
+    return umma::smem_desc(umma::smem_u32(p) + static_cast<uint32_t>(kstep) * 256u, 128u, sbo);
+}
+
+__device__ __forceinline__ int packed_index(int r, int q) {  // r <= q
+    return r * kGramDim - r * (r - 1) / 2 + (q - r);
+}
+
+// Bin and fraction of u on a grid: u below the first node or above the last
+// uses the end bin (t clamped to [0, 1]).
+__device__ __forceinline__ void locate(const NodeGrid& g, float u, int& i, float& t) {
+    float x = (u - g.lo) * g.inv_h;
+    x = fminf(fmaxf(x, 0.0f), static_cast<float>(kNodes - 1));
+    i = min(static_cast<int>(x), kNodes - 2);
+    t = fminf(x - static_cast<float>(i), 1.0f);
+}
+
+// ---------------------------------------------------------------------------
+// Node tables: continuation values of date e and features of date e-1.
+// ---------------------------------------------------------------------------
+struct __align__(1024) NodeSmem {
+    __nv_bfloat16 h1[128 * 64];  // A: [node][hidden 1], K-major, K = 64
+    __nv_bfloat16 w2[64 * 64];   // B: [hidden 2][hidden 1], K-major
+    __align__(16) float w0[64];  // W1[j][0]
+    __align__(16) float c1[64];  // fma(W1[j][1], x1, b1[j]) at the date's time input
+    float b2[64];
+    float w3[64];
+    uint64_t mbar;
+    uint32_t tmem_base;
+};
+
+// Layer 1 of one node with the date's time input folded into c:
+// z[j] = fma(W1[j][0], x0, c[j]); four hidden units per 8-byte store.
+__device__ __forceinline__ void layer1_node(const float* w0, const float* c, float x0, __nv_bfloat16* h1, int s) {
+#pragma unroll 4
+    for (int j = 0; j < 64; j += 4) {
+        const float4 w = *reinterpret_cast<const float4*>(w0 + j);
+        const float4 b = *reinterpret_cast<const float4*>(c + j);
+        float t;
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(gelu(__fmaf_rn(w.x, x0, b.x), t), gelu(__fmaf_rn(w.y, x0, b.y), t));
+        const __nv_bfloat162 hi = __floats2bfloat162_rn(gelu(__fmaf_rn(w.z, x0, b.z), t), gelu(__fmaf_rn(w.w, x0, b.w), t));
+        uint2 v;
+        v.x = *reinterpret_cast<const uint32_t*>(&lo);
+        v.y = *reinterpret_cast<const uint32_t*>(&hi);
+        *reinterpret_cast<uint2*>(at(h1, s, j, 64)) = v;  // units j..j+3: one 8-byte run (j % 8 is 0 or 4)
+    }
+}
+
+__global__ void __launch_bounds__(128)
+    lsm_mlp_nodes(int k, const LsmDev* __restrict__ cs, int n_contracts, const float* __restrict__ nets,
+                  const float* __restrict__ snaps, const int* __restrict__ snap_ok, float* __restrict__ feats,
+                  float* __restrict__ etab, uint32_t* __restrict__ err) {
+    __shared__ NodeSmem S;
+    const int ci = blockIdx.x;
+    if (ci >= n_contracts) return;
+    const LsmDev c = cs[ci];
+    const int n = c.n_steps;
+    const int e = n - k;
+    if (e < 1) return;
+    const int d = e - 1;
+    const int s = threadIdx.x, warp = s >> 5;
+    float* F = feats + static_cast<size_t>(ci) * kNodes * 64;
+    // 1. continuation table of date e, from the features fitted there (still in F)
+    if (k > 0 && e <= n - 1 && snap_ok[c.reg_offset + e] == 1) {
+        const float* snap = snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride;
+        if (s < 64) S.w3[s] = snap[kW3 + s];
+        __syncthreads();
+        const float b3 = snap[kB3];
+        for (int i = s; i < kNodes; i += 128) {
+            const float4* row = reinterpret_cast<const float4*>(F + static_cast<size_t>(i) * 64);
+            float y = b3;
+#pragma unroll 4
+            for (int q = 0; q < 16; ++q) {
+                const float4 f = row[q];
+                y = __fmaf_rn(S.w3[4 * q], f.x, y);
+                y = __fmaf_rn(S.w3[4 * q + 1], f.y, y);
+                y = __fmaf_rn(S.w3[4 * q + 2], f.z, y);
+                y = __fmaf_rn(S.w3[4 * q + 3], f.w, y);
+            }
+            etab[static_cast<size_t>(ci) * kNodes + i] = y;
+        }
+    }
+    if (d < 1) return;
+    __syncthreads();  // every read of the previous table is done before it is overwritten
+    // 2. feature table of date d = e-1 with the current network
+    const float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
+    const float x1 = static_cast<float>(n - d) / static_cast<float>(n);
+    if (s < 64) {
+        S.w0[s] = net[kW1 + 2 * s];
+        S.c1[s] = __fmaf_rn(net[kW1 + 2 * s + 1], x1, net[kB1 + s]);
+        S.b2[s] = net[kB2 + s];
+        for (int j = 0; j < 64; j += 2)
+            *reinterpret_cast<__nv_bfloat162*>(at(S.w2, s, j, 64)) =
+                __floats2bfloat162_rn(net[kW2 + s * 64 + j], net[kW2 + s * 64 + j + 1]);
+    }
+    if (s == 0) umma::mbar_init(&S.mbar, 1);
+    if (warp == 0) umma::tmem_alloc(&S.tmem_base, 64);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tm = S.tmem_base;
+    const NodeGrid g = node_grid(c, d);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = 0; tile < kNodes / 128 && ok; ++tile) {
+        const int i = tile * 128 + s;
+        const float u = __fmaf_rn(static_cast<float>(i), g.h, g.lo);
+        const float x0 = 4.0f * (expf(u) - 1.0f);
+        layer1_node(S.w0, S.c1, x0, S.h1, s);
+        umma::fence_smem_to_async();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (s == 0) {
+            umma::fence_after_sync();
+            for (int kk = 0; kk < 4; ++kk)
+                umma::mma_bf16(tm, desc(S.h1, 1024, kk), desc(S.w2, 1024, kk), kNodeIdesc, kk > 0);
+            umma::mma_commit(&S.mbar);
+        }
+        ok = __syncthreads_and(umma::mbar_wait(&S.mbar, phase, err, 41));
+        if (!ok) break;
+        phase ^= 1u;
+        umma::fence_after_sync();
+        float4* dst = reinterpret_cast<float4*>(F + static_cast<size_t>(i) * 64);
+        for (int cc = 0; cc < 4; ++cc) {
+            float zz[16];
+            umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, cc * 16), zz);
+#pragma unroll
+            for (int q = 0; q < 16; q += 4) {
+                float t;
+                float4 v;
+                v.x = gelu(zz[q] + S.b2[cc * 16 + q], t);
+                v.y = gelu(zz[q + 1] + S.b2[cc * 16 + q + 1], t);
+                v.z = gelu(zz[q + 2] + S.b2[cc * 16 + q + 2], t);
+                v.w = gelu(zz[q + 3] + S.b2[cc * 16 + q + 3], t);
+                dst[(cc * 16 + q) / 4] = v;
+            }
+        }
+        umma::fence_before_sync();
+        __syncthreads();  // h1 and the accumulator are reused by the next tile
+    }
+    if (!ok) umma::mbar_wait(&S.mbar, phase, err, 42);  // the MMA that timed out, once more (bounded)
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tm, 64);
+}
+
+// ---------------------------------------------------------------------------
+// Binned path pass.
+// ---------------------------------------------------------------------------
+constexpr int kBinThreads = 256;
+
+template <int PREC>
+__global__ void __launch_bounds__(kBinThreads)
+    lsm_mlp_binned(int k, int mode, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
+                   uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
+                   const int* __restrict__ snap_ok, const float* __restrict__ etab,
+                   unsigned long long* __restrict__ mom_part, Welford* __restrict__ final_part) {
+    __shared__ float tab[kNodes];                              // continuation table of date e
+    __shared__ unsigned long long mom[kMoments][kNodes];       // moments of date e-1, bin by bin
+    __shared__ Welford swf[kBinThreads / 32];
+    __shared__ Sum64 s64[kBinThreads / 32];
+    const uint32_t g = blockIdx.x;
+    if (g >= total_groups) return;
+    const uint32_t ci = group_contract[g];
+    const LsmDev c = cs[ci];
+    const int n = c.n_steps;
+    const int e = n - k;
+    if (e < 1) return;
+    const bool step = (mode & kStep) != 0;
+    const bool init = step && k == 0;
+    const bool last = step && e == 1;
+    const bool exercise = step && k > 0 && e <= n - 1 && snap_ok[c.reg_offset + e] == 1;
+    const bool gram = (mode & kGram) != 0 && e - 1 >= 1;
+    if (!step && !gram) return;
+    const int s = threadIdx.x, warp = s >> 5;
+    // Per-path arithmetic in the path precision (FP64 on the FP64 path, FP32 on
+    // the FP32 path); bins, fractions and targets in FP32.
+    using T = typename std::conditional<PREC == 0, double, float>::type;
+    const T phi = PREC == 0 ? T(c.type == 0 ? 1.0 : -1.0) : T(c.phi_f);
+    const T strike = PREC == 0 ? T(c.strike) : T(c.strike_f);
+    const T inv_k = PREC == 0 ? T(1.0 / c.strike) : T(c.inv_strike_f);
+    const T disc = PREC == 0 ? T(c.disc) : T(c.disc_f);
+    const float inv_kf = c.inv_strike_f;
+    const T* S_path = static_cast<const T*>(store) + c.s_offset;
+    T* cft = reinterpret_cast<T*>(cf) + c.cf_offset;
+    NodeGrid ge{0.0f, 0.0f, 0.0f, 0.0f}, gd{0.0f, 0.0f, 0.0f, 0.0f};
+    if (exercise) {
+        ge = node_grid(c, e);
+        for (int i = s; i < kNodes; i += kBinThreads) tab[i] = etab[static_cast<size_t>(ci) * kNodes + i];
+    }
+    float yq_scale = 0.0f;
+    if (gram) {
+        gd = node_grid(c, e - 1);
+        yq_scale = static_cast<float>(kYScale) / gd.y_bound;
+        for (int i = s; i < kMoments * kNodes; i += kBinThreads) (&mom[0][0])[i] = 0ull;
+    }
+    __syncthreads();
+    const uint32_t gl = g - c.group_begin;
+    const uint32_t chunk0 = gl * c.group_chunks;
+    const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
+    Welford w{0ull, 0.0, 0.0};
+    Sum32 fin{0u, 0.0f, 0.0f, 0.0f, 0.0f};  // FP32 path: the last date's payoffs
+    constexpr int kPer = kLsmChunk / kBinThreads;  // paths per thread and chunk
+    for (uint32_t ch = chunk0; ch < chunk1; ++ch) {
+        // every path load of this thread's kPer paths first (independent, in flight together)
+        T vv[kPer], se[kPer], sd[kPer];
+        bool live[kPer];
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + q * kBinThreads + s;
+            live[q] = i < c.path_count;
+            vv[q] = se[q] = sd[q] = T(0);
+            if (live[q]) {
+                vv[q] = init ? S_path[static_cast<uint64_t>(n - 1) * c.path_count + i] : cft[i];
+                if (exercise) se[q] = S_path[static_cast<uint64_t>(e - 1) * c.path_count + i];
+                if (gram) sd[q] = S_path[static_cast<uint64_t>(e - 2) * c.path_count + i];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            if (!live[q]) continue;
+            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + q * kBinThreads + s;
+            T v = vv[q];
+            if (init) {
+                const T x = phi * (v - strike);
+                v = x > T(0) ? x : T(0);
+            }
+            if (exercise) {
+                const T xx = phi * (se[q] - strike);
+                if (xx > T(0)) {
+                    int b;
+                    float t;
+                    locate(ge, __logf(static_cast<float>(se[q]) * inv_kf), b, t);
+                    const float cont = __fmaf_rn(t, tab[b + 1] - tab[b], tab[b]);
+                    if (cont < 0.0f) v = xx;  // predicted time value < 0: exercise
+                }
+            }
+            if (step) {
+                v *= disc;
+                if (last) {
+                    if constexpr (PREC == 0) {
+                        welford_add(w, v);
+                    } else {
+                        sum32_add(fin, v);
+                    }
+                } else {
+                    cft[i] = v;
+                }
+            }
+            if (gram) {
+                const T xx = phi * (sd[q] - strike);
+                if (xx > T(0)) {
+                    int b;
+                    float t;
+                    locate(gd, __logf(static_cast<float>(sd[q]) * inv_kf), b, t);
+                    const float y = static_cast<float>((v - xx) * inv_k);
+                    const long long tq = __float2ll_rn(t * static_cast<float>(kTScale));
+                    long long yq = __float2ll_rn(y * yq_scale);
+                    yq = yq > 16777216ll ? 16777216ll : (yq < -16777216ll ? -16777216ll : yq);
+                    atomicAdd(&mom[0][b], 1ull);
+                    atomicAdd(&mom[1][b], static_cast<unsigned long long>(tq));
+                    atomicAdd(&mom[2][b], static_cast<unsigned long long>(tq * tq));
+                    atomicAdd(&mom[3][b], static_cast<unsigned long long>(yq));
+                    atomicAdd(&mom[4][b], static_cast<unsigned long long>(tq * yq));
+                }
+            }
+        }
+        if (last) {  // one final partial per chunk, fixed tree
+            if constexpr (PREC == 0) {
+                Welford r = welford_warp_reduce(w);
+                if ((s & 31) == 0) swf[warp] = r;
+                __syncthreads();
+                if (s == 0) {
+                    Welford m = swf[0];
+                    for (int q = 1; q < kBinThreads / 32; ++q) m = welford_merge(m, swf[q]);
+                    final_part[c.chunk_begin + ch] = m;
+                }
+                w = Welford{0ull, 0.0, 0.0};
+            } else {
+                const Sum32 r = sum32_warp_reduce(fin);
+                if ((s & 31) == 0) s64[warp] = sum32_wide(r);
+                __syncthreads();
+                if (s == 0) final_part[c.chunk_begin + ch] = sum64_fold<kBinThreads / 32>(s64);
+                fin = Sum32{0u, 0.0f, 0.0f, 0.0f, 0.0f};
+            }
+            __syncthreads();
+        }
+    }
+    if (gram) {
+        __syncthreads();
+        unsigned long long* out = mom_part + static_cast<size_t>(g) * kMoments * kNodes;
+        for (int i = s; i < kMoments * kNodes; i += kBinThreads) out[i] = (&mom[0][0])[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gram matrix of [f | 1 | y] from the bin moments, one quarter of the bins
+// per CTA.  Blocks of 4 x 4 entries of the upper triangle (one per thread);
+// per bin, with A = Saa F_i + Sab F_{i+1} and B = Sab F_i + Sbb F_{i+1} on the
+// block's rows, the block gains A F_i^T + B F_{i+1}^T on its columns.
+// ---------------------------------------------------------------------------
+constexpr int kGramThreads = 256;
+constexpr int kBlocks = kFStride / 4;                         // 17 blocks of 4 indices (65 used)
+constexpr int kBlockTasks = kBlocks * (kBlocks + 1) / 2;      // upper-triangular blocks
+static_assert(kBlockTasks + kBlocks <= kGramThreads, "one task per thread");
+
+__global__ void __launch_bounds__(kGramThreads)
+    lsm_mlp_gram_slices(int k, const LsmDev* __restrict__ cs, int n_contracts,
+                        const unsigned long long* __restrict__ mom_part, const float* __restrict__ feats,
+                        float* __restrict__ gram_part) {
+    __shared__ __align__(16) float F[kBinsPerSlice + 1][kFStride];
+    __shared__ float wgt[5][kBinsPerSlice];  // Saa, Sab, Sbb, Say, Sby of each bin
+    const int ci = blockIdx.x, slice = blockIdx.y;
+    if (ci >= n_contracts) return;
+    const LsmDev c = cs[ci];
+    const int d = c.n_steps - k - 1;
+    if (d < 1) return;
+    const int s = threadIdx.x;
+    const int row0 = slice * kBinsPerSlice;
+    if (s < kBinsPerSlice) {
+        const int b = row0 + s;
+        float w[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        if (b <= kNodes - 2) {
+            unsigned long long m[kMoments] = {0ull, 0ull, 0ull, 0ull, 0ull};
+            const unsigned long long* p = mom_part + static_cast<size_t>(c.group_begin) * kMoments * kNodes + b;
+            for (uint32_t gg = 0; gg < c.n_groups; ++gg)
+#pragma unroll
+                for (int q = 0; q < kMoments; ++q) m[q] += p[(static_cast<size_t>(gg) * kMoments + q) * kNodes];
+            const double yb = static_cast<double>(node_grid(c, d).y_bound);
+            const double cnt = static_cast<double>(m[0]);
+            const double st = static_cast<double>(m[1]) / kTScale;
+            const double stt = static_cast<double>(m[2]) / (kTScale * kTScale);
+            const double sy = static_cast<double>(static_cast<long long>(m[3])) * (yb / kYScale);
+            const double sty = static_cast<double>(static_cast<long long>(m[4])) * (yb / (kTScale * kYScale));
+            w[0] = static_cast<float>(cnt - 2.0 * st + stt);  // sum (1-t)^2
+            w[1] = static_cast<float>(st - stt);              // sum t (1-t)
+            w[2] = static_cast<float>(stt);                   // sum t^2
+            w[3] = static_cast<float>(sy - sty);              // sum (1-t) y
+            w[4] = static_cast<float>(sty);                   // sum t y
+        }
+#pragma unroll
+        for (int q = 0; q < 5; ++q) wgt[q][s] = w[q];
+    }
+    // feature rows row0 .. row0 + kBinsPerSlice, with the constant 1 in column 64
+    const float* src = feats + static_cast<size_t>(ci) * kNodes * 64;
+    for (int idx = s; idx < (kBinsPerSlice + 1) * (kFStride / 4); idx += kGramThreads) {
+        const int r = idx / (kFStride / 4), q4 = idx % (kFStride / 4);
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (row0 + r < kNodes) {
+            if (q4 < 16) v = reinterpret_cast<const float4*>(src + static_cast<size_t>(row0 + r) * 64)[q4];
+            else v.x = 1.0f;
+        }
+        *reinterpret_cast<float4*>(&F[r][4 * q4]) = v;
+    }
+    __syncthreads();
+    float* out = gram_part + (static_cast<size_t>(ci) * kNodeSlices + slice) * kGramPacked;
+    if (s < kBlockTasks) {
+        int bi = 0, rem = s;  // s -> (bi, bj), bi <= bj, row-major over the upper triangle
+        while (rem >= kBlocks - bi) {
+            rem -= kBlocks - bi;
+            ++bi;
+        }
+        const int bj = bi + rem;
+        float acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = 0.0f;
+        float4 R = *reinterpret_cast<const float4*>(&F[0][4 * bi]);
+        float4 Q = *reinterpret_cast<const float4*>(&F[0][4 * bj]);
+        for (int j = 0; j < kBinsPerSlice; ++j) {
+            const float4 Rn = *reinterpret_cast<const float4*>(&F[j + 1][4 * bi]);
+            const float4 Qn = *reinterpret_cast<const float4*>(&F[j + 1][4 * bj]);
+            const float saa = wgt[0][j], sab = wgt[1][j], sbb = wgt[2][j];
+            const float r[4] = {R.x, R.y, R.z, R.w}, rn[4] = {Rn.x, Rn.y, Rn.z, Rn.w};
+            const float q[4] = {Q.x, Q.y, Q.z, Q.w}, qn[4] = {Qn.x, Qn.y, Qn.z, Qn.w};
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float A = __fmaf_rn(saa, r[a], sab * rn[a]);
+                const float B = __fmaf_rn(sab, r[a], sbb * rn[a]);
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] = __fmaf_rn(A, q[b], __fmaf_rn(B, qn[b], acc[a][b]));
+            }
+            R = Rn;
+            Q = Qn;
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int r = 4 * bi + a, q = 4 * bj + b;
+                if (r <= q && q <= 64) out[packed_index(r, q)] = acc[a][b];
+            }
+    } else if (s < kBlockTasks + kBlocks) {  // right-hand side: column 65 on rows 4 bi .. 4 bi + 3
+        const int bi = s - kBlockTasks;
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        float4 R = *reinterpret_cast<const float4*>(&F[0][4 * bi]);
+        for (int j = 0; j < kBinsPerSlice; ++j) {
+            const float4 Rn = *reinterpret_cast<const float4*>(&F[j + 1][4 * bi]);
+            const float say = wgt[3][j], sby = wgt[4][j];
+            acc[0] = __fmaf_rn(say, R.x, __fmaf_rn(sby, Rn.x, acc[0]));
+            acc[1] = __fmaf_rn(say, R.y, __fmaf_rn(sby, Rn.y, acc[1]));
+            acc[2] = __fmaf_rn(say, R.z, __fmaf_rn(sby, Rn.z, acc[2]));
+            acc[3] = __fmaf_rn(say, R.w, __fmaf_rn(sby, Rn.w, acc[3]));
+            R = Rn;
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+            if (4 * bi + a <= 64) out[packed_index(4 * bi + a, 65)] = acc[a];
+    } else if (s == kBlockTasks + kBlocks) {
+        out[packed_index(65, 65)] = 0.0f;  // sum y^2: not used by the fit
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_lsm_mlp_nodes(int precision, int k, int mode, const LsmDev* c, int n_contracts,
+                                 const uint32_t* group_contract, uint32_t total_groups, const void* store,
+                                 double* cf, const float* nets, const float* snaps, const int* snap_ok,
+                                 float* feats, float* etab, unsigned long long* mom_part, float* gram_part,
+                                 Welford* final_part, uint32_t* err, cudaStream_t stream) {
+    cudaGetLastError();
+    if (n_contracts <= 0 || total_groups == 0) return cudaSuccess;
+    lsm_mlp_nodes<<<n_contracts, 128, 0, stream>>>(k, c, n_contracts, nets, snaps, snap_ok, feats, etab, err);
+    if (precision == 0)
+        lsm_mlp_binned<0><<<total_groups, kBinThreads, 0, stream>>>(k, mode, c, group_contract, total_groups, store, cf,
+                                                                     snap_ok, etab, mom_part, final_part);
+    else
+        lsm_mlp_binned<1><<<total_groups, kBinThreads, 0, stream>>>(k, mode, c, group_contract, total_groups, store, cf,
+                                                                     snap_ok, etab, mom_part, final_part);
+    if (mode & kGram)
+        lsm_mlp_gram_slices<<<dim3(n_contracts, kNodeSlices), kGramThreads, 0, stream>>>(k, c, n_contracts, mom_part,
+                                                                                         feats, gram_part);
+    return cudaGetLastError();
+}
+
+}  // namespace mcdg
