@@ -32,7 +32,7 @@ struct LsmDev {
 };
 
 constexpr int kLsmMaxGroups = 256;  // learned-regression CTAs per contract at most
-constexpr int kLsmMinGroupChunks = 16;  // chunks per learned-regression CTA at least (amortises its set-up)
+constexpr int kLsmMinGroupChunks = 32;  // chunks per learned-regression CTA at least (amortises its set-up)
 constexpr int kGramPacked = 66 * 67 / 2;  // upper triangle of the 66 x 66 Gram matrix, row-major
 
 // Regression state of one (contract, date): T = R1^{-1} (upper triangular,

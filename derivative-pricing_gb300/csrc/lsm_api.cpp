@@ -78,10 +78,10 @@ int plan_lsm(Ctx& ctx, const mcd_lsm_contract* cs, size_t n, LsmPlan& p) {
         p.cf_elems += c.path_count;
         p.reg_rows += static_cast<uint64_t>(c.monitoring_points) + 1;
         // learned regression: at most kLsmMaxGroups CTAs per contract, each
-        // of at least kLsmMinGroupChunks chunks (a CTA's set-up -- weights,
-        // tensor memory, its Gram read-out -- is then a small share of its
-        // work); the split depends on this contract alone, so its Gram sums
-        // (and hence its price) do not depend on the rest of the batch
+        // of at least kLsmMinGroupChunks chunks (a CTA's set-up -- clearing
+        // and writing out its bin moments -- is then a small share of its
+        // work); the moments are exact integers, so the price does not depend
+        // on the split
         const uint64_t per_group =
             std::max<uint64_t>((chunks + kLsmMaxGroups - 1) / kLsmMaxGroups, kLsmMinGroupChunks);
         const uint32_t groups = static_cast<uint32_t>((chunks + per_group - 1) / per_group);

@@ -18,13 +18,14 @@
 //                   (4 x K16), weight gradient dW2 = dZ2^T H1 (8 x K16, M padded
 //                   to 128 with zero rows) -- and the CUDA cores do layers 1 and
 //                   3, the GELUs and the fixed-order reductions.
-//   lsm_mlp_pass    one CTA per group of chunks: exercise with the network
-//                   of date e, discount, and the Gram matrix of date e-1 on the
-//                   tensor core -- per 128-path tile an MMA with M = 128 (66
-//                   rows used), N = 80, K = 128 paths over
-//                   [features | 1 | target], accumulated in tensor memory.
-//   lsm_mlp_gram_reduce  one thread per Gram entry and contract: fixed-order
-//                   compensated sum of the group Gram matrices.
+//   lsm_mlp_nodes, lsm_mlp_binned, lsm_mlp_gram_slices (lsm_mlp_nodes.cu)
+//                   the fit of every date on node tables: the network at 512
+//                   values of ln(S/K) on the tensor core, paths binned with
+//                   exact integer moments, the Gram matrix of
+//                   [features | 1 | target] from the moments.
+//   lsm_mlp_pass    one CTA per group of chunks: the terminal step, and
+//                   replays of given networks with the network evaluated
+//                   path by path (Z2 = H1 W2^T on the tensor core).
 //   lsm_mlp_solve   one CTA per contract: scaled ridge Cholesky solve (65 x 65,
 //                   FP32 factor, FP64-residual refinement) for the output
 //                   layer of that date.
@@ -422,21 +423,19 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // ---------------------------------------------------------------------------
-// pass over a group of chunks: exercise at date e with the network of that
-// date, discount, final Welford (e = 1) and/or the tensor-core Gram matrix of
-// date e - 1 over [features(S_{e-1}) | 1 | time-value target]
+// Per-path step over a group of chunks: exercise at date e with the network of
+// that date evaluated path by path (layer 1 on the CUDA cores, Z2 = H1 W2^T on
+// the tensor core), discount, and the cash-flow update or, at e = 1, the final
+// Welford partial.  Used for the terminal step (k = 0: no exercise) and to
+// replay given networks (mcd_lsm_reprice_mlp); the fit itself runs on node
+// tables (lsm_mlp_nodes.cu).
 // ---------------------------------------------------------------------------
-constexpr int kGramN = 80;    // MMA N of the Gram product (66 used)
 constexpr int kGramDim = 66;  // 64 features, bias, target
 
 struct __align__(1024) PassSmem {
-    __nv_bfloat16 h1d[128 * 64];   // decision network input tile (S at date e)
-    __nv_bfloat16 h1c[128 * 64];   // current network input tile (S at date e-1)
-    __nv_bfloat16 xt[128 * 128];   // Gram operand [row][path]; rows 66..127 stay zero
+    __nv_bfloat16 h1d[128 * 64];    // network input tile (S at date e)
     __nv_bfloat16 w2d[64 * 64];
-    __nv_bfloat16 w2c[64 * 64];
-    float pd[kParamStride - 4096];  // decision network without W2: W1 b1 | b2 W3 b3
-    float pc[kParamStride - 4096];
+    float pd[kParamStride - 4096];  // network without W2: W1 b1 | b2 W3 b3
     uint64_t mbar;
     uint32_t tmem_base;
 };
@@ -453,7 +452,7 @@ __device__ void load_net(const float* __restrict__ net, float* small, __nv_bfloa
                 __floats2bfloat162_rn(net[kW2 + s * 64 + j], net[kW2 + s * 64 + j + 1]);
 }
 
-// Small-parameter offsets inside PassSmem::pd / pc.
+// Small-parameter offsets inside PassSmem::pd.
 constexpr int sW1 = kW1, sB1 = kB1, sB2 = kW2, sW3 = kW2 + (kW3 - kB2), sB3 = kW2 + (kB3 - kB2);
 
 __device__ __forceinline__ void layer1_row(const float* small, float x0, float x1, __nv_bfloat16* h1, int s) {
@@ -467,10 +466,9 @@ __device__ __forceinline__ void layer1_row(const float* small, float x0, float x
 
 template <int PREC>
 __global__ void __launch_bounds__(128)
-    lsm_mlp_pass(int k, int mode, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
+    lsm_mlp_pass(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
                  uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
-                 const float* __restrict__ nets, const float* __restrict__ snaps, const int* __restrict__ snap_ok,
-                 float* __restrict__ gram_part, Welford* __restrict__ final_part, uint4* __restrict__ feat_cache,
+                 const float* __restrict__ snaps, const int* __restrict__ snap_ok, Welford* __restrict__ final_part,
                  uint32_t* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     PassSmem& S = *reinterpret_cast<PassSmem*>(smem_raw);
@@ -482,46 +480,25 @@ __global__ void __launch_bounds__(128)
     const int n = c.n_steps;
     const int e = n - k;
     if (e < 1) return;
-    const bool step = (mode & kStep) != 0;
-    const bool init = step && k == 0;
-    const bool last = step && e == 1;
-    const bool exercise = step && k > 0 && e <= n - 1 && snap_ok[c.reg_offset + e] == 1;
-    const bool gram = (mode & kGram) != 0 && e - 1 >= 1;
-    if (!step && !gram) return;
-    // Feature cache (mode bit kCache): the hidden layers do not change between
-    // dates, so the features of S_e computed for date e's Gram matrix in the
-    // previous iteration are the decision network's features now; they are
-    // read back (BF16, exactly what the output layer was fitted on) instead of
-    // re-running layers 1 and 2, and this iteration's Gram features are
-    // stored for the next one.  One path's 64 features = 128 B, in place.
-    const bool cached = (mode & kCache) != 0;
-    const bool fill = (mode & kFill) != 0;  // store this pass's Gram features
-    const bool dec_net = exercise && !cached;  // evaluate the decision network's hidden layers
+    const bool init = k == 0;
+    const bool last = e == 1;
+    const bool exercise = k > 0 && e <= n - 1 && snap_ok[c.reg_offset + e] == 1;
     const int s = threadIdx.x, warp = s >> 5;
     const double phi = c.type == 0 ? 1.0 : -1.0;
     const double inv_k = 1.0 / c.strike;
-    const bool mma = dec_net || gram;
-    if (exercise && cached) {  // output layer only
-        const float* net = snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride;
-        for (int i = s; i < kParams - kB2; i += 128) S.pd[kW2 + i] = net[kB2 + i];
-    }
-    if (mma) {
-        if (dec_net) load_net(snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride, S.pd, S.w2d);
-        if (gram) load_net(nets + static_cast<size_t>(ci) * 3 * kParamStride, S.pc, S.w2c);
-        for (int i = s; i < 128 * 128 / 2; i += 128) reinterpret_cast<uint32_t*>(S.xt)[i] = 0u;
+    if (exercise) {
+        load_net(snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride, S.pd, S.w2d);
         if (s == 0) umma::mbar_init(&S.mbar, 1);
-        if (warp == 0) umma::tmem_alloc(&S.tmem_base, 256);
+        if (warp == 0) umma::tmem_alloc(&S.tmem_base, 64);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         umma::fence_before_sync();
         __syncthreads();
         umma::fence_after_sync();
     }
-    const uint32_t tm = mma ? S.tmem_base : 0u;
+    const uint32_t tm = exercise ? S.tmem_base : 0u;
     uint32_t phase = 0;
     bool ok = true;
-    bool gram_pending = false, gram_started = false;
     const float x1e = static_cast<float>(n - e) / static_cast<float>(n);
-    const float x1d = static_cast<float>(n - (e - 1)) / static_cast<float>(n);
     const uint32_t gl = g - c.group_begin;
     const uint32_t chunk0 = gl * c.group_chunks;
     const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
@@ -530,7 +507,7 @@ __global__ void __launch_bounds__(128)
         for (int tile = 0; tile < kLsmChunk / 128; ++tile) {
             const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + tile * 128 + s;
             const bool live = i < c.path_count;
-            double v = 0.0, ex_e = 0.0, ex_d = 0.0, s_d = 0.0;
+            double v = 0.0, ex_e = 0.0;
             if (live) {
                 if (init) {
                     const double sT = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(n - 1) * c.path_count + i);
@@ -540,7 +517,6 @@ __global__ void __launch_bounds__(128)
                     v = cf_load<PREC>(cf, c.cf_offset + i);
                 }
             }
-            float yhat_cached = 0.0f;
             if (exercise) {
                 float x0 = 0.0f;
                 if (live) {
@@ -549,115 +525,37 @@ __global__ void __launch_bounds__(128)
                     ex_e = xx > 0.0 ? xx : 0.0;
                     x0 = static_cast<float>(4.0 * (se * inv_k - 1.0));
                 }
-                if (dec_net) {
-                    layer1_row(S.pd, x0, x1e, S.h1d, s);
-                } else if (live && ex_e > 0.0) {  // cached features: output layer only
-                    const uint4* src = feat_cache + (c.cf_offset + i) * 8;
-                    float yh = S.pd[sB3];
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        const uint4 u = src[q];
-                        const uint32_t words[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-                        for (int h = 0; h < 4; ++h) {
-                            const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&words[h]));
-                            yh = __fmaf_rn(S.pd[sW3 + q * 8 + 2 * h], f.x, yh);
-                            yh = __fmaf_rn(S.pd[sW3 + q * 8 + 2 * h + 1], f.y, yh);
-                        }
-                    }
-                    yhat_cached = yh;
-                }
-            }
-            if (gram) {
-                float x0 = 0.0f;
-                if (live) {
-                    s_d = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 2) * c.path_count + i);
-                    const double xx = phi * (s_d - c.strike);
-                    ex_d = xx > 0.0 ? xx : 0.0;
-                    x0 = static_cast<float>(4.0 * (s_d * inv_k - 1.0));
-                }
-                layer1_row(S.pc, x0, x1d, S.h1c, s);
-            }
-            if (mma) {
+                layer1_row(S.pd, x0, x1e, S.h1d, s);
                 umma::fence_smem_to_async();
                 umma::fence_before_sync();
                 __syncthreads();
                 if (s == 0) {
                     umma::fence_after_sync();
-                    if (dec_net)
-                        for (int kk = 0; kk < 4; ++kk)
-                            umma::mma_bf16(tm, desc(S.h1d, 1024, kk), desc(S.w2d, 1024, kk), kIdesc, kk > 0);
-                    if (gram)
-                        for (int kk = 0; kk < 4; ++kk)
-                            umma::mma_bf16(tm + 64, desc(S.h1c, 1024, kk), desc(S.w2c, 1024, kk), kIdesc, kk > 0);
-                    umma::mma_commit(&S.mbar);  // also covers the previous tile's Gram MMA
+                    for (int kk = 0; kk < 4; ++kk)
+                        umma::mma_bf16(tm, desc(S.h1d, 1024, kk), desc(S.w2d, 1024, kk), kIdesc, kk > 0);
+                    umma::mma_commit(&S.mbar);
                 }
                 ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 11));
                 phase ^= 1u;
-                gram_pending = false;
                 umma::fence_after_sync();
-            }
-            if (exercise) {
-                float yhat = yhat_cached;
-                if (dec_net) {
-                    yhat = S.pd[sB3];
-                    for (int cc = 0; cc < 4; ++cc) {
-                        float zz[16];
-                        umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, cc * 16), zz);
-                        for (int q = 0; q < 16; ++q) {
-                            float t;
-                            yhat = __fmaf_rn(S.pd[sW3 + cc * 16 + q], gelu(zz[q] + S.pd[sB2 + cc * 16 + q], t), yhat);
-                        }
+                float yhat = S.pd[sB3];
+                for (int cc = 0; cc < 4; ++cc) {
+                    float zz[16];
+                    umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, cc * 16), zz);
+                    for (int q = 0; q < 16; ++q) {
+                        float t;
+                        yhat = __fmaf_rn(S.pd[sW3 + cc * 16 + q], gelu(zz[q] + S.pd[sB2 + cc * 16 + q], t), yhat);
                     }
                 }
                 // predicted time value < 0: exercise
                 if (live && ok && ex_e > 0.0 && yhat < 0.0f) v = ex_e;
+                umma::fence_before_sync();
+                __syncthreads();  // the input tile and the accumulator are reused by the next tile
             }
-            if (live && step) {
+            if (live) {
                 v *= c.disc;
                 if (last) welford_add(w, v);
                 else cf_store<PREC>(cf, c.cf_offset + i, v);
-            }
-            if (gram) {
-                const bool itm = live && ex_d > 0.0;
-                const float y = itm ? static_cast<float>((v - ex_d) * inv_k) : 0.0f;
-                uint4* dst = fill && itm ? feat_cache + (c.cf_offset + i) * 8 : nullptr;
-                for (int cc = 0; cc < 4; ++cc) {
-                    float zz[16];
-                    umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 64 + cc * 16), zz);
-                    uint32_t packed[8];
-#pragma unroll
-                    for (int q = 0; q < 16; q += 2) {
-                        float t;
-                        const float ha = itm ? gelu(zz[q] + S.pc[sB2 + cc * 16 + q], t) : 0.0f;
-                        const float hb = itm ? gelu(zz[q + 1] + S.pc[sB2 + cc * 16 + q + 1], t) : 0.0f;
-                        const __nv_bfloat162 hp = __floats2bfloat162_rn(ha, hb);
-                        *at(S.xt, cc * 16 + q, s, 128) = hp.x;
-                        *at(S.xt, cc * 16 + q + 1, s, 128) = hp.y;
-                        packed[q / 2] = *reinterpret_cast<const uint32_t*>(&hp);
-                    }
-                    if (dst) {  // the decision features of this date, for the next iteration
-                        dst[2 * cc] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                        dst[2 * cc + 1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-                    }
-                }
-                *at(S.xt, 64, s, 128) = __float2bfloat16_rn(itm ? 1.0f : 0.0f);
-                *at(S.xt, 65, s, 128) = __float2bfloat16_rn(y);
-                umma::fence_smem_to_async();
-                umma::fence_before_sync();
-                __syncthreads();
-                if (s == 0) {
-                    umma::fence_after_sync();
-                    // D[i][j] += sum_paths xt[i][p] xt[j][p]  (M = 128 rows, N = 80)
-                    for (int kk = 0; kk < 8; ++kk)
-                        umma::mma_bf16(tm + 128, desc(S.xt, 2048, kk), desc(S.xt, 2048, kk),
-                                       umma::idesc_bf16(128, kGramN), gram_started || kk > 0);
-                }
-                gram_started = true;
-                gram_pending = true;
-            } else if (mma) {
-                umma::fence_before_sync();
-                __syncthreads();  // h1 tiles and accumulators are reused by the next tile
             }
         }
         if (last) {  // one final partial per chunk, fixed tree
@@ -669,32 +567,11 @@ __global__ void __launch_bounds__(128)
             w = Welford{0ull, 0.0, 0.0};
         }
     }
-    if (mma) {
-        if (gram_pending) {
-            if (s == 0) umma::mma_commit(&S.mbar);
-            ok = __syncthreads_and(ok && umma::mbar_wait(&S.mbar, phase, err, 12));
-            phase ^= 1u;
-            umma::fence_after_sync();
-        }
-        if (gram) {
-            float* out = gram_part + static_cast<size_t>(g) * kGramPacked;
-            if (warp < 3) {  // lanes 0..95 hold rows 0..95; the upper triangle of rows 0..65 is kept
-                const int row0 = s * kGramDim - s * (s - 1) / 2;  // packed index of (s, s)
-                for (int cc = 0; cc < 5; ++cc) {
-                    float dd[16];
-                    umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 128 + cc * 16), dd);
-                    if (s < kGramDim)
-                        for (int q = 0; q < 16; ++q) {
-                            const int col = cc * 16 + q;
-                            if (col >= s && col < kGramDim) out[row0 + col - s] = ok ? dd[q] : 0.0f;
-                        }
-                }
-            }
-        }
+    if (exercise) {
         if (!ok) umma::mbar_wait(&S.mbar, phase, err, 13);
         umma::fence_before_sync();
         __syncthreads();
-        if (warp == 0) umma::tmem_dealloc(tm, 256);
+        if (warp == 0) umma::tmem_dealloc(tm, 64);
     }
 }
 
@@ -702,13 +579,13 @@ __global__ void __launch_bounds__(128)
 // output layer of date d = n - k - 1: ridge least squares on the Gram matrix
 //
 // The 64 GELU features are smooth functions of one state variable and are
-// strongly collinear, and the Gram matrix is accumulated in FP32 by the
-// tensor cores, so it is only positive semi-definite to a small fraction of
-// its diagonal.  The regressors are therefore scaled to unit diagonal and a
-// ridge of kRidge is added in those units; a pivot that still falls below
-// half the ridge drops its regressor (coefficient 0) instead of failing the
-// date.  FP64 is slow on this part, so the group partials are summed in FP32
-// with compensation (lsm_mlp_gram_reduce), the 65 x 65 Cholesky factor is
+// strongly collinear, and the Gram matrix is accumulated in FP32, so it is
+// only positive semi-definite to a small fraction of its diagonal.  The
+// regressors are therefore scaled to unit diagonal and a ridge of kRidge is
+// added in those units; a pivot that still falls below half the ridge drops
+// its regressor (coefficient 0) instead of failing the date.  The partials of
+// the bin slices (lsm_mlp_gram_slices) are summed in FP64 in order; FP64
+// is slow on this part, so the 65 x 65 Cholesky factor is
 // computed in FP32 (every thread keeps its share of the triangle in
 // registers; one barrier per column), and two steps of iterative refinement
 // with FP64 residuals bring the solution to FP64 accuracy for the
@@ -763,7 +640,7 @@ __global__ void __launch_bounds__(kSolveThreads)
     const int d = c.n_steps - k - 1;
     if (d < 1) return;
     const int s = threadIdx.x, lane = s & 31, warp = s >> 5;
-    for (int idx = s; idx < kGramPacked; idx += kSolveThreads) {  // the bin quarters' partials, in order
+    for (int idx = s; idx < kGramPacked; idx += kSolveThreads) {  // the bin slices' partials, in order
         const float* p = gram_part + static_cast<size_t>(ci) * kNodeSlices * kGramPacked + idx;
         double v = 0.0;
         for (int sl = 0; sl < kNodeSlices; ++sl) v += static_cast<double>(p[static_cast<size_t>(sl) * kGramPacked]);
@@ -1027,15 +904,13 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
     cudaGetLastError();
     if (total_groups == 0) return cudaSuccess;
     const size_t pass_smem = sizeof(PassSmem);
-    auto pass = [&](int mode) {  // the per-path network: terminal step, and replays of a given policy
+    auto step = [&]() {  // the per-path network: terminal step, and replays of given networks
         if (precision == 0)
-            lsm_mlp_pass<0><<<total_groups, 128, pass_smem, stream>>>(k, mode, c, group_contract, total_groups, store,
-                                                                      cf, nets, snaps, snap_ok, gram_part, final_part,
-                                                                      nullptr, err);
+            lsm_mlp_pass<0><<<total_groups, 128, pass_smem, stream>>>(k, c, group_contract, total_groups, store, cf,
+                                                                      snaps, snap_ok, final_part, err);
         else
-            lsm_mlp_pass<1><<<total_groups, 128, pass_smem, stream>>>(k, mode, c, group_contract, total_groups, store,
-                                                                      cf, nets, snaps, snap_ok, gram_part, final_part,
-                                                                      nullptr, err);
+            lsm_mlp_pass<1><<<total_groups, 128, pass_smem, stream>>>(k, c, group_contract, total_groups, store, cf,
+                                                                      snaps, snap_ok, final_part, err);
     };
     auto trainer = [&]() {
         if (precision == 0)
@@ -1046,12 +921,12 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
                                                                               snap_ok, adam_t, cfg, err);
     };
     if (!train) {
-        pass(kStep);
+        step();
         return cudaGetLastError();
     }
     int mode = kStep | kGram;  // exercise at date e, discount, regression data of date e-1
     if (k == 0) {
-        pass(kStep);  // terminal cash flows, first discount
+        step();       // terminal cash flows, first discount
         trainer();    // learn the features on the latest date
         mode = kGram;
     }

@@ -20,9 +20,8 @@ struct MlpConfig {
 };
 
 // Pass modes: kStep = exercise, discount and cash-flow update at date n-k;
-// kGram = regression data of date n-k-1; kCache / kFill: the per-path decision
-// kernel's feature reuse.
-enum PassMode { kStep = 1, kGram = 2, kCache = 4, kFill = 8 };
+// kGram = regression data of date n-k-1.
+enum PassMode { kStep = 1, kGram = 2 };
 
 // Node tables.  The network's inputs are x0 = 4 (S/K - 1) and the date's time
 // input, which is one value per date, so at a date every learned feature is a
@@ -33,7 +32,7 @@ enum PassMode { kStep = 1, kGram = 2, kCache = 4, kFill = 8 };
 // features, built from per-bin moments of the paths) and for its exercise
 // decision (an interpolated continuation table).
 constexpr int kNodes = 512;
-constexpr int kNodeSlices = 4;                       // Gram CTAs per contract (bins split in four)
+constexpr int kNodeSlices = kNodes / 128;           // Gram CTAs per contract (128 bins each)
 constexpr int kMoments = 5;                          // per bin: n, sum t, sum t^2, sum y, sum t y
 constexpr double kTScale = 65536.0;                  // t in [0, 1] as an integer of 16 bits
 constexpr double kYScale = 16777216.0;               // |y| / y_bound as an integer of 24 bits

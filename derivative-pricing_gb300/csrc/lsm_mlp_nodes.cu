@@ -14,7 +14,7 @@
 //                        fitted at e), then the feature table F of date e-1:
 //                        layer 1 on the CUDA cores, Z2 = H1 W2^T on the tensor
 //                        core (tcgen05, BF16 operands, FP32 accumulator in
-//                        tensor memory), GELU; four 128-node tiles.
+//                        tensor memory), GELU; 128-node tiles.
 //   lsm_mlp_binned       one CTA per group of chunks: exercise at date e where
 //                        the interpolated continuation value is negative,
 //                        discount, cash-flow update, and for the paths in the
@@ -29,7 +29,7 @@
 //                        G = sum over bins of (1-t)^2 F_i F_i^T + t(1-t)
 //                        (F_i F_{i+1}^T + F_{i+1} F_i^T) + t^2 F_{i+1} F_{i+1}^T
 //                        (and the right-hand side likewise), one partial per
-//                        quarter of the bins; lsm_mlp_solve sums the four.
+//                        128 bins; lsm_mlp_solve sums them in order.
 //
 // The least-squares fit over the interpolated features is exact (no path is
 // left out and no feature rounded to BF16 on its way to the Gram matrix); the
@@ -362,8 +362,7 @@ __global__ void __launch_bounds__(kBinThreads)
 }
 
 // ---------------------------------------------------------------------------
-// Gram matrix of [f | 1 | y] from the bin moments, one quarter of the bins
-// per CTA.  Blocks of 4 x 4 entries of the upper triangle (one per thread);
+// Gram matrix of [f | 1 | y] from the bin moments, 128 bins per CTA.  Blocks of 4 x 4 entries of the upper triangle (one per thread);
 // per bin, with A = Saa F_i + Sab F_{i+1} and B = Sab F_i + Sbb F_{i+1} on the
 // block's rows, the block gains A F_i^T + B F_{i+1}^T on its columns.
 // ---------------------------------------------------------------------------

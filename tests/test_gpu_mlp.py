@@ -145,3 +145,23 @@ def test_learned_batch_matches_single(engine):
         one = engine.monte_carlo_lsm_american(*c, precision="fp32", regression="mlp")
         assert batch[i]["price"] == one.price, (i, batch[i]["price"], one.price)
         assert batch[i]["reserved"] == one.reserved
+
+
+@pytest.mark.parametrize("case", [(40, 40, .06, 0, .2, 1.0, 1), (36, 40, .06, 0, .4, 2.0, 1),
+                                  (100, 100, .05, .08, .3, 1.0, 0)])
+def test_node_tables_agree_with_the_network_path_by_path(engine, case):
+    """The fit decides exercise from node tables (each date's network at 512
+    values of ln(S/K), interpolated); replaying the fitted networks path by path
+    (mcd_lsm_reprice_mlp) on the same paths changes only decisions of paths that
+    are nearly indifferent between exercising and holding.  Their realised cash
+    flows move the in-sample price by a fraction of a standard error (0.05-0.3
+    SE here, not shrinking with finer tables: about what the in-sample price
+    moves when the basis changes at all), never by a standard error."""
+    s, k, r, q, v, t, ty = case
+    paths, n = 1 << 17, 50
+    res = engine.monte_carlo_lsm_american(s, k, r, q, v, t, ty, n, paths, 42, precision="fp32", regression="mlp")
+    assert res.reserved == 0
+    w, has = engine.mlp_policy(0, n)
+    same = engine.reprice_mlp(s, k, r, q, v, t, ty, n, paths, 42, w, has, "fp32")
+    print(case, res.price, same.price, (same.price - res.price) / res.standard_error)
+    assert abs(same.price - res.price) < 0.5 * res.standard_error
