@@ -605,23 +605,46 @@ __device__ __forceinline__ int packed_index(int r, int q) {  // r <= q
 }
 
 // x = L^-T L^-1 b for the FP32 factor L (lower, row stride kGramDim,
-// reciprocal diagonal in inv_diag), by one warp on shared vectors: b is
-// overwritten, the solution lands in x.  Dropped regressors give 0 (their
-// inv_diag is 0).
-__device__ void chol_solve_warp(const float* L, const float* inv_diag, float* b, float* z, float* x, int lane) {
+// reciprocal diagonal in inv_diag) by one warp: lane l keeps entries l, l+32
+// and l+64 of the vector in registers (z, then x, replace b in place) and
+// each pivot value is broadcast by a shuffle.  b is rhs rounded to FP32; x is
+// added to acc in FP64.  Dropped regressors give 0 (their inv_diag is 0).
+__device__ void chol_solve_warp(const float* L, const float* inv_diag, const double* rhs, double* acc, int lane) {
+    constexpr int kSlots = (kM + 31) / 32;
+    static_assert(kSlots == 3, "three entries per lane");
+    float v[kSlots];
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) {
+        const int r = lane + 32 * q;
+        v[q] = r < kM ? static_cast<float>(rhs[r]) : 0.0f;
+    }
     for (int i = 0; i < kM; ++i) {  // L z = b, column by column
-        __syncwarp();
-        const float zi = b[i] * inv_diag[i];
-        if (lane == 0) z[i] = zi;
-        for (int r = i + 1 + lane; r < kM; r += 32) b[r] = __fmaf_rn(-L[r * kGramDim + i], zi, b[r]);
+        const int qi = i >> 5;
+        const float mine = qi == 0 ? v[0] : (qi == 1 ? v[1] : v[2]);
+        const float zi = __shfl_sync(0xffffffffu, mine * inv_diag[i], i & 31);
+#pragma unroll
+        for (int q = 0; q < kSlots; ++q) {
+            const int r = lane + 32 * q;
+            if (r == i) v[q] = zi;
+            else if (r > i && r < kM) v[q] = __fmaf_rn(-L[r * kGramDim + i], zi, v[q]);
+        }
     }
     for (int i = kM - 1; i >= 0; --i) {  // L^T x = z
-        __syncwarp();
-        const float xi = z[i] * inv_diag[i];
-        if (lane == 0) x[i] = xi;
-        for (int r = lane; r < i; r += 32) z[r] = __fmaf_rn(-L[i * kGramDim + r], xi, z[r]);
+        const int qi = i >> 5;
+        const float mine = qi == 0 ? v[0] : (qi == 1 ? v[1] : v[2]);
+        const float xi = __shfl_sync(0xffffffffu, mine * inv_diag[i], i & 31);
+#pragma unroll
+        for (int q = 0; q < kSlots; ++q) {
+            const int r = lane + 32 * q;
+            if (r == i) v[q] = xi;
+            else if (r < i) v[q] = __fmaf_rn(-L[i * kGramDim + r], xi, v[q]);
+        }
     }
-    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) {
+        const int r = lane + 32 * q;
+        if (r < kM) acc[r] += static_cast<double>(v[q]);
+    }
 }
 
 __global__ void __launch_bounds__(kSolveThreads)
@@ -631,7 +654,6 @@ __global__ void __launch_bounds__(kSolveThreads)
     __shared__ float L[kM * kGramDim];  // FP32 Cholesky factor (lower)
     __shared__ float col[2][kM];        // column j of the partially reduced matrix (double-buffered)
     __shared__ float inv_diag[kM];
-    __shared__ float vb[kM], vz[kM], vx[kM];
     __shared__ double sc[kM], xs[kM], res[kM];
     __shared__ int bad;
     const int ci = blockIdx.x;
@@ -707,11 +729,7 @@ __global__ void __launch_bounds__(kSolveThreads)
     if (s < kM) res[s] = G[packed_index(s, 65)];
     __syncthreads();
     for (int it = 0; it < 3; ++it) {
-        if (warp == 0) {
-            for (int i = lane; i < kM; i += 32) vb[i] = static_cast<float>(res[i]);
-            chol_solve_warp(L, inv_diag, vb, vz, vx, lane);
-            for (int i = lane; i < kM; i += 32) xs[i] += static_cast<double>(vx[i]);
-        }
+        if (warp == 0) chol_solve_warp(L, inv_diag, res, xs, lane);
         __syncthreads();
         if (it == 2) break;
         for (int i = warp; i < kM; i += kSolveThreads / 32) {  // one warp per row

@@ -92,6 +92,7 @@ struct __align__(1024) NodeSmem {
     __align__(16) float c1[64];  // fma(W1[j][1], x1, b1[j]) at the date's time input
     float b2[64];
     float w3[64];
+    NodeGrid grid;
     uint64_t mbar;
     uint32_t tmem_base;
 };
@@ -160,14 +161,17 @@ __global__ void __launch_bounds__(128)
             *reinterpret_cast<__nv_bfloat162*>(at(S.w2, s, j, 64)) =
                 __floats2bfloat162_rn(net[kW2 + s * 64 + j], net[kW2 + s * 64 + j + 1]);
     }
-    if (s == 0) umma::mbar_init(&S.mbar, 1);
+    if (s == 0) {
+        umma::mbar_init(&S.mbar, 1);
+        S.grid = node_grid(c, d);  // FP64 library calls: once per CTA
+    }
     if (warp == 0) umma::tmem_alloc(&S.tmem_base, 64);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tm = S.tmem_base;
-    const NodeGrid g = node_grid(c, d);
+    const NodeGrid g = S.grid;
     uint32_t phase = 0;
     bool ok = true;
     for (int tile = 0; tile < kNodes / 128 && ok; ++tile) {
@@ -215,10 +219,10 @@ __global__ void __launch_bounds__(128)
 // ---------------------------------------------------------------------------
 // Binned path pass.
 // ---------------------------------------------------------------------------
-constexpr int kBinThreads = 256;
+constexpr int kBinThreads = 256;  // five CTAs per SM (48 registers): latency-bound on the shared-memory atomics
 
 template <int PREC>
-__global__ void __launch_bounds__(kBinThreads)
+__global__ void __launch_bounds__(kBinThreads, 5)
     lsm_mlp_binned(int k, int mode, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
                    uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
                    const int* __restrict__ snap_ok, const float* __restrict__ etab,
@@ -227,6 +231,7 @@ __global__ void __launch_bounds__(kBinThreads)
     __shared__ unsigned long long mom[kMoments][kNodes];       // moments of date e-1, bin by bin
     __shared__ Welford swf[kBinThreads / 32];
     __shared__ Sum64 s64[kBinThreads / 32];
+    __shared__ NodeGrid s_grid[2];                             // dates e and e-1
     const uint32_t g = blockIdx.x;
     if (g >= total_groups) return;
     const uint32_t ci = group_contract[g];
@@ -251,18 +256,17 @@ __global__ void __launch_bounds__(kBinThreads)
     const float inv_kf = c.inv_strike_f;
     const T* S_path = static_cast<const T*>(store) + c.s_offset;
     T* cft = reinterpret_cast<T*>(cf) + c.cf_offset;
-    NodeGrid ge{0.0f, 0.0f, 0.0f, 0.0f}, gd{0.0f, 0.0f, 0.0f, 0.0f};
-    if (exercise) {
-        ge = node_grid(c, e);
+    if (s == 0) {  // FP64 library calls: once per CTA
+        s_grid[0] = exercise ? node_grid(c, e) : NodeGrid{0.0f, 0.0f, 0.0f, 1.0f};
+        s_grid[1] = gram ? node_grid(c, e - 1) : NodeGrid{0.0f, 0.0f, 0.0f, 1.0f};
+    }
+    if (exercise)
         for (int i = s; i < kNodes; i += kBinThreads) tab[i] = etab[static_cast<size_t>(ci) * kNodes + i];
-    }
-    float yq_scale = 0.0f;
-    if (gram) {
-        gd = node_grid(c, e - 1);
-        yq_scale = static_cast<float>(kYScale) / gd.y_bound;
+    if (gram)
         for (int i = s; i < kMoments * kNodes; i += kBinThreads) (&mom[0][0])[i] = 0ull;
-    }
     __syncthreads();
+    const NodeGrid ge = s_grid[0], gd = s_grid[1];
+    const float yq_scale = static_cast<float>(kYScale) / gd.y_bound;
     const uint32_t gl = g - c.group_begin;
     const uint32_t chunk0 = gl * c.group_chunks;
     const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
@@ -377,6 +381,7 @@ __global__ void __launch_bounds__(kGramThreads)
                         float* __restrict__ gram_part) {
     __shared__ __align__(16) float F[kBinsPerSlice + 1][kFStride];
     __shared__ float wgt[5][kBinsPerSlice];  // Saa, Sab, Sbb, Say, Sby of each bin
+    __shared__ double s_yb;
     const int ci = blockIdx.x, slice = blockIdx.y;
     if (ci >= n_contracts) return;
     const LsmDev c = cs[ci];
@@ -384,6 +389,8 @@ __global__ void __launch_bounds__(kGramThreads)
     if (d < 1) return;
     const int s = threadIdx.x;
     const int row0 = slice * kBinsPerSlice;
+    if (s == 0) s_yb = static_cast<double>(node_grid(c, d).y_bound);  // FP64 library calls: once per CTA
+    __syncthreads();
     if (s < kBinsPerSlice) {
         const int b = row0 + s;
         float w[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -393,7 +400,7 @@ __global__ void __launch_bounds__(kGramThreads)
             for (uint32_t gg = 0; gg < c.n_groups; ++gg)
 #pragma unroll
                 for (int q = 0; q < kMoments; ++q) m[q] += p[(static_cast<size_t>(gg) * kMoments + q) * kNodes];
-            const double yb = static_cast<double>(node_grid(c, d).y_bound);
+            const double yb = s_yb;
             const double cnt = static_cast<double>(m[0]);
             const double st = static_cast<double>(m[1]) / kTScale;
             const double stt = static_cast<double>(m[2]) / (kTScale * kTScale);
