@@ -598,14 +598,14 @@ constexpr double kRidge = 1e-3;
 constexpr int kSolveThreads = 256;
 constexpr int kM = kGramDim - 1;                                      // 65 regressors (64 features + bias)
 constexpr int kTri = kM * (kM + 1) / 2;                               // lower triangle of the 65 x 65 system
-constexpr int kOwn = (kTri + kSolveThreads - 1) / kSolveThreads;      // triangle entries per thread
 
 __device__ __forceinline__ int packed_index(int r, int q) {  // r <= q
     return r * kGramDim - r * (r - 1) / 2 + (q - r);
 }
 
-// x = L^-T L^-1 b for the FP32 factor L (lower, row stride kGramDim,
-// reciprocal diagonal in inv_diag) by one warp: lane l keeps entries l, l+32
+// x = L^-T L^-1 b for the FP32 factor L, stored transposed in the upper
+// triangle of W (L[r][i] at W[i * kGramDim + r], r > i) with the reciprocal
+// diagonal in inv_diag, by one warp: lane l keeps entries l, l+32
 // and l+64 of the vector in registers (z, then x, replace b in place) and
 // each pivot value is broadcast by a shuffle.  b is rhs rounded to FP32; x is
 // added to acc in FP64.  Dropped regressors give 0 (their inv_diag is 0).
@@ -626,7 +626,7 @@ __device__ void chol_solve_warp(const float* L, const float* inv_diag, const dou
         for (int q = 0; q < kSlots; ++q) {
             const int r = lane + 32 * q;
             if (r == i) v[q] = zi;
-            else if (r > i && r < kM) v[q] = __fmaf_rn(-L[r * kGramDim + i], zi, v[q]);
+            else if (r > i && r < kM) v[q] = __fmaf_rn(-L[i * kGramDim + r], zi, v[q]);
         }
     }
     for (int i = kM - 1; i >= 0; --i) {  // L^T x = z
@@ -637,7 +637,7 @@ __device__ void chol_solve_warp(const float* L, const float* inv_diag, const dou
         for (int q = 0; q < kSlots; ++q) {
             const int r = lane + 32 * q;
             if (r == i) v[q] = xi;
-            else if (r < i) v[q] = __fmaf_rn(-L[i * kGramDim + r], xi, v[q]);
+            else if (r < i) v[q] = __fmaf_rn(-L[r * kGramDim + i], xi, v[q]);
         }
     }
 #pragma unroll
@@ -651,8 +651,7 @@ __global__ void __launch_bounds__(kSolveThreads)
     lsm_mlp_solve(int k, const LsmDev* __restrict__ cs, int n_contracts, const float* __restrict__ gram_part,
                   float* __restrict__ nets, float* __restrict__ snaps, int* __restrict__ snap_ok) {
     __shared__ double G[kGramPacked];   // Gram matrix, packed upper triangle; standardised in place
-    __shared__ float L[kM * kGramDim];  // FP32 Cholesky factor (lower)
-    __shared__ float col[2][kM];        // column j of the partially reduced matrix (double-buffered)
+    __shared__ float L[kM * kGramDim];  // FP32: working lower triangle; the factor, transposed, above it
     __shared__ float inv_diag[kM];
     __shared__ double sc[kM], xs[kM], res[kM];
     __shared__ int bad;
@@ -680,47 +679,35 @@ __global__ void __launch_bounds__(kSolveThreads)
         sc[s] = a > 0.0 ? 1.0 / sqrt(a) : 0.0;  // a feature that is zero on every path gets coefficient 0
     }
     __syncthreads();
-    // Owned entries (r, q), q <= r, of the lower triangle, standardised, in
-    // registers; the packed FP64 copy is standardised too (for residuals).
-    int own_r[kOwn], own_q[kOwn];
-    float a[kOwn];
-#pragma unroll
-    for (int u = 0; u < kOwn; ++u) {
-        const int e = s + kSolveThreads * u;
-        own_r[u] = -1;
-        own_q[u] = -1;
-        a[u] = 0.0f;
-        if (e < kTri) {
-            int r = static_cast<int>((sqrtf(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
-            while (r * (r + 1) / 2 > e) --r;
-            while ((r + 1) * (r + 2) / 2 <= e) ++r;
-            const int q = e - r * (r + 1) / 2;
-            const int pi = packed_index(q, r);
-            double v = G[pi] * sc[r] * sc[q];
-            if (q == r) v = (sc[r] > 0.0 ? 1.0 : 0.0) + kRidge;
-            G[pi] = v;
-            own_r[u] = r;
-            own_q[u] = q;
-            a[u] = static_cast<float>(v);
-        }
+    // The lower triangle, standardised, as FP32 in L; the packed FP64 copy is
+    // standardised too (for the residuals).
+    for (int e = s; e < kTri; e += kSolveThreads) {
+        int r = static_cast<int>((sqrtf(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
+        while (r * (r + 1) / 2 > e) --r;
+        while ((r + 1) * (r + 2) / 2 <= e) ++r;
+        const int q = e - r * (r + 1) / 2;
+        const int pi = packed_index(q, r);
+        double v = G[pi] * sc[r] * sc[q];
+        if (q == r) v = (sc[r] > 0.0 ? 1.0 : 0.0) + kRidge;
+        G[pi] = v;
+        L[r * kGramDim + q] = static_cast<float>(v);
     }
     if (s < kM) G[packed_index(s, 65)] *= sc[s];  // right-hand side
-    // right-looking Cholesky in FP32 on the owned entries, one barrier per column
+    // Right-looking Cholesky in FP32, one barrier per column: at column j every
+    // warp updates its rows r > j (lanes over the columns j < q <= r) with
+    // column j of the reduced matrix, and row j of the upper triangle receives
+    // the factor's column j (read by nobody else during the step).
     for (int j = 0; j < kM; ++j) {
-        float* cj = col[j & 1];
-#pragma unroll
-        for (int u = 0; u < kOwn; ++u)
-            if (own_q[u] == j) cj[own_r[u]] = a[u];
         __syncthreads();
-        const float dj = cj[j];
+        const float dj = L[j * kGramDim + j];
         const bool drop = !(dj >= static_cast<float>(0.5 * kRidge));
         const float inv = drop ? 0.0f : rsqrtf(dj);
-#pragma unroll
-        for (int u = 0; u < kOwn; ++u) {
-            const int r = own_r[u], q = own_q[u];
-            if (q > j) a[u] = __fmaf_rn(-(cj[r] * inv), cj[q] * inv, a[u]);
-            else if (q == j) L[r * kGramDim + j] = r == j ? (drop ? 1.0f : dj * inv) : cj[r] * inv;
+        for (int r = j + 1 + warp; r < kM; r += kSolveThreads / 32) {
+            const float lr = L[r * kGramDim + j] * inv;
+            for (int q = j + 1 + lane; q <= r; q += 32)
+                L[r * kGramDim + q] = __fmaf_rn(-lr, L[q * kGramDim + j] * inv, L[r * kGramDim + q]);
         }
+        if (s > j && s < kM) L[j * kGramDim + s] = L[s * kGramDim + j] * inv;
         if (s == 0) inv_diag[j] = inv;  // 1 / L[j][j], 0 when the regressor is dropped
     }
     __syncthreads();
