@@ -326,14 +326,16 @@ __global__ void __launch_bounds__(kBinThreads, 5)
                     float t;
                     locate(gd, __logf(static_cast<float>(sd[q]) * inv_kf), b, t);
                     const float y = static_cast<float>((v - xx) * inv_k);
-                    const long long tq = __float2ll_rn(t * static_cast<float>(kTScale));
-                    long long yq = __float2ll_rn(y * yq_scale);
-                    yq = yq > 16777216ll ? 16777216ll : (yq < -16777216ll ? -16777216ll : yq);
+                    // 32-bit conversions (a 64-bit one would run on the FP64 unit), widened by
+                    // integer products: tq in [0, 2^16], |yq| <= 2^24
+                    const int tq = __float2int_rn(t * static_cast<float>(kTScale));
+                    const int yq = min(max(__float2int_rn(fminf(fmaxf(y * yq_scale, -16777216.0f), 16777216.0f)),
+                                           -16777216), 16777216);
                     atomicAdd(&mom[0][b], 1ull);
                     atomicAdd(&mom[1][b], static_cast<unsigned long long>(tq));
-                    atomicAdd(&mom[2][b], static_cast<unsigned long long>(tq * tq));
-                    atomicAdd(&mom[3][b], static_cast<unsigned long long>(yq));
-                    atomicAdd(&mom[4][b], static_cast<unsigned long long>(tq * yq));
+                    atomicAdd(&mom[2][b], static_cast<unsigned long long>(static_cast<long long>(tq) * tq));
+                    atomicAdd(&mom[3][b], static_cast<unsigned long long>(static_cast<long long>(yq)));
+                    atomicAdd(&mom[4][b], static_cast<unsigned long long>(static_cast<long long>(tq) * yq));
                 }
             }
         }
