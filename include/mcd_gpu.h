@@ -275,9 +275,14 @@ int mcd_lsm_batch(mcd_ctx* ctx, const mcd_lsm_contract* contracts, size_t n, int
  * BF16 tensor-core forward/backward with FP32 accumulation) at the latest
  * exercise date; its 64 hidden features plus a bias are then the regression
  * basis at every date, whose output layer is fitted by ridge least squares
- * over all in-the-money paths of that date (tensor-core Gram matrix, ridge
- * 1e-3 in unit-diagonal scaling).  Target and decision: the time value
- * (continuation - exercise)/K; exercise where it is predicted negative.  A
+ * over all in-the-money paths of that date (ridge 1e-3 in unit-diagonal
+ * scaling).  At a date the features are functions of ln(S/K) alone, so the
+ * network is evaluated on the tensor core at 512 values of ln(S/K) spanning
+ * the date's in-the-money paths and each path uses the linear interpolation
+ * (Gram matrix exact for the interpolated features, from integer bin
+ * moments; the price depends on no launch or batch detail).  Target and
+ * decision: the time value (continuation - exercise)/K; exercise where it is
+ * predicted negative.  The learned regression takes path_count <= 2^31.  A
  * date with fewer than 4 in-the-money paths has no exercise; a contract whose
  * fit produced non-finite weights is priced by the QR regression instead
  * (mcd_lsm_result.reserved = 1).  Schedule: steps_first Adam steps at the
