@@ -105,6 +105,10 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
                    const std::vector<int>* frozen_ok = nullptr) {
     const size_t n = p.dev.size();
     const size_t elem = precision == 0 ? sizeof(double) : sizeof(float);
+    if (mlp && !frozen)  // the bin moments of one CTA are exact 64-bit integers up to 2^23 paths
+        for (const LsmDev& d : p.dev)
+            if (static_cast<uint64_t>(d.group_chunks) * kLsmChunk > (1ull << 23))
+                return ctx.fail(MCD_ERR_INVALID_ARGUMENT, "learned regression: path_count must be <= 2^31");
     int rc = ctx.reserve(ctx.ext[kDev], sizeof(LsmDev) * n, "lsm contracts");
     if (!rc) rc = ctx.reserve(ctx.ext[kChunkMap], sizeof(uint32_t) * std::max<size_t>(p.total_chunks, 1), "lsm chunk map");
     if (!rc) rc = ctx.reserve(ctx.ext[kStore], elem * std::max<uint64_t>(p.store_elems, 1), "lsm path store");
@@ -133,10 +137,6 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
         }
     }
     if (rc) return rc;
-    if (mlp && !frozen)  // the bin moments of one CTA are exact 64-bit integers up to 2^23 paths
-        for (const LsmDev& d : p.dev)
-            if (static_cast<uint64_t>(d.group_chunks) * kLsmChunk > (1ull << 23))
-                return ctx.fail(MCD_ERR_INVALID_ARGUMENT, "learned regression: path_count must be <= 2^31");
     cudaError_t e = cudaMemcpyAsync(ctx.ext[kDev].ptr, p.dev.data(), sizeof(LsmDev) * n, cudaMemcpyHostToDevice, ctx.stream);
     if (e == cudaSuccess && p.total_chunks)
         e = cudaMemcpyAsync(ctx.ext[kChunkMap].ptr, p.chunk_contract.data(), sizeof(uint32_t) * p.total_chunks,

@@ -165,3 +165,13 @@ def test_node_tables_agree_with_the_network_path_by_path(engine, case):
     same = engine.reprice_mlp(s, k, r, q, v, t, ty, n, paths, 42, w, has, "fp32")
     print(case, res.price, same.price, (same.price - res.price) / res.standard_error)
     assert abs(same.price - res.price) < 0.5 * res.standard_error
+
+
+def test_learned_path_count_limit(engine, gpu_lib):
+    """Bin moments are exact 64-bit integers up to 2^23 paths per CTA, so the
+    learned regression refuses more than 2^31 paths per contract (before any
+    allocation)."""
+    c = np.zeros(1, dtype=gpu_lib.LSM_CONTRACT_DTYPE)
+    c[0] = (40.0, 40.0, 0.06, 0.0, 0.2, 1.0, 1, 1, (1 << 31) + 1024, 1)
+    with pytest.raises(gpu_lib.McdError, match="2\\^31"):
+        engine.lsm_batch(c, "fp32", "mlp")
