@@ -175,3 +175,25 @@ def test_learned_path_count_limit(engine, gpu_lib):
     c[0] = (40.0, 40.0, 0.06, 0.0, 0.2, 1.0, 1, 1, (1 << 31) + 1024, 1)
     with pytest.raises(gpu_lib.McdError, match="2\\^31"):
         engine.lsm_batch(c, "fp32", "mlp")
+
+
+def test_learned_fp64_paths_and_fine_tuning(engine, orc):
+    """The learned regression on FP64 paths (the binned pass in FP64) and with
+    per-date fine-tuning of the features (steps > 0: node tables rebuilt from
+    the updated network every date) both price the put within noise of the
+    FP32 default and of the CRR tree."""
+    s, k, r, q, v, t, ty = 40, 40, .06, 0, .2, 1.0, 1
+    paths, n = 1 << 17, 50
+    base = engine.monte_carlo_lsm_american(s, k, r, q, v, t, ty, n, paths, 42, precision="fp32", regression="mlp")
+    f64 = engine.monte_carlo_lsm_american(s, k, r, q, v, t, ty, n, paths, 42, precision="fp64", regression="mlp")
+    try:
+        engine.set_mlp_config(300, 20, 3e-3, 1e-3)
+        tuned = engine.monte_carlo_lsm_american(s, k, r, q, v, t, ty, n, paths, 42, precision="fp32",
+                                                regression="mlp")
+    finally:
+        engine.set_mlp_config()
+    tree = orc.orc_crr_binomial_american(s, k, r, q, v, t, 2000, ty)
+    for res in (f64, tuned):
+        assert res.reserved == 0
+        assert abs(res.price - base.price) < 1.0 * base.standard_error, (res.price, base.price)
+        assert abs(res.price - tree) < 3 * res.standard_error + 0.02, (res.price, tree)
