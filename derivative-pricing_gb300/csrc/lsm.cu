@@ -35,9 +35,10 @@
 // FP32 path evaluates the basis, the exercise tests and the Gram products in
 // FP32 (FP64 runs at a small fraction of the FP32 rate here), keeps the cash
 // flows and continuation values in FP32 and accumulates the Gram products
-// with compensated FP32 sums per chunk; the final payoffs are summed in
-// compensated FP32 per thread and over the warp tree (Sum32), warp sums,
-// chunk partials and the Cholesky-QR2 solves in FP64.  (The FP32 discount factor
+// with compensated FP32 sums per chunk (per thread, then one warp per sum
+// over the chunk's threads); the final payoffs are summed in compensated
+// FP32 per thread and over the warp tree (Sum32); warp sums, chunk partials
+// and the Cholesky-QR2 solves are FP64.  (The FP32 discount factor
 // carries a relative error below 3e-8 per date, a bias under 2e-6 of the
 // price after 50 dates.)
 //
@@ -90,49 +91,39 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
     hi = s;
 }
 
-// Folded sum i, stored in the 8 bytes of warp 0's (hi, lo) pair of sum i.
+// Fixed-shape block reduction of N compensated sums (256 threads): every
+// thread's (hi, lo) pairs go to shared memory, then warp w folds sums w,
+// w + 8, ...: lane l takes threads l, l + 32, ..., l + 224 in that order
+// (compensated), then a compensated shuffle tree; the FP64 value hi + lo of
+// each sum lands in res and, for thread 0, in out.
 template <int N>
-__device__ __forceinline__ double& smem_out_slot(float (*smem)[N][2], int i) {
-    return *reinterpret_cast<double*>(&smem[0][i][0]);
-}
-
-// Fixed-shape block reduction of N compensated sums (256 threads): warp
-// trees, then thread 0 folds the 8 warps in order; FP64 results in out
-// (valid in thread 0).
-template <int N>
-__device__ void block_sum_df(float (&hi)[N], float (&lo)[N], float (*smem)[N][2], double (&out)[N]) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ void block_sum_df(const float (&hi)[N], const float (&lo)[N], float2 (*scratch)[kLsmThreads],
+                             double* res, double (&out)[N]) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
+    for (int i = 0; i < N; ++i) scratch[i][t] = make_float2(hi[i], lo[i]);
+    __syncthreads();
+    for (int i = warp; i < N; i += kLsmThreads / 32) {
+        float h = 0.0f, l = 0.0f;
+#pragma unroll
+        for (int u = 0; u < kLsmThreads / 32; ++u) {
+            const float2 v = scratch[i][lane + 32 * u];
+            df_add(h, l, v.x);
+            l += v.y;
+        }
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) {
-            const float oh = __shfl_down_sync(0xffffffffu, hi[i], off);
-            const float ol = __shfl_down_sync(0xffffffffu, lo[i], off);
-            df_add(hi[i], lo[i], oh);
-            lo[i] += ol;
+            const float oh = __shfl_down_sync(0xffffffffu, h, off);
+            const float ol = __shfl_down_sync(0xffffffffu, l, off);
+            df_add(h, l, oh);
+            l += ol;
         }
-    }
-    if (lane == 0) {
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-            smem[warp][i][0] = hi[i];
-            smem[warp][i][1] = lo[i];
-        }
+        if (lane == 0) res[i] = static_cast<double>(h) + static_cast<double>(l);
     }
     __syncthreads();
-    // one thread per sum folds the warps in order (a lone FP64 lane costs the
-    // FP64 pipe as much as a full warp, so the N folds run side by side)
-    if (threadIdx.x < N) {
-        const int i = threadIdx.x;
-        double x = 0.0;
-        for (int w = 0; w < kLsmThreads / 32; ++w)
-            x += static_cast<double>(smem[w][i][0]) + static_cast<double>(smem[w][i][1]);
-        smem_out_slot(smem, i) = x;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    if (t == 0) {
 #pragma unroll
-        for (int i = 0; i < N; ++i) out[i] = smem_out_slot(smem, i);
+        for (int i = 0; i < N; ++i) out[i] = res[i];
     }
 }
 
@@ -235,7 +226,8 @@ __global__ void __launch_bounds__(kLsmThreads)
                  const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_a,
                  Welford* __restrict__ final_part) {
     __shared__ double smem[kLsmThreads / 32][11];
-    __shared__ __align__(8) float smem_f[kLsmThreads / 32][11][2];
+    __shared__ float2 scratch[11][kLsmThreads];  // FP32 path: the Gram sums' per-thread pairs
+    __shared__ double sres[11];
     __shared__ Welford swf[kLsmThreads / 32];
     __shared__ Sum64 s64[kLsmThreads / 32];
     const uint32_t chunk = blockIdx.x;
@@ -392,7 +384,7 @@ __global__ void __launch_bounds__(kLsmThreads)
         }
         if (gram) {
             double acc[11];
-            block_sum_df<11>(hi, lo, smem_f, acc);
+            block_sum_df<11>(hi, lo, scratch, sres, acc);
             if (threadIdx.x == 0) {
 #pragma unroll
                 for (int q = 0; q < 11; ++q) part_a[chunk].v[q] = acc[q];
@@ -495,7 +487,8 @@ __global__ void __launch_bounds__(kLsmThreads)
                uint32_t total_chunks, const void* __restrict__ store, const double* __restrict__ cf,
                const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_b) {
     __shared__ double smem[kLsmThreads / 32][15];
-    __shared__ __align__(8) float smem_f[kLsmThreads / 32][15][2];
+    __shared__ float2 scratch[15][kLsmThreads];  // FP32 path: the sums' per-thread pairs
+    __shared__ double sres[15];
     const uint32_t chunk = blockIdx.x;
     if (chunk >= total_chunks) return;
     const LsmDev c = cs[chunk_contract[chunk]];
@@ -590,7 +583,7 @@ __global__ void __launch_bounds__(kLsmThreads)
             df_add(hi[13], lo[13], q2 * y);
             df_add(hi[14], lo[14], q3 * y);
         }
-        block_sum_df<15>(hi, lo, smem_f, out);
+        block_sum_df<15>(hi, lo, scratch, sres, out);
     }
     if (threadIdx.x == 0) {
 #pragma unroll
