@@ -693,19 +693,33 @@ __global__ void __launch_bounds__(kSolveThreads)
         L[r * kGramDim + q] = static_cast<float>(v);
     }
     if (s < kM) G[packed_index(s, 65)] *= sc[s];  // right-hand side
-    // Right-looking Cholesky in FP32, one barrier per column: at column j every
-    // warp updates its rows r > j (lanes over the columns j < q <= r) with
-    // column j of the reduced matrix, and row j of the upper triangle receives
-    // the factor's column j (read by nobody else during the step).
+    // Right-looking Cholesky in FP32, one barrier per column.  At column j
+    // thread t updates column q = j + 1 + (t mod 64) on rows r = q + t / 64,
+    // r + 4, ... with column j of the reduced matrix; its loads are all issued
+    // before its stores (no thread reads what another writes in the step), and
+    // row j of the upper triangle receives the factor's column j.
+    constexpr int kRowGroups = kSolveThreads / 64;
+    constexpr int kMaxRows = (kM + kRowGroups - 1) / kRowGroups;
     for (int j = 0; j < kM; ++j) {
         __syncthreads();
         const float dj = L[j * kGramDim + j];
         const bool drop = !(dj >= static_cast<float>(0.5 * kRidge));
         const float inv = drop ? 0.0f : rsqrtf(dj);
-        for (int r = j + 1 + warp; r < kM; r += kSolveThreads / 32) {
-            const float lr = L[r * kGramDim + j] * inv;
-            for (int q = j + 1 + lane; q <= r; q += 32)
-                L[r * kGramDim + q] = __fmaf_rn(-lr, L[q * kGramDim + j] * inv, L[r * kGramDim + q]);
+        const int q = j + 1 + (s & 63);
+        if (q < kM) {
+            const float lq = L[q * kGramDim + j] * inv;
+            float lr[kMaxRows], cur[kMaxRows];
+#pragma unroll
+            for (int m = 0; m < kMaxRows; ++m) {
+                const int r = q + (s >> 6) + kRowGroups * m;
+                lr[m] = r < kM ? L[r * kGramDim + j] : 0.0f;
+                cur[m] = r < kM ? L[r * kGramDim + q] : 0.0f;
+            }
+#pragma unroll
+            for (int m = 0; m < kMaxRows; ++m) {
+                const int r = q + (s >> 6) + kRowGroups * m;
+                if (r < kM) L[r * kGramDim + q] = __fmaf_rn(-(lr[m] * inv), lq, cur[m]);
+            }
         }
         if (s > j && s < kM) L[j * kGramDim + s] = L[s * kGramDim + j] * inv;
         if (s == 0) inv_diag[j] = inv;  // 1 / L[j][j], 0 when the regressor is dropped
@@ -734,18 +748,18 @@ __global__ void __launch_bounds__(kSolveThreads)
         if (!(fabs(b) <= 1e30)) atomicOr(&bad, 1);  // also catches NaN
     }
     __syncthreads();
-    // snapshot of date d: current features + fitted output layer
+    // snapshot of date d: current features + fitted output layer (W3 then b3)
     float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
     float* snap = snaps + (static_cast<size_t>(c.reg_offset) + d) * kParamStride;
     const bool ok = bad == 0;
-    for (int i = s; i < kParamStride; i += kSolveThreads) {
-        float val = net[i];
-        if (ok) {
-            if (i >= kW3 && i < kB3) val = static_cast<float>(res[i - kW3]);
-            else if (i == kB3) val = static_cast<float>(res[64]);
-        }
-        snap[i] = val;
-        if (ok && i >= kW3 && i <= kB3) net[i] = val;  // fine-tuning continues from the fit
+    static_assert(kParamStride % 4 == 0 && kB3 == kW3 + 64, "snapshot layout");
+    for (int i = s; i < kParamStride / 4; i += kSolveThreads)
+        reinterpret_cast<float4*>(snap)[i] = reinterpret_cast<const float4*>(net)[i];
+    __syncthreads();
+    if (ok && s <= 64) {
+        const float val = static_cast<float>(res[s]);
+        snap[kW3 + s] = val;
+        net[kW3 + s] = val;  // fine-tuning continues from the fit
     }
     if (s == 0) snap_ok[c.reg_offset + d] = ok ? 1 : 0;
 }
