@@ -70,11 +70,14 @@ def _run(cmd, verbose):
 def nvcc_flags(src: str):
     flags = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
              "-ffp-contract=off", "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC] + ARCH
-    # Per-file flags: a leading "// nvcc-flags: ..." line in the source.
+    # Per-file flags: a "// nvcc-flags: ..." line in the source's leading
+    # comment block (read up to the first line that is neither a comment nor blank).
     with open(src) as f:
-        for line in f.read().splitlines()[:40]:
+        for line in f.read().splitlines():
             if line.startswith("// nvcc-flags:"):
                 flags += line.split(":", 1)[1].split()
+            elif line.strip() and not line.lstrip().startswith("//"):
+                break
     extra = os.environ.get("MCD_NVCC_FLAGS")
     if extra:
         flags += extra.split()

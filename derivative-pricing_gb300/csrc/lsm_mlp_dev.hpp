@@ -33,7 +33,8 @@ enum PassMode { kStep = 1, kGram = 2 };
 // decision (an interpolated continuation table).
 constexpr int kNodes = 512;
 constexpr int kNodeSlices = kNodes / 128;           // Gram CTAs per contract (128 bins each)
-constexpr int kMoments = 5;                          // per bin: n, sum t, sum t^2, sum y, sum t y
+constexpr int kMoments = 4;                          // per bin: n 2^40 + sum t, sum t^2, sum y, sum t y
+constexpr int kCountShift = 40;                      // n above sum t (< 2^39 for <= 2^23 paths per CTA)
 constexpr double kTScale = 65536.0;                  // t in [0, 1] as an integer of 16 bits
 constexpr double kYScale = 16777216.0;               // |y| / y_bound as an integer of 24 bits
 constexpr double kGridSd = 7.0;                      // the grid covers the mean +/- 7 standard deviations

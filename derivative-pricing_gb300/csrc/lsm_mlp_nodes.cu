@@ -20,8 +20,9 @@
 //                        discount, cash-flow update, and for the paths in the
 //                        money at date e-1 the per-bin moments n, sum t,
 //                        sum t^2, sum y, sum t y (y = time value / K) as exact
-//                        integers (t to 16 bits, y to 24 bits of its bound)
-//                        with shared-memory atomics: the sums do not depend on
+//                        integers (t to 16 bits, y to 24 bits of its bound;
+//                        n and sum t share one word) with four shared-memory
+//                        atomics per path: the sums do not depend on
 //                        the order of the additions, so the result is
 //                        deterministic.
 //   lsm_mlp_gram_slices  kNodeSlices CTAs per contract: the Gram matrix of
@@ -331,11 +332,10 @@ __global__ void __launch_bounds__(kBinThreads, 5)
                     const int tq = __float2int_rn(t * static_cast<float>(kTScale));
                     const int yq = min(max(__float2int_rn(fminf(fmaxf(y * yq_scale, -16777216.0f), 16777216.0f)),
                                            -16777216), 16777216);
-                    atomicAdd(&mom[0][b], 1ull);
-                    atomicAdd(&mom[1][b], static_cast<unsigned long long>(tq));
-                    atomicAdd(&mom[2][b], static_cast<unsigned long long>(static_cast<long long>(tq) * tq));
-                    atomicAdd(&mom[3][b], static_cast<unsigned long long>(static_cast<long long>(yq)));
-                    atomicAdd(&mom[4][b], static_cast<unsigned long long>(static_cast<long long>(tq) * yq));
+                    atomicAdd(&mom[0][b], (1ull << kCountShift) + static_cast<unsigned long long>(tq));
+                    atomicAdd(&mom[1][b], static_cast<unsigned long long>(static_cast<long long>(tq) * tq));
+                    atomicAdd(&mom[2][b], static_cast<unsigned long long>(static_cast<long long>(yq)));
+                    atomicAdd(&mom[3][b], static_cast<unsigned long long>(static_cast<long long>(tq) * yq));
                 }
             }
         }
@@ -397,11 +397,16 @@ __global__ void __launch_bounds__(kGramThreads)
         const int b = row0 + s;
         float w[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         if (b <= kNodes - 2) {
-            unsigned long long m[kMoments] = {0ull, 0ull, 0ull, 0ull, 0ull};
+            // n, sum t, sum t^2, sum y, sum t y (the first word of a group holds n 2^40 + sum t)
+            unsigned long long m[5] = {0ull, 0ull, 0ull, 0ull, 0ull};
             const unsigned long long* p = mom_part + static_cast<size_t>(c.group_begin) * kMoments * kNodes + b;
-            for (uint32_t gg = 0; gg < c.n_groups; ++gg)
+            for (uint32_t gg = 0; gg < c.n_groups; ++gg) {
+                const unsigned long long first = p[static_cast<size_t>(gg) * kMoments * kNodes];
+                m[0] += first >> kCountShift;
+                m[1] += first & ((1ull << kCountShift) - 1ull);
 #pragma unroll
-                for (int q = 0; q < kMoments; ++q) m[q] += p[(static_cast<size_t>(gg) * kMoments + q) * kNodes];
+                for (int q = 1; q < kMoments; ++q) m[q + 1] += p[(static_cast<size_t>(gg) * kMoments + q) * kNodes];
+            }
             const double yb = s_yb;
             const double cnt = static_cast<double>(m[0]);
             const double st = static_cast<double>(m[1]) / kTScale;
