@@ -444,20 +444,33 @@ __global__ void lsm_solve_a(int k, const LsmDev* __restrict__ cs, int n_contract
     for (int a = 0; a < 4; ++a)
         for (int b2 = a; b2 < 4; ++b2) G[a][b2] = G[b2][a] = s[1 + tri(a, b2)];
     double R[4][4] = {};
-    bool ok = true;
-    for (int j = 0; j < 4 && ok; ++j) {
-        double d = G[j][j];
-        for (int p = 0; p < j; ++p) d -= R[p][j] * R[p][j];
-        if (!(d > 0.0)) {
-            ok = false;
-            break;
+    // R only preconditions pass B, so when the Gram matrix of the raw basis
+    // (condition up to ~1e13) is not numerically positive definite -- its
+    // sums carry ~44 bits on the FP32 path -- the factorisation is retried
+    // with a diagonal shift of 1e-10 of its trace (shifted Cholesky QR,
+    // Fukaya, Kannan, Nakatsukasa, Zhang and Yamamoto, SIAM J. Sci. Comput.
+    // 42 (2020)); pass B and the Householder solve then fit the unshifted
+    // problem.  A date that factorises without the shift is unaffected.
+    const double shift_step = 1e-10 * (G[0][0] + G[1][1] + G[2][2] + G[3][3]);
+    bool ok = false;
+    for (int attempt = 0; attempt < 2 && !ok; ++attempt) {
+        const double shift = attempt == 0 ? 0.0 : shift_step;
+        ok = true;
+        for (int j = 0; j < 4 && ok; ++j) {
+            double d = G[j][j] + shift;
+            for (int p = 0; p < j; ++p) d -= R[p][j] * R[p][j];
+            if (!(d > 0.0)) {
+                ok = false;
+                break;
+            }
+            R[j][j] = sqrt(d);
+            for (int l = j + 1; l < 4; ++l) {
+                double x = G[j][l];
+                for (int p = 0; p < j; ++p) x -= R[p][j] * R[p][l];
+                R[j][l] = x / R[j][j];
+            }
         }
-        R[j][j] = sqrt(d);
-        for (int l = j + 1; l < 4; ++l) {
-            double x = G[j][l];
-            for (int p = 0; p < j; ++p) x -= R[p][j] * R[p][l];
-            R[j][l] = x / R[j][j];
-        }
+        if (ok && attempt == 1) r.degenerate = 2;  // factorised with the shift
     }
     double T[4][4] = {};
     if (ok) {

@@ -42,7 +42,7 @@ struct LsmReg {
     double T[10];
     double gamma[4];
     int32_t has;          // coefficients valid at this date (>= 4 ITM paths)
-    int32_t degenerate;   // Cholesky of the first pass failed; solved without preconditioning
+    int32_t degenerate;   // first-pass Cholesky: 0 plain, 2 with a diagonal shift, 1 failed (no preconditioning)
     float T_f[10];        // FP32 copies for the FP32-path kernels (written with T and gamma)
     float gamma_f[4];
 };

@@ -143,3 +143,17 @@ def test_frozen_boundary_delta_has_lower_variance_than_naive_refit(engine):
     print(f"frozen-boundary delta sd {sf:.5f}, naive refit sd {sn:.5f}, ratio {sn / sf:.2f}")
     assert sf < sn
     assert -0.6 < float(np.mean(frozen)) < -0.2  # an at-the-money American put's delta
+
+
+def test_fp32_ill_conditioned_first_pass(engine, orc):
+    """A put whose raw Laguerre Gram matrix is not numerically positive
+    definite on some date of the FP32 path: the first-pass Cholesky is
+    retried with a small diagonal shift (shifted Cholesky QR) instead of
+    dropping the preconditioner, so the FP32 price stays with the FP64 price
+    and the tree (without the retry it fell 27 standard errors short)."""
+    args = (39.57831059016732, 40.0, 0.06, 0.0, 0.2668022683651664, 1.1610222409416884, 1, 93, 1 << 18, 1468)
+    r32 = engine.monte_carlo_lsm_american(*args, precision="fp32")
+    r64 = engine.monte_carlo_lsm_american(*args, precision="fp64")
+    tree = orc.orc_crr_binomial_american(*args[:6], 2000, 1)
+    assert abs(r32.price - r64.price) < 0.25 * r64.standard_error, (r32.price, r64.price)
+    assert abs(r64.price - tree) < 3 * r64.standard_error + 0.02, (r64.price, tree)
