@@ -241,20 +241,30 @@ __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff
     }
     const float c1 = 1.0f - powf(0.9f, static_cast<float>(t_adam));
     const float c2 = 1.0f - powf(0.999f, static_cast<float>(t_adam));
-    // ---- dW2 rows from tensor memory (lanes 0..63 = output neurons)
+    // ---- dW2 rows from tensor memory (lanes 0..63 = output neurons, readable
+    // by warps 0-1 only), staged in shared memory so that all four warps share
+    // the 4096 Adam updates: the FP32 copy goes into the first half of dz2t
+    // (rows 0..63 of dZ2^T, whose MMA has completed; the next step rewrites them)
+    float* stage = reinterpret_cast<float*>(S.dz2t);
     if (warp < 2) {
         for (int c = 0; c < 4; ++c) {
             float dw[16];
             umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 128 + c * 16), dw);
-            for (int q = 0; q < 16; ++q) {
-                const int idx = kW2 + s * 64 + c * 16 + q;
-                if (grad_out) grad_out[idx] = dw[q];
-                if (update) adam(S.p[idx], S.m[idx], S.v[idx], dw[q], lr, c1, c2);
-            }
+#pragma unroll
+            for (int q = 0; q < 16; ++q) stage[s * 64 + ((c * 16 + q) ^ (s & 31))] = dw[q];  // XOR swizzle
         }
     }
     umma::fence_before_sync();
     __syncthreads();
+    // consecutive threads take consecutive parameters: the parameter and moment
+    // arrays are read and written without bank conflicts
+    for (int i = s; i < 64 * 64; i += 128) {
+        const int row = i >> 6, col = i & 63;
+        const float g = stage[row * 64 + (col ^ (row & 31))];
+        const int idx = kW2 + i;
+        if (grad_out) grad_out[idx] = g;
+        if (update) adam(S.p[idx], S.m[idx], S.v[idx], g, lr, c1, c2);
+    }
     // ---- the small parameters
     for (int q = s; q < 321; q += 128) {
         int idx;
