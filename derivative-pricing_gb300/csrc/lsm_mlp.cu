@@ -613,45 +613,48 @@ __device__ __forceinline__ int packed_index(int r, int q) {  // r <= q
     return r * kGramDim - r * (r - 1) / 2 + (q - r);
 }
 
+// Pivots 32 QI .. 32 QI + 31 of the forward (L z = b) or backward (L^T x = z)
+// substitution: the pivot's owner keeps it in v[QI], known at compile time, so
+// the factor loads of a step do not wait for the previous step.
+template <int QI, bool kForward>
+__device__ __forceinline__ void subst_block(const float* L, const float* inv_diag, float (&v)[3], int lane) {
+    constexpr int kBegin = 32 * QI, kEnd = (32 * QI + 32 < kM) ? 32 * QI + 32 : kM;
+#pragma unroll 4
+    for (int n = 0; n < kEnd - kBegin; ++n) {
+        const int i = kForward ? kBegin + n : kEnd - 1 - n;
+        const float pv = __shfl_sync(0xffffffffu, v[QI] * inv_diag[i], i & 31);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int r = lane + 32 * q;
+            if (r == i) v[q] = pv;
+            else if (kForward ? (r > i && r < kM) : (r < i))
+                v[q] = __fmaf_rn(-(kForward ? L[i * kGramDim + r] : L[r * kGramDim + i]), pv, v[q]);
+        }
+    }
+}
+
 // x = L^-T L^-1 b for the FP32 factor L, stored transposed in the upper
 // triangle of W (L[r][i] at W[i * kGramDim + r], r > i) with the reciprocal
-// diagonal in inv_diag, by one warp: lane l keeps entries l, l+32
-// and l+64 of the vector in registers (z, then x, replace b in place) and
-// each pivot value is broadcast by a shuffle.  b is rhs rounded to FP32; x is
-// added to acc in FP64.  Dropped regressors give 0 (their inv_diag is 0).
+// diagonal in inv_diag, by one warp: lane l keeps entries l, l+32 and l+64 of
+// the vector in registers (z, then x, replace b in place) and each pivot value
+// is broadcast by a shuffle.  b is rhs rounded to FP32; x is added to acc in
+// FP64.  Dropped regressors give 0 (their inv_diag is 0).
 __device__ void chol_solve_warp(const float* L, const float* inv_diag, const double* rhs, double* acc, int lane) {
-    constexpr int kSlots = (kM + 31) / 32;
-    static_assert(kSlots == 3, "three entries per lane");
-    float v[kSlots];
+    static_assert((kM + 31) / 32 == 3, "three entries per lane");
+    float v[3];
 #pragma unroll
-    for (int q = 0; q < kSlots; ++q) {
+    for (int q = 0; q < 3; ++q) {
         const int r = lane + 32 * q;
         v[q] = r < kM ? static_cast<float>(rhs[r]) : 0.0f;
     }
-    for (int i = 0; i < kM; ++i) {  // L z = b, column by column
-        const int qi = i >> 5;
-        const float mine = qi == 0 ? v[0] : (qi == 1 ? v[1] : v[2]);
-        const float zi = __shfl_sync(0xffffffffu, mine * inv_diag[i], i & 31);
+    subst_block<0, true>(L, inv_diag, v, lane);
+    subst_block<1, true>(L, inv_diag, v, lane);
+    subst_block<2, true>(L, inv_diag, v, lane);
+    subst_block<2, false>(L, inv_diag, v, lane);
+    subst_block<1, false>(L, inv_diag, v, lane);
+    subst_block<0, false>(L, inv_diag, v, lane);
 #pragma unroll
-        for (int q = 0; q < kSlots; ++q) {
-            const int r = lane + 32 * q;
-            if (r == i) v[q] = zi;
-            else if (r > i && r < kM) v[q] = __fmaf_rn(-L[i * kGramDim + r], zi, v[q]);
-        }
-    }
-    for (int i = kM - 1; i >= 0; --i) {  // L^T x = z
-        const int qi = i >> 5;
-        const float mine = qi == 0 ? v[0] : (qi == 1 ? v[1] : v[2]);
-        const float xi = __shfl_sync(0xffffffffu, mine * inv_diag[i], i & 31);
-#pragma unroll
-        for (int q = 0; q < kSlots; ++q) {
-            const int r = lane + 32 * q;
-            if (r == i) v[q] = xi;
-            else if (r < i) v[q] = __fmaf_rn(-L[r * kGramDim + i], xi, v[q]);
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < kSlots; ++q) {
+    for (int q = 0; q < 3; ++q) {
         const int r = lane + 32 * q;
         if (r < kM) acc[r] += static_cast<double>(v[q]);
     }
