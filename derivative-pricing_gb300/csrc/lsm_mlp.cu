@@ -456,10 +456,11 @@ __device__ void load_net(const float* __restrict__ net, float* small, __nv_bfloa
     const int s = threadIdx.x;
     for (int i = s; i < kW2; i += 128) small[i] = net[i];
     for (int i = s; i < kParams - kB2; i += 128) small[kW2 + i] = net[kB2 + i];
-    if (s < 64)
-        for (int j = 0; j < 64; j += 2)
-            *reinterpret_cast<__nv_bfloat162*>(at(w2, s, j, 64)) =
-                __floats2bfloat162_rn(net[kW2 + s * 64 + j], net[kW2 + s * 64 + j + 1]);
+    for (int i = s; i < 64 * 32; i += 128) {  // W2 [out][in] read in order (coalesced), pairs to BF16
+        const int r = i >> 5, j = 2 * (i & 31);
+        const float2 w = *reinterpret_cast<const float2*>(net + kW2 + r * 64 + j);
+        *reinterpret_cast<__nv_bfloat162*>(at(w2, r, j, 64)) = __floats2bfloat162_rn(w.x, w.y);
+    }
 }
 
 // Small-parameter offsets inside PassSmem::pd.

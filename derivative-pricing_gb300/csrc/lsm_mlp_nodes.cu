@@ -158,9 +158,11 @@ __global__ void __launch_bounds__(128)
         S.w0[s] = net[kW1 + 2 * s];
         S.c1[s] = __fmaf_rn(net[kW1 + 2 * s + 1], x1, net[kB1 + s]);
         S.b2[s] = net[kB2 + s];
-        for (int j = 0; j < 64; j += 2)
-            *reinterpret_cast<__nv_bfloat162*>(at(S.w2, s, j, 64)) =
-                __floats2bfloat162_rn(net[kW2 + s * 64 + j], net[kW2 + s * 64 + j + 1]);
+    }
+    for (int i = s; i < 64 * 32; i += 128) {  // W2 [out][in] read in order (coalesced), pairs to BF16
+        const int r = i >> 5, j = 2 * (i & 31);
+        const float2 w = *reinterpret_cast<const float2*>(net + kW2 + r * 64 + j);
+        *reinterpret_cast<__nv_bfloat162*>(at(S.w2, r, j, 64)) = __floats2bfloat162_rn(w.x, w.y);
     }
     if (s == 0) {
         umma::mbar_init(&S.mbar, 1);
