@@ -675,11 +675,27 @@ __global__ void __launch_bounds__(kSolveThreads)
     const int d = c.n_steps - k - 1;
     if (d < 1) return;
     const int s = threadIdx.x, lane = s & 31, warp = s >> 5;
-    for (int idx = s; idx < kGramPacked; idx += kSolveThreads) {  // the bin slices' partials, in order
-        const float* p = gram_part + static_cast<size_t>(ci) * kNodeSlices * kGramPacked + idx;
-        double v = 0.0;
-        for (int sl = 0; sl < kNodeSlices; ++sl) v += static_cast<double>(p[static_cast<size_t>(sl) * kGramPacked]);
-        G[idx] = v;
+    {  // the bin slices' partials, summed in order (all loads issued first)
+        constexpr int kIters = (kGramPacked + kSolveThreads - 1) / kSolveThreads;
+        const float* part = gram_part + static_cast<size_t>(ci) * kNodeSlices * kGramPacked;
+        float pv[kIters][kNodeSlices];
+#pragma unroll
+        for (int u = 0; u < kIters; ++u) {
+            const int idx = s + kSolveThreads * u;
+#pragma unroll
+            for (int sl = 0; sl < kNodeSlices; ++sl)
+                pv[u][sl] = idx < kGramPacked ? part[static_cast<size_t>(sl) * kGramPacked + idx] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < kIters; ++u) {
+            const int idx = s + kSolveThreads * u;
+            if (idx < kGramPacked) {
+                double v = 0.0;
+#pragma unroll
+                for (int sl = 0; sl < kNodeSlices; ++sl) v += static_cast<double>(pv[u][sl]);
+                G[idx] = v;
+            }
+        }
     }
     if (s == 0) bad = 0;
     __syncthreads();
@@ -747,12 +763,22 @@ __global__ void __launch_bounds__(kSolveThreads)
         if (warp == 0) chol_solve_warp(L, inv_diag, res, xs, lane);
         __syncthreads();
         if (it == 2) break;
-        for (int i = warp; i < kM; i += kSolveThreads / 32) {  // one warp per row
-            double acc = 0.0;
-            for (int j = lane; j < kM; j += 32)
-                if (inv_diag[j] != 0.0f) acc += G[i <= j ? packed_index(i, j) : packed_index(j, i)] * xs[j];
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) res[i] = inv_diag[i] != 0.0f ? G[packed_index(i, 65)] - acc : 0.0;
+        if (s < kM) {  // one thread per row: 32 strided partial sums, then a pairwise tree
+            const int i = s;
+            double part[32];
+#pragma unroll
+            for (int l = 0; l < 32; ++l) {
+                double acc = 0.0;
+#pragma unroll
+                for (int j = l; j < kM; j += 32)
+                    if (inv_diag[j] != 0.0f) acc += G[i <= j ? packed_index(i, j) : packed_index(j, i)] * xs[j];
+                part[l] = acc;
+            }
+#pragma unroll
+            for (int w = 16; w >= 1; w >>= 1)
+#pragma unroll
+                for (int l = 0; l < w; ++l) part[l] = part[l] + part[l + w];
+            res[i] = inv_diag[i] != 0.0f ? G[packed_index(i, 65)] - part[0] : 0.0;
         }
         __syncthreads();
     }
