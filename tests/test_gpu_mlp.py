@@ -197,3 +197,19 @@ def test_learned_fp64_paths_and_fine_tuning(engine, orc):
         assert res.reserved == 0
         assert abs(res.price - base.price) < 1.0 * base.standard_error, (res.price, base.price)
         assert abs(res.price - tree) < 3 * res.standard_error + 0.02, (res.price, tree)
+
+
+@pytest.mark.parametrize("n_dates, paths", [(1, 50000), (2, 50000), (5, 3), (3, 1)])
+def test_learned_edge_cases(engine, n_dates, paths):
+    """One exercise date (no regression: the terminal payoff discounted), two
+    dates (one fit), and path counts too small for a fit (fewer than 4 paths
+    in the money: no exercise at that date).  The learned regression prices
+    these like the QR regression where no fit is involved, and never fails."""
+    c = (38.0, 40.0, 0.06, 0.0, 0.25, 1.0, 1, n_dates, paths, 9)
+    ml = engine.monte_carlo_lsm_american(*c, precision="fp32", regression="mlp")
+    qr = engine.monte_carlo_lsm_american(*c, precision="fp32", regression="qr")
+    assert np.isfinite(ml.price) and np.isfinite(ml.standard_error) and ml.reserved == 0
+    if n_dates == 1 or paths < 4:
+        assert abs(ml.price - qr.price) <= 1e-6 * max(1.0, abs(qr.price)), (ml.price, qr.price)
+    else:
+        assert abs(ml.price - qr.price) < 3 * qr.standard_error + 0.02, (ml.price, qr.price)
