@@ -104,3 +104,63 @@ def init_params(rng):
     p[W2:B2] = rng.standard_normal(4096) * np.sqrt(2.0 / 64)
     p[W3:B3] = rng.standard_normal(64) * 0.125
     return p
+
+
+# ---------------------------------------------------------------------------
+# The fit on node tables (derivative-pricing_gb300/csrc/lsm_mlp_nodes.cu).
+# At a date the features are functions of u = ln(S/K) alone; they are tabled
+# at nodes u_i = lo + i h and every path uses f(u) = (1 - t) F_i + t F_{i+1}
+# (u in bin i at fraction t; u outside the grid uses the end bin, t clamped).
+# ---------------------------------------------------------------------------
+T_SCALE = 65536.0      # t as an integer of 16 bits
+Y_SCALE = 16777216.0   # y / y_bound as an integer of 24 bits
+
+
+def locate(u, lo, h, n_nodes):
+    """Bin and fraction of each u (the kernel's float arithmetic is FP32; here FP64)."""
+    x = np.clip((np.asarray(u, dtype=np.float64) - lo) / h, 0.0, n_nodes - 1.0)
+    i = np.minimum(x.astype(np.int64), n_nodes - 2)
+    t = np.minimum(x - i, 1.0)
+    return i, t
+
+
+def gram_direct(F, i, t, y):
+    """Gram matrix of [f | 1 | y] built path by path from interpolated features F[n_nodes, k]."""
+    f = (1.0 - t)[:, None] * F[i] + t[:, None] * F[i + 1]
+    X = np.c_[f, np.ones(len(t)), y]
+    return X.T @ X
+
+
+def bin_moments(i, t, y, y_bound, n_nodes):
+    """The per-bin integer moments the binned pass accumulates: n, sum tq, sum tq^2,
+    sum yq, sum tq yq with tq = round(t 2^16), yq = round(y / y_bound 2^24) clamped."""
+    tq = np.rint(np.asarray(t) * T_SCALE).astype(np.int64)
+    yq = np.clip(np.rint(np.asarray(y) / y_bound * Y_SCALE), -Y_SCALE, Y_SCALE).astype(np.int64)
+    m = np.zeros((5, n_nodes - 1), dtype=np.int64)
+    np.add.at(m[0], i, 1)
+    np.add.at(m[1], i, tq)
+    np.add.at(m[2], i, tq * tq)
+    np.add.at(m[3], i, yq)
+    np.add.at(m[4], i, tq * yq)
+    return m
+
+
+def gram_from_moments(F, m, y_bound):
+    """lsm_mlp_gram_slices' formula: G = sum over bins of Saa F_i F_i^T + Sab (F_i F_{i+1}^T
+    + F_{i+1} F_i^T) + Sbb F_{i+1} F_{i+1}^T, the right-hand side sum Say F_i + Sby F_{i+1},
+    with Saa = sum (1-t)^2, Sab = sum t(1-t), Sbb = sum t^2, Say = sum (1-t) y, Sby = sum t y;
+    the constant feature is a column of ones in F (the y^2 entry is not formed)."""
+    n = m[0].astype(np.float64)
+    st = m[1] / T_SCALE
+    stt = m[2] / T_SCALE ** 2
+    sy = m[3] * (y_bound / Y_SCALE)
+    sty = m[4] * (y_bound / (T_SCALE * Y_SCALE))
+    saa, sab, sbb, say, sby = n - 2 * st + stt, st - stt, stt, sy - sty, sty
+    Fc = np.c_[F, np.ones(len(F))]
+    A, B = Fc[:-1], Fc[1:]
+    k = Fc.shape[1]
+    G = np.zeros((k + 1, k + 1))
+    G[:k, :k] = (A.T * saa) @ A + (A.T * sab) @ B + (B.T * sab) @ A + (B.T * sbb) @ B
+    G[:k, k] = A.T @ say + B.T @ sby
+    G[k, :k] = G[:k, k]
+    return G
