@@ -105,10 +105,13 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
                    const std::vector<int>* frozen_ok = nullptr) {
     const size_t n = p.dev.size();
     const size_t elem = precision == 0 ? sizeof(double) : sizeof(float);
-    if (mlp && !frozen)  // the bin moments of one CTA are exact 64-bit integers up to 2^23 paths
-        for (const LsmDev& d : p.dev)
+    if (mlp && !frozen)  // training samples paths; the bin moments of one CTA are exact up to 2^23 paths
+        for (const LsmDev& d : p.dev) {
+            if (d.path_count == 0)
+                return ctx.fail(MCD_ERR_INVALID_ARGUMENT, "learned regression: path_count must be >= 1");
             if (static_cast<uint64_t>(d.group_chunks) * kLsmChunk > (1ull << 23))
                 return ctx.fail(MCD_ERR_INVALID_ARGUMENT, "learned regression: path_count must be <= 2^31");
+        }
     int rc = ctx.reserve(ctx.ext[kDev], sizeof(LsmDev) * n, "lsm contracts");
     if (!rc) rc = ctx.reserve(ctx.ext[kChunkMap], sizeof(uint32_t) * std::max<size_t>(p.total_chunks, 1), "lsm chunk map");
     if (!rc) rc = ctx.reserve(ctx.ext[kStore], elem * std::max<uint64_t>(p.store_elems, 1), "lsm path store");

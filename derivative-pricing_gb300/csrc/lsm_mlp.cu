@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(128, 1)
     const LsmDev c = cs[ci];
     const int n = c.n_steps;
     const int date = n - k - 1;
-    if (date < 1) return;
+    if (date < 1 || c.path_count == 0) return;  // nothing to sample (the host rejects 0 paths)
     const int s = threadIdx.x;
     float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
     if (k == 0) {

@@ -175,6 +175,9 @@ def test_learned_path_count_limit(engine, gpu_lib):
     c[0] = (40.0, 40.0, 0.06, 0.0, 0.2, 1.0, 1, 1, (1 << 31) + 1024, 1)
     with pytest.raises(gpu_lib.McdError, match="2\\^31"):
         engine.lsm_batch(c, "fp32", "mlp")
+    c[0] = (40.0, 40.0, 0.06, 0.0, 0.2, 1.0, 1, 5, 0, 1)  # no paths to train on
+    with pytest.raises(gpu_lib.McdError, match=">= 1"):
+        engine.lsm_batch(c, "fp32", "mlp")
 
 
 def test_learned_fp64_paths_and_fine_tuning(engine, orc):
