@@ -407,7 +407,9 @@ __global__ void __launch_bounds__(128, 1)
         const uint32_t h = mix32(static_cast<uint32_t>(c.seed) * 0x9E3779B1u ^ mix32((static_cast<uint32_t>(date) << 20) ^
                                                                                      (static_cast<uint32_t>(st) << 7) ^ s));
         const uint64_t i = static_cast<uint64_t>(h) % c.path_count;
+        // both loads in flight together (the cash flow is used only in the money)
         const double sv = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(date - 1) * c.path_count + i);
+        const double cfv = cf_load<PREC>(cf, c.cf_offset + i);
         const double ex = (c.type == 0 ? 1.0 : -1.0) * (sv - c.strike);
         const bool itm = ex > 0.0;
         S.x0[s] = static_cast<float>(4.0 * (sv * inv_k - 1.0));
@@ -416,7 +418,7 @@ __global__ void __launch_bounds__(128, 1)
         // decision only needs its sign, and it is an order of magnitude
         // smaller than the continuation value itself, so the network's
         // relative error costs far fewer wrong decisions.
-        S.y[s] = itm ? static_cast<float>((cf_load<PREC>(cf, c.cf_offset + i) - ex) * inv_k) : 0.0f;
+        S.y[s] = itm ? static_cast<float>((cfv - ex) * inv_k) : 0.0f;
         S.w[s] = itm ? 1.0f : 0.0f;
         const int n_eff = __syncthreads_count(itm);
         ++t;
