@@ -282,7 +282,7 @@ int mcd_lsm_batch(mcd_ctx* ctx, const mcd_lsm_contract* contracts, size_t n, int
  * (Gram matrix exact for the interpolated features, from integer bin
  * moments; the price depends on no launch or batch detail).  Target and
  * decision: the time value (continuation - exercise)/K; exercise where it is
- * predicted negative.  The learned regression takes path_count <= 2^31.  A
+ * predicted negative.  The learned regression takes 1 <= path_count <= 2^31.  A
  * date with fewer than 4 in-the-money paths has no exercise; a contract whose
  * fit produced non-finite weights is priced by the QR regression instead
  * (mcd_lsm_result.reserved = 1).  Schedule: steps_first Adam steps at the
