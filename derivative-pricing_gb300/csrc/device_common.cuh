@@ -8,7 +8,9 @@
 //  * FP64 transform: (bits+0.5)/2^32 (rng.cpp:34-37), Acklam's rational inverse
 //    CDF and one Halley step against erfc (src/core/normal.cpp:22-82).
 //  * FP32 transform: the same u, formed as q = min(u, 1-u) from the bits (so the
-//    tails keep full relative precision), mapped by Wichura's AS241 PPND7.
+//    tails keep full relative precision), mapped by this project's polynomial
+//    fits in w = -ln(4q(1-q)) (Giles' change of variable for erfinv; the
+//    coefficients come from csrc/fit_inverse_normal.py).
 //  * Welford triples and the Chan-Golub-LeVeque merge
 //    (include/mcd/core/stats.hpp:23-65).
 #pragma once

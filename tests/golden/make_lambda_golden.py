@@ -8,7 +8,7 @@ validation failures, GET /cfa-invariants and an unknown route.  Timing fields
 Needs the reference tree and a C++ compiler: the pybind11 module is built from a
 copy of the tree in a temporary directory (the tree itself is never written).
 
-    python tests/golden/make_lambda_golden.py [--reference /root/reference]
+    python tests/golden/make_lambda_golden.py --reference <reference checkout>
 """
 from __future__ import annotations
 
@@ -105,7 +105,9 @@ def build_module(reference, work):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("MCD_REFERENCE_ROOT"),
+                    required="MCD_REFERENCE_ROOT" not in os.environ,
+                    help="the reference's source checkout (or set MCD_REFERENCE_ROOT)")
     a = ap.parse_args()
     with tempfile.TemporaryDirectory() as work:
         tree = build_module(a.reference, work)

@@ -1,11 +1,14 @@
 """GPU parity for Longstaff-Schwartz (src/pricers/lsm.cpp:62-213) through the C ABI.
 
 Bars:
-  * FP64: price within 1e-10 relative of the reference's own output (golden) --
-    the GPU solves the same least-squares problem by Cholesky-QR2 instead of a
-    sequential Householder QR, so coefficients agree to ~1e-9 and exercise
-    decisions coincide; the fitted continuation values agree to 1e-8 of the
-    coefficient scale.
+  * FP64: price within 1e-12 relative of the reference's own output (golden),
+    standard error within 1e-10 -- the GPU solves the same least-squares problem
+    by Cholesky-QR2 instead of a sequential Householder QR; the coefficients are
+    determined by the data only up to the problem's conditioning (the
+    reference's own Householder moves them by ~1e-9 relative when the rows are
+    reordered, tests/test_lsm_conditioning.py), the fitted continuation values
+    agree to 1e-8 of the coefficient scale, and every exercise decision
+    coincides.  The full-size grid is tests/test_gpu_lsm_grid.py.
   * Frozen-policy repricing with the reference's own policy: within 1e-12.
   * FP32 paths: within 0.5 SE of the FP64 price on the same draws.
   * Within 3 SE of the CRR American tree (tests/lsm_test.cpp:78-98 grid) and
@@ -29,8 +32,8 @@ def test_fp64_matches_reference_golden(engine, golden):
         res, co, has = engine.monte_carlo_lsm_american(s, k, r, q, v, t, ty, n, paths, seed,
                                                        precision="fp64", policy=True)
         assert res.path_count == paths
-        assert abs(res.price - case["price"]) <= 1e-10 * case["price"], (case["args"], res.price)
-        assert abs(res.standard_error - case["se"]) <= 1e-8 * case["se"]
+        assert abs(res.price - case["price"]) <= 1e-12 * case["price"], (case["args"], res.price)
+        assert abs(res.standard_error - case["se"]) <= 1e-10 * case["se"]
         assert res.exercise_at_inception == case["inception"]
         assert has.tolist() == case["has"]
         ref = np.array(case["coefficients"]).reshape(-1, 4)
