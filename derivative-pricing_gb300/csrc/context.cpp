@@ -99,39 +99,41 @@ bool finite_all(std::initializer_list<double> xs) {
     return true;
 }
 
-// Validates one contract and converts it to the kernel layout.  The derived
-// constants use the reference's operation order (gbm.cpp:8-10,
-// monte_carlo.cpp:159-160, :191-193, :219, :277-280) so FP64 paths see the
-// same values the reference computes per step.
-int plan_contract(Ctx& ctx, const mcd_contract& in, uint32_t index, DevContract& out) {
-    char msg[256];
-    auto bad = [&](const char* why) {
-        std::snprintf(msg, sizeof msg, "contract %u: %s", index, why);
-        return ctx.fail(MCD_ERR_INVALID_ARGUMENT, msg);
-    };
-    if (in.product < 0 || in.product > 4) return bad("unknown product");
-    if (in.type != 0 && in.type != 1) return bad("type must be 0 (call) or 1 (put)");
+// Validates one contract and converts it to the kernel layout; returns null
+// or the reason the contract is rejected.  No context: mcd_price_batch's
+// planner and the allocation-free entry point (batch_static.cu) share it, so
+// their checks and constants cannot drift apart.  The derived constants use
+// the reference's operation order (gbm.cpp:8-10, monte_carlo.cpp:159-160,
+// :191-193, :219, :277-280) so FP64 paths see the same values the reference
+// computes per step.
+const char* convert_contract(const mcd_contract& in, uint32_t index, DevContract& out) {
+    if (in.product < 0 || in.product > 4) return "unknown product";
+    if (in.type != 0 && in.type != 1) return "type must be 0 (call) or 1 (put)";
     if (!finite_all({in.spot, in.strike, in.barrier, in.rebate, in.rate, in.carry_yield, in.vol,
                      in.time, in.cash_amount}))
-        return bad("non-finite parameter");
-    if (!(in.spot > 0.0)) return bad("spot must be > 0");
-    if (!(in.vol > 0.0)) return bad("vol must be > 0");
-    if (!(in.time > 0.0)) return bad("time must be > 0");
-    if (in.path_count > (1ull << 53)) return bad("path_count must be <= 2^53");
+        return "non-finite parameter";
+    if (!(in.spot > 0.0)) return "spot must be > 0";
+    if (!(in.vol > 0.0)) return "vol must be > 0";
+    if (!(in.time > 0.0)) return "time must be > 0";
+    if (in.path_count > (1ull << 53)) return "path_count must be <= 2^53";
     const bool path_dependent = in.product >= MCD_PRODUCT_ASIAN;
-    if (path_dependent && in.monitoring_points < 1) return bad("monitoring_points must be >= 1");
+    if (path_dependent && in.monitoring_points < 1) return "monitoring_points must be >= 1";
     if (in.product == MCD_PRODUCT_BARRIER) {
-        if (!(in.barrier > 0.0)) return bad("barrier must be > 0");
-        if (in.direction != 0 && in.direction != 1) return bad("direction must be 0 (up) or 1 (down)");
-        if (in.knock != 0 && in.knock != 1) return bad("knock must be 0 (in) or 1 (out)");
+        if (!(in.barrier > 0.0)) return "barrier must be > 0";
+        if (in.direction != 0 && in.direction != 1) return "direction must be 0 (up) or 1 (down)";
+        if (in.knock != 0 && in.knock != 1) return "knock must be 0 (in) or 1 (out)";
     }
     if ((in.product == MCD_PRODUCT_ASIAN || in.product == MCD_PRODUCT_LOOKBACK) &&
         in.strike_style != 0 && in.strike_style != 1)
-        return bad("strike_style must be 0 (fixed) or 1 (floating)");
+        return "strike_style must be 0 (fixed) or 1 (floating)";
     if (in.product == MCD_PRODUCT_ASIAN && in.average_style != 0 && in.average_style != 1)
-        return bad("average_style must be 0 (arithmetic) or 1 (geometric)");
+        return "average_style must be 0 (arithmetic) or 1 (geometric)";
     if (in.product == MCD_PRODUCT_DIGITAL && in.digital_style != 0 && in.digital_style != 1)
-        return bad("digital_style must be 0 (cash) or 1 (asset)");
+        return "digital_style must be 0 (cash) or 1 (asset)";
+    // Slab count in 64 bits before it is narrowed: path counts up to 2^53 are
+    // accepted above, and from 2^44 paths on the count no longer fits 32 bits.
+    const uint64_t slabs = (in.path_count + kSlabPaths - 1) / kSlabPaths;
+    if (slabs > 0xFFFFFFFFull) return "too many paths";
 
     std::memset(&out, 0, sizeof out);
     out.type = in.type;
@@ -183,10 +185,16 @@ int plan_contract(Ctx& ctx, const mcd_contract& in, uint32_t index, DevContract&
     }
     out.drift = (in.rate - in.carry_yield - 0.5 * vol * vol) * dt;
     out.vs = vol * std::sqrt(dt);
-    const uint64_t slabs = (in.path_count + kSlabPaths - 1) / kSlabPaths;
-    if (slabs > 0xFFFFFFFFull) return bad("too many paths");
     out.n_slabs = static_cast<uint32_t>(slabs);
-    return MCD_OK;
+    return nullptr;
+}
+
+int plan_contract(Ctx& ctx, const mcd_contract& in, uint32_t index, DevContract& out) {
+    const char* why = convert_contract(in, index, out);
+    if (!why) return MCD_OK;
+    char msg[256];
+    std::snprintf(msg, sizeof msg, "contract %u: %s", index, why);
+    return ctx.fail(MCD_ERR_INVALID_ARGUMENT, msg);
 }
 
 // Cost of one slab of a contract, used for longest-first ordering.
@@ -478,10 +486,26 @@ int mcd_price_batch_device(mcd_ctx* handle, const mcd_contract* contracts, size_
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "precision must be 0 (FP64) or 1 (FP32)");
     if (n == 0) return MCD_OK;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-    DevicePlanKey key{contracts, n, precision};
+    // The plan is keyed on the contract array's content, not only its
+    // address: a digest of the caller's records is computed on the caller's
+    // stream (after whatever the caller queued there, e.g. an in-place rewrite
+    // of the contracts) and read back; a changed digest re-plans.  Waiting for
+    // it also retires this context's previous launches on that stream, so a
+    // new plan never overwrites buffers a running graph still reads.
+    static_assert(sizeof(mcd_contract) % sizeof(uint64_t) == 0, "contract records are whole words");
+    uint64_t* d_digest = reinterpret_cast<uint64_t*>(ctx->d_flags + 4);
+    cudaError_t e = launch_words_digest(reinterpret_cast<const uint64_t*>(contracts),
+                                        n * (sizeof(mcd_contract) / sizeof(uint64_t)), d_digest, s);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "contract digest");
+    uint64_t digest = 0;
+    e = cudaMemcpyAsync(&digest, d_digest, sizeof digest, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "read contract digest");
+    DevicePlanKey key{contracts, n, precision, digest};
     if (!(ctx->device_plan_valid && ctx->device_plan_key == key)) {
         std::vector<mcd_contract> host(n);
-        cudaError_t e = cudaMemcpy(host.data(), contracts, sizeof(mcd_contract) * n, cudaMemcpyDeviceToHost);
+        e = cudaMemcpyAsync(host.data(), contracts, sizeof(mcd_contract) * n, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return ctx->cuda_fail(e, "read device contracts");
         int rc = plan_batch(*ctx, host.data(), n, ctx->device_plan);
         if (rc) return rc;

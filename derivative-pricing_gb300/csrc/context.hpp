@@ -51,12 +51,15 @@ struct CachedGraph {
     cudaGraphExec_t exec;
 };
 
+// Key of the device-resident plan: the caller's array, its length, the
+// precision and a digest of the records' content (launch_words_digest).
 struct DevicePlanKey {
     const void* contracts;
     size_t n;
     int precision;
+    uint64_t digest;
     bool operator==(const DevicePlanKey& o) const {
-        return contracts == o.contracts && n == o.n && precision == o.precision;
+        return contracts == o.contracts && n == o.n && precision == o.precision && digest == o.digest;
     }
 };
 
@@ -67,11 +70,11 @@ struct Ctx {
     std::string error;
 
     DeviceBuffer d_contracts, d_prefix, d_partials, d_results, d_scratch, d_scratch2;
-    uint32_t* d_flags = nullptr;  // [0] ticket, [1] error word, rest spare
+    uint32_t* d_flags = nullptr;  // [0] ticket, [1] error word, [4..5] contract digest, rest spare
     HostBuffer h_stage;
 
     BatchPlan host_plan, device_plan;
-    DevicePlanKey device_plan_key{nullptr, 0, 0};
+    DevicePlanKey device_plan_key{nullptr, 0, 0, 0};
     bool device_plan_valid = false;
 
     LaunchShape shape[2];

@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "mcd_gpu.h"
 
 namespace mcdg {
 
@@ -58,6 +59,11 @@ struct DevContract {
     uint32_t orig_index;   // position in the caller's array
 };
 
+// Validates one contract and converts it to the kernel layout; null on
+// success, else the reason it is rejected (context.cpp).  Shared by
+// mcd_price_batch's planner and the allocation-free entry point.
+const char* convert_contract(const mcd_contract& in, uint32_t index, DevContract& out);
+
 // Launches (all asynchronous on `stream`).
 cudaError_t launch_path_kernel(int precision, int variant, int grid, const DevContract* contracts,
                                int n_contracts, const uint32_t* item_prefix, uint32_t total_items,
@@ -67,6 +73,10 @@ cudaError_t launch_merge_kernel(const DevContract* contracts, int n_contracts,
                                 const uint32_t* item_prefix, const Welford* partials,
                                 void* results /* mcd_mc_result[] */, cudaStream_t stream);
 cudaError_t path_kernel_occupancy(int precision, int variant, int* blocks_per_sm);
+// Order-independent 64-bit digest of n_words 64-bit words (one CTA): the sum
+// over i of mix(word_i, i), written to *out.
+cudaError_t launch_words_digest(const uint64_t* words, size_t n_words, uint64_t* out,
+                                cudaStream_t stream);
 
 cudaError_t launch_philox_kernel(const uint32_t* counters, const uint32_t* keys, size_t n,
                                  uint32_t* out, cudaStream_t stream);

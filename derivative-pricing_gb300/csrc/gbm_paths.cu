@@ -495,7 +495,38 @@ cudaError_t occupancy_prec(int variant, int* blocks) {
     }
 }
 
+// Digest of a word array: sum over i of splitmix64's finaliser (Steele, Lea
+// and Flood, OOPSLA 2014) applied to word_i + (i + 1) * golden-ratio constant.
+// Integer sums do not depend on the order of the additions, so the digest is
+// the same for any grid; one CTA suffices for a contract list.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(256) words_digest_kernel(const uint64_t* __restrict__ words, size_t n,
+                                                           uint64_t* __restrict__ out) {
+    __shared__ uint64_t part[8];
+    uint64_t acc = 0;
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) acc += mix64(words[i] + (i + 1) * 0x9E3779B97F4A7C15ull);
+    for (int off = 16; off >= 1; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t total = 0;
+        for (int w = 0; w < 8; ++w) total += part[w];
+        *out = total;
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_words_digest(const uint64_t* words, size_t n_words, uint64_t* out, cudaStream_t stream) {
+    cudaGetLastError();
+    words_digest_kernel<<<1, 256, 0, stream>>>(words, n_words, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_path_kernel(int precision, int variant, int grid, const DevContract* contracts,
                                int n_contracts, const uint32_t* item_prefix, uint32_t total_items,

@@ -152,10 +152,13 @@ int mcd_price_lookback(mcd_ctx* ctx, double spot, double strike, double rate, do
 int mcd_price_batch(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, int precision,
                     mcd_mc_result* results);
 /* Device-resident variant: `contracts` and `results` are device pointers; the
- * work is queued on `stream` (a cudaStream_t, or NULL for the context's
- * stream) and the call returns without synchronising.  The contract list is
- * read from the device once to plan the launch; replanning happens only when
- * the pointer, count or precision changes (mcd_batch_invalidate forces it). */
+ * pricing is queued on `stream` (a cudaStream_t, or NULL for the context's
+ * stream) and the call returns without waiting for it.  Each call first
+ * computes an 8-byte digest of the contract records on `stream` and waits for
+ * it (so everything the caller queued there before, such as an in-place
+ * rewrite of the contracts, is seen); the launch plan is rebuilt whenever the
+ * pointer, count, precision or digest changes (mcd_batch_invalidate forces
+ * it), reading the records on `stream` as well. */
 int mcd_price_batch_device(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, int precision,
                            mcd_mc_result* results, void* stream);
 int mcd_batch_invalidate(mcd_ctx* ctx);
@@ -170,7 +173,10 @@ int mcd_batch_invalidate(mcd_ctx* ctx);
  * the same results; its scratch (contract records, slab partials, device
  * results, ticket and error word) lives in one fixed __device__ array of
  * about 7 MB.  Every GPU that loads the library holds that array until the
- * process exits.
+ * process exits.  Under CUDA's lazy module loading (the runtime's default)
+ * the array is reserved on a device by the first call there, not when the
+ * library is loaded: a caller that then reserves the rest of device memory
+ * makes that first call (n = 0 will do) before doing so.
  *
  * Limits: at most 4096 contracts and 262144 slabs of MCD_SLAB_PATHS paths
  * (about 1.07e9 paths in total) per call.  Larger requests fail with
@@ -180,9 +186,9 @@ int mcd_batch_invalidate(mcd_ctx* ctx);
  * results are in `results`.  On failure, a message is written to
  * error_message (if error_capacity > 0).
  *
- * The first call on a device does the set-up for that device: it resolves the
- * array's device address with that device current.  Make that first call
- * before any stream capture.  All calls share the one array, and it keeps
+ * The first call on a device does the set-up for that device (a call with
+ * n = 0 does only that): it resolves the array's device address with that
+ * device current.  Make that first call before any stream capture.  All calls share the one array, and it keeps
  * the last call's contents.  Calls that overlapped on the GPU would race on
  * it; this entry point serialises its calls with a process-wide lock and
  * waits for its GPU work before returning, so its own calls never overlap. */

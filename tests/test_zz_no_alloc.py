@@ -102,3 +102,47 @@ def test_static_rejects_sizes_beyond_its_limit(gpu_lib):
     # still usable afterwards
     ok = _batch(gpu_lib, 4, seed=9)
     _call_static(fn, gpu_lib, ok, 1)
+
+
+def test_static_matches_oracle_directly(gpu_lib, orc):
+    """The allocation-free entry point against the CPU oracle (the reference's
+    algorithm restated), without going through the allocating entry point:
+    FP64 prices within 1e-12 relative on identical draws."""
+    import oracle as O
+    fn = _static_fn(gpu_lib)
+    c = _batch(gpu_lib, 24, seed=12)
+    c["path_count"] = np.maximum(c["path_count"], 1)
+    for _ in range(2):  # two calls in a row on the shared array
+        got = _call_static(fn, gpu_lib, c, 0)
+        arr = (O.Contract * len(c))()
+        for i, row in enumerate(c):
+            for name in row.dtype.names:
+                setattr(arr[i], name, row[name].item())
+        want = (O.McResult * len(c))()
+        orc.orc_price_batch(arr, len(c), 1, 0, want)
+        for i in range(len(c)):
+            assert got["path_count"][i] == want[i].path_count
+            assert abs(got["price"][i] - want[i].price) <= PRICE_REL * abs(want[i].price) + 1e-300, (i, c[i])
+
+
+def test_static_rejects_path_counts_whose_slab_count_overflows(gpu_lib):
+    """2^44 paths and more need 2^32 slabs or more: rejected, never wrapped."""
+    fn = _static_fn(gpu_lib)
+    out = np.zeros(1, dtype=gpu_lib.RESULT_DTYPE)
+    msg = C.create_string_buffer(256)
+    for paths in (1 << 44, (1 << 44) + 1, 1 << 53):
+        c = gpu_lib.contracts(1)
+        c["product"] = 0
+        c["spot"] = c["strike"] = 100.0
+        c["vol"] = .2
+        c["time"] = 1.0
+        c["path_count"] = paths
+        rc = fn(c.ctypes.data, 1, 1, out.ctypes.data, None, msg, len(msg))
+        assert rc == -1, (paths, msg.value)
+        assert msg.value
+
+
+def test_static_setup_call_with_no_contracts(gpu_lib):
+    fn = _static_fn(gpu_lib)
+    msg = C.create_string_buffer(256)
+    assert fn(None, 0, 1, None, None, msg, len(msg)) == 0, msg.value
