@@ -96,7 +96,7 @@ struct Ctx {
 
     // State owned by the other modules (Heston, LSM, QMC, Greeks); freed by
     // release_extensions().
-    DeviceBuffer ext[40];
+    DeviceBuffer ext[48];
 
     // Sensitivity engine (greeks_api.cpp): launch shape and the last graph.
     LaunchShape greeks_shape[2];

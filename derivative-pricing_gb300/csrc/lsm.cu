@@ -15,22 +15,25 @@
 // threads (4 paths per thread, stride 256).
 //
 // Backward pass.  All contracts of a batch step back in lockstep: iteration k
-// handles date e = n_c - k of contract c.  Per iteration:
-//   lsm_exercise  exercise at date e with that date's coefficients, discount,
-//                 and either the Gram sums of date e-1 (pass A) or, when e = 1,
-//                 the final Welford partial;
-//   lsm_solve_a   per contract: fixed-order reduction, Cholesky G = R^T R,
-//                 T = R^{-1};
-//   lsm_gram_b    Gram sums and right-hand side in the preconditioned basis
-//                 b' = b T (pass B);
-//   lsm_solve_b   per contract: reduction, 4x4 Householder solve of
-//                 G' beta' = h', gamma = T beta' (coefficients in the
-//                 Laguerre basis, as the reference's policy stores them).
-// This is Cholesky-QR2 applied to the least-squares problem: the first pass
-// removes the conditioning (cond(X) reaches ~2e6 for these bases, cond(G)
-// ~4e12), the second is solved at QR accuracy, so the coefficients agree with
-// the reference's Householder QR to ~1e-10 relative and exercise decisions
-// essentially never differ.  Every reduction tree is fixed by chunk index.
+// handles date e = n_c - k of contract c, in one pass over the date's columns
+// (lsm_step): exercise at date e with that date's coefficients, discount, and
+// either the regression sums of date e-1 -- Gram matrix and right-hand side
+// in the basis b T_e, T_e being date e's preconditioner (adjacent dates'
+// in-the-money populations are alike, so b T_e is already close to
+// orthonormal on date e-1) -- or, when e = 1, the final Welford partial.  The
+// last CTA of a contract to finish folds the chunk partials in chunk order
+// and solves date e-1 (no separate launch; no CTA waits for another): the
+// Cholesky factor R of the lagged Gram matrix gives date e-1's own
+// preconditioner T = T_e R^{-1}; when that matrix is well conditioned the 4x4
+// Householder solve of the preconditioned normal equations gives the
+// coefficients at once.  Otherwise -- always on the first regression date,
+// whose lag is the identity (cond of the raw Laguerre Gram matrix reaches
+// ~4e12) -- lsm_refine makes a second pass in the basis b T and solves it:
+// Cholesky-QR2 for that date.  Either way the coefficients agree with the
+// reference's Householder QR to the limit set by the least-squares
+// conditioning (its own algorithm moves them that much when the rows are
+// reordered), and the fitted continuation values, hence the exercise
+// decisions, coincide.  Every reduction tree is fixed by chunk index.
 // Precision: the FP64 path is the reference's arithmetic throughout.  The
 // FP32 path evaluates the basis, the exercise tests and the Gram products in
 // FP32 (FP64 runs at a small fraction of the FP32 rate here), keeps the cash
@@ -216,23 +219,238 @@ __global__ void __launch_bounds__(kLsmThreads)
 }
 
 // ---------------------------------------------------------------------------
-// iteration k: exercise at date e, discount, pass A for date e-1 (or final)
+// per-date 4x4 algebra (FP64, one thread)
 // ---------------------------------------------------------------------------
+// Upper-triangular index of (r, c), r <= c, in the packed 10-entry layout.
+__device__ __forceinline__ int tri(int r, int col) {
+    const int base[4] = {0, 4, 7, 9};
+    return base[r] + (col - r);
+}
+
+// Cholesky factor of G + shift I = R^T R (R upper); false when a pivot is
+// not positive.
+__device__ bool chol4(const double G[4][4], double shift, double R[4][4]) {
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = 0; b2 < 4; ++b2) R[a][b2] = 0.0;
+    for (int j = 0; j < 4; ++j) {
+        double d = G[j][j] + shift;
+        for (int p = 0; p < j; ++p) d -= R[p][j] * R[p][j];
+        if (!(d > 0.0)) return false;
+        R[j][j] = sqrt(d);
+        for (int l = j + 1; l < 4; ++l) {
+            double x = G[j][l];
+            for (int p = 0; p < j; ++p) x -= R[p][j] * R[p][l];
+            R[j][l] = x / R[j][j];
+        }
+    }
+    return true;
+}
+
+// T = R^{-1} for upper-triangular R.
+__device__ void inv_upper4(const double R[4][4], double T[4][4]) {
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = 0; b2 < 4; ++b2) T[a][b2] = 0.0;
+    for (int j = 3; j >= 0; --j) {
+        T[j][j] = 1.0 / R[j][j];
+        for (int l = j + 1; l < 4; ++l) {
+            double x = 0.0;
+            for (int p = j; p < l; ++p) x += T[j][p] * R[p][l];
+            T[j][l] = -x / R[l][l];
+        }
+    }
+}
+
+// 4x4 Householder least squares (the reference's algorithm, src/core/linalg.cpp:7-71,
+// on a square system): A is overwritten, y too.
+__device__ void householder4(double A[4][4], double y[4], double beta[4]) {
+    for (int kk = 0; kk < 4; ++kk) {
+        double norm_sq = 0.0;
+        for (int i = kk; i < 4; ++i) norm_sq += A[i][kk] * A[i][kk];
+        const double norm = sqrt(norm_sq);
+        if (norm == 0.0) continue;
+        const double akk = A[kk][kk];
+        const double alpha = akk >= 0.0 ? -norm : norm;
+        double v[4] = {0, 0, 0, 0};
+        v[kk] = akk - alpha;
+        for (int i = kk + 1; i < 4; ++i) v[i] = A[i][kk];
+        double vn = 0.0;
+        for (int i = kk; i < 4; ++i) vn += v[i] * v[i];
+        if (vn == 0.0) continue;
+        for (int jj = kk; jj < 4; ++jj) {
+            double dot = 0.0;
+            for (int i = kk; i < 4; ++i) dot += v[i] * A[i][jj];
+            const double f = 2.0 * dot / vn;
+            for (int i = kk; i < 4; ++i) A[i][jj] -= f * v[i];
+        }
+        double dy = 0.0;
+        for (int i = kk; i < 4; ++i) dy += v[i] * y[i];
+        const double fy = 2.0 * dy / vn;
+        for (int i = kk; i < 4; ++i) y[i] -= fy * v[i];
+    }
+    for (int i = 3; i >= 0; --i) {
+        double sum = y[i];
+        for (int jj = i + 1; jj < 4; ++jj) sum -= A[i][jj] * beta[jj];
+        const double diag = A[i][i];
+        beta[i] = diag != 0.0 ? sum / diag : 0.0;
+    }
+}
+
+__device__ __forceinline__ void unpack_upper(const double* packed, double T[4][4]) {
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = 0; b2 < 4; ++b2) T[a][b2] = b2 >= a ? packed[tri(a, b2)] : 0.0;
+}
+
+__device__ __forceinline__ void store_T(LsmReg& r, const double T[4][4]) {
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = a; b2 < 4; ++b2) {
+            r.T[tri(a, b2)] = T[a][b2];
+            r.T_f[tri(a, b2)] = static_cast<float>(T[a][b2]);
+        }
+}
+
+// Least squares on the preconditioned normal equations: s = (count, 10
+// packed entries of G = P^T X^T X P, 4 entries of h = P^T X^T y) for the
+// basis X P of preconditioner P (upper triangular).  Solves G beta = h by
+// the 4x4 Householder QR and returns gamma = P beta, the coefficients in the
+// Laguerre basis (the reference's policy layout).
+__device__ void solve_preconditioned(const double s[15], const double P[4][4], double gamma[4]) {
+    double G[4][4], y[4], beta[4] = {0, 0, 0, 0};
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = a; b2 < 4; ++b2) G[a][b2] = G[b2][a] = s[1 + tri(a, b2)];
+    for (int a = 0; a < 4; ++a) y[a] = s[11 + a];
+    householder4(G, y, beta);
+    for (int a = 0; a < 4; ++a) {
+        double x = 0.0;
+        for (int b2 = a; b2 < 4; ++b2) x += P[a][b2] * beta[b2];
+        gamma[a] = x;
+    }
+}
+
+// The regression of one date from its sums in the basis of the lagged
+// preconditioner L (the next later date's T).  Cholesky of G' = R^T R gives
+// this date's preconditioner T = L R^{-1} (so that T^T X^T X T = I).  When G'
+// is well conditioned (cond bound ||R||_F^2 ||R^-1||_F^2 <= kappa_max) the
+// date is solved here: has = 1.  Otherwise T is stored and the date is marked
+// for a second pass in the basis X T (has = 2): that pass and its solve are
+// Cholesky-QR2.  The first regression date (L = I, the raw Laguerre Gram
+// matrix, condition up to ~1e13) always takes it; where that raw matrix is not
+// numerically positive definite (its FP32-path sums carry ~44 bits) the
+// factorisation is retried with a diagonal shift of 1e-10 of the trace --
+// shifted Cholesky QR (Fukaya, Kannan, Nakatsukasa, Zhang and Yamamoto, SIAM
+// J. Sci. Comput. 42 (2020)) -- and the second pass fits the unshifted problem.
+__device__ void solve_lagged(const double s[15], const double L[4][4], double kappa_max, LsmReg& r) {
+    if (s[0] < 4.0) {  // too few in-the-money paths (src/pricers/lsm.cpp:102-104)
+        r.has = -1;
+        r.degenerate = 0;
+        store_T(r, L);  // the lag passes through to the next earlier date
+        return;
+    }
+    double G[4][4];
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = a; b2 < 4; ++b2) G[a][b2] = G[b2][a] = s[1 + tri(a, b2)];
+    double R[4][4], Ri[4][4], T[4][4];
+    bool ok = chol4(G, 0.0, R);
+    double kappa = 1e300;
+    if (ok) {
+        inv_upper4(R, Ri);
+        double fr = 0.0, fi = 0.0;
+        for (int a = 0; a < 4; ++a)
+            for (int b2 = a; b2 < 4; ++b2) {
+                fr += R[a][b2] * R[a][b2];
+                fi += Ri[a][b2] * Ri[a][b2];
+            }
+        kappa = fr * fi;
+    }
+    r.degenerate = 0;
+    if (!ok) {
+        const double shift = 1e-10 * (G[0][0] + G[1][1] + G[2][2] + G[3][3]);
+        ok = chol4(G, shift, R);
+        if (ok) inv_upper4(R, Ri);
+        r.degenerate = ok ? 2 : 1;
+    }
+    if (ok) {
+        for (int a = 0; a < 4; ++a)
+            for (int b2 = 0; b2 < 4; ++b2) {
+                double x = 0.0;
+                for (int p = a; p <= b2; ++p) x += L[a][p] * Ri[p][b2];
+                T[a][b2] = b2 >= a ? x : 0.0;
+            }
+    } else {
+        for (int a = 0; a < 4; ++a)
+            for (int b2 = 0; b2 < 4; ++b2) T[a][b2] = L[a][b2];
+    }
+    store_T(r, T);
+    if (r.degenerate == 0 && kappa <= kappa_max) {
+        double gamma[4];
+        solve_preconditioned(s, L, gamma);
+        for (int a = 0; a < 4; ++a) {
+            r.gamma[a] = gamma[a];
+            r.gamma_f[a] = static_cast<float>(gamma[a]);
+        }
+        r.has = 1;
+    } else {
+        r.has = 2;
+    }
+}
+
+// Fixed-order fold of a contract's chunk partials by the whole CTA: thread t
+// takes chunks t, t + 256, ... in order, then the fixed block tree; the
+// result is valid in thread 0.
+template <int N>
+__device__ void fold_partials(const LsmPartial* __restrict__ part, uint32_t begin, uint32_t count,
+                              double (&v)[N], double (*smem)[N]) {
+#pragma unroll
+    for (int q = 0; q < N; ++q) v[q] = 0.0;
+    for (uint32_t ch = threadIdx.x; ch < count; ch += kLsmThreads) {
+        const double* p = part[begin + ch].v;
+#pragma unroll
+        for (int q = 0; q < N; ++q) v[q] += __ldcg(p + q);
+    }
+    block_sum<N>(v, smem);
+}
+
+// Publishes this CTA's chunk partial (written by thread 0 before the call)
+// and tells whether this CTA is the contract's last to do so: the partial is
+// fenced before the counter is bumped, the last CTA fences again before it
+// reads the others', and resets the counter for the next launch.  No CTA
+// waits on another.
+__device__ __forceinline__ bool last_chunk_of_contract(uint32_t* counter, uint32_t n_chunks, int* s_flag) {
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const uint32_t prev = atomicAdd(counter, 1u);
+        const bool last = prev == n_chunks - 1;
+        if (last) *counter = 0u;
+        *s_flag = last ? 1 : 0;
+    }
+    __syncthreads();
+    const bool last = *s_flag != 0;
+    if (last) __threadfence();
+    return last;
+}
+
+// ---------------------------------------------------------------------------
+// iteration k: exercise at date e, discount, and the regression sums of date
+// e-1 in the lagged basis -- or, when e = 1, the final Welford partial.  The
+// contract's last CTA folds the sums and solves date e-1.
+// ---------------------------------------------------------------------------
+// FP32: four CTAs per SM (64 registers; the rare per-date solve of thread 0
+// takes the few spills).
 template <int PREC>
-__global__ void __launch_bounds__(kLsmThreads)
-    lsm_exercise(int k, const LsmDev* __restrict__ cs,
-                 const uint32_t* __restrict__ chunk_contract, uint32_t total_chunks,
-                 const void* __restrict__ store, double* __restrict__ cf,
-                 const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_a,
-                 Welford* __restrict__ final_part) {
-    __shared__ double smem[kLsmThreads / 32][11];
-    __shared__ float2 scratch[11][kLsmThreads];  // FP32 path: the Gram sums' per-thread pairs
-    __shared__ double sres[11];
+__global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
+    lsm_step(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
+             uint32_t total_chunks, const void* __restrict__ store, double* __restrict__ cf,
+             LsmReg* __restrict__ reg, LsmPartial* __restrict__ part, Welford* __restrict__ final_part,
+             uint32_t* __restrict__ counters, double kappa_max) {
+    __shared__ double smem[kLsmThreads / 32][15];
+    __shared__ float2 scratch[15][kLsmThreads];  // FP32 path: the sums' per-thread pairs
+    __shared__ double sres[15];
     __shared__ Welford swf[kLsmThreads / 32];
     __shared__ Sum64 s64[kLsmThreads / 32];
+    __shared__ int s_last;
     const uint32_t chunk = blockIdx.x;
     if (chunk >= total_chunks) return;
-    const LsmDev c = cs[chunk_contract[chunk]];
+    const uint32_t ci = chunk_contract[chunk];
+    const LsmDev c = cs[ci];
     const int n = c.n_steps;
     const int e = n - k;
     if (e < 1) return;  // this contract has finished (uniform per CTA)
@@ -250,10 +468,15 @@ __global__ void __launch_bounds__(kLsmThreads)
     }
     const uint32_t local = chunk - c.chunk_begin;
     Welford w{0ull, 0.0, 0.0};
+    double out[15];
     if constexpr (PREC == 0) {
-        double acc[11];
+        // lagged preconditioner: date e's T (identity before the first regression)
+        double T[10];
 #pragma unroll
-        for (int q = 0; q < 11; ++q) acc[q] = 0.0;
+        for (int q = 0; q < 10; ++q) T[q] = init ? ((q == 0 || q == 4 || q == 7 || q == 9) ? 1.0 : 0.0) : re->T[q];
+        double acc[15];
+#pragma unroll
+        for (int q = 0; q < 15; ++q) acc[q] = 0.0;
         for (int j = 0; j < kLsmChunk / kLsmThreads; ++j) {
             const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
             if (i >= c.path_count) break;
@@ -283,46 +506,54 @@ __global__ void __launch_bounds__(kLsmThreads)
                 welford_add(w, v);
             } else {
                 cf[c.cf_offset + i] = v;
-                if (gram) {
-                    const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 2) * c.path_count + i);
-                    if (intrinsic(s, c.strike, c.type) > 0.0) {
-                        double b[4];
-                        basis64(s, c.strike, b);
-                        acc[0] += 1.0;
-                        acc[1] += b[0] * b[0];
-                        acc[2] += b[0] * b[1];
-                        acc[3] += b[0] * b[2];
-                        acc[4] += b[0] * b[3];
-                        acc[5] += b[1] * b[1];
-                        acc[6] += b[1] * b[2];
-                        acc[7] += b[1] * b[3];
-                        acc[8] += b[2] * b[2];
-                        acc[9] += b[2] * b[3];
-                        acc[10] += b[3] * b[3];
-                    }
+                const double s = load_s<PREC>(store, c.s_offset + static_cast<uint64_t>(e - 2) * c.path_count + i);
+                if (intrinsic(s, c.strike, c.type) > 0.0) {
+                    double b[4];
+                    basis64(s, c.strike, b);
+                    // b'_l = sum_{j <= l} b_j T[j][l]
+                    const double q0 = b[0] * T[0];
+                    const double q1 = b[0] * T[1] + b[1] * T[4];
+                    const double q2 = b[0] * T[2] + b[1] * T[5] + b[2] * T[7];
+                    const double q3 = b[0] * T[3] + b[1] * T[6] + b[2] * T[8] + b[3] * T[9];
+                    acc[0] += 1.0;
+                    acc[1] += q0 * q0;
+                    acc[2] += q0 * q1;
+                    acc[3] += q0 * q2;
+                    acc[4] += q0 * q3;
+                    acc[5] += q1 * q1;
+                    acc[6] += q1 * q2;
+                    acc[7] += q1 * q3;
+                    acc[8] += q2 * q2;
+                    acc[9] += q2 * q3;
+                    acc[10] += q3 * q3;
+                    acc[11] += q0 * v;
+                    acc[12] += q1 * v;
+                    acc[13] += q2 * v;
+                    acc[14] += q3 * v;
                 }
             }
         }
         if (gram) {
-            block_sum<11>(acc, smem);
-            if (threadIdx.x == 0) {
+            block_sum<15>(acc, smem);
 #pragma unroll
-                for (int q = 0; q < 11; ++q) part_a[chunk].v[q] = acc[q];
-            }
+            for (int q = 0; q < 15; ++q) out[q] = acc[q];
         }
     } else {
         // FP32 paths: FP32 cash flows (stored in the FP64 buffer's space),
-        // basis, continuation value, exercise tests and Gram products; the
-        // Gram sums and the final payoff sums up to the warp are
-        // compensated FP32, everything above FP64.
+        // basis, continuation value, exercise tests and products; the sums
+        // and the final payoff sums up to the warp are compensated FP32,
+        // everything above FP64.
         const float phi = c.phi_f, strike = c.strike_f, inv_kf = c.inv_strike_f, disc = c.disc_f;
         const float g0f = exercise ? re->gamma_f[0] : 0.0f, g1f = exercise ? re->gamma_f[1] : 0.0f,
                     g2f = exercise ? re->gamma_f[2] : 0.0f, g3f = exercise ? re->gamma_f[3] : 0.0f;
+        float T[10];
+#pragma unroll
+        for (int q = 0; q < 10; ++q) T[q] = init ? ((q == 0 || q == 4 || q == 7 || q == 9) ? 1.0f : 0.0f) : re->T_f[q];
         const float* S = static_cast<const float*>(store) + c.s_offset;
         float* cff = reinterpret_cast<float*>(cf) + c.cf_offset;
-        float hi[11], lo[11];
+        float hi[15], lo[15];
 #pragma unroll
-        for (int q = 0; q < 11; ++q) hi[q] = lo[q] = 0.0f;
+        for (int q = 0; q < 15; ++q) hi[q] = lo[q] = 0.0f;
         Sum32 fin{0u, 0.0f, 0.0f, 0.0f, 0.0f};  // final payoffs (last date)
         constexpr int kPer = kLsmChunk / kLsmThreads;
         // all loads of this thread's paths first (independent, in flight together)
@@ -361,20 +592,28 @@ __global__ void __launch_bounds__(kLsmThreads)
                 sum32_add(fin, v);
             } else {
                 cff[i] = v;
-                if (gram && phi * (sd[j] - strike) > 0.0f) {
+                if (phi * (sd[j] - strike) > 0.0f) {
                     float b[4];
                     basis32(sd[j], inv_kf, b);
+                    const float q0 = b[0] * T[0];
+                    const float q1 = __fmaf_rn(b[1], T[4], b[0] * T[1]);
+                    const float q2 = __fmaf_rn(b[2], T[7], __fmaf_rn(b[1], T[5], b[0] * T[2]));
+                    const float q3 = __fmaf_rn(b[3], T[9], __fmaf_rn(b[2], T[8], __fmaf_rn(b[1], T[6], b[0] * T[3])));
                     df_add(hi[0], lo[0], 1.0f);
-                    df_add(hi[1], lo[1], b[0] * b[0]);
-                    df_add(hi[2], lo[2], b[0] * b[1]);
-                    df_add(hi[3], lo[3], b[0] * b[2]);
-                    df_add(hi[4], lo[4], b[0] * b[3]);
-                    df_add(hi[5], lo[5], b[1] * b[1]);
-                    df_add(hi[6], lo[6], b[1] * b[2]);
-                    df_add(hi[7], lo[7], b[1] * b[3]);
-                    df_add(hi[8], lo[8], b[2] * b[2]);
-                    df_add(hi[9], lo[9], b[2] * b[3]);
-                    df_add(hi[10], lo[10], b[3] * b[3]);
+                    df_add(hi[1], lo[1], q0 * q0);
+                    df_add(hi[2], lo[2], q0 * q1);
+                    df_add(hi[3], lo[3], q0 * q2);
+                    df_add(hi[4], lo[4], q0 * q3);
+                    df_add(hi[5], lo[5], q1 * q1);
+                    df_add(hi[6], lo[6], q1 * q2);
+                    df_add(hi[7], lo[7], q1 * q3);
+                    df_add(hi[8], lo[8], q2 * q2);
+                    df_add(hi[9], lo[9], q2 * q3);
+                    df_add(hi[10], lo[10], q3 * q3);
+                    df_add(hi[11], lo[11], q0 * v);
+                    df_add(hi[12], lo[12], q1 * v);
+                    df_add(hi[13], lo[13], q2 * v);
+                    df_add(hi[14], lo[14], q3 * v);
                 }
             }
         }
@@ -382,14 +621,7 @@ __global__ void __launch_bounds__(kLsmThreads)
             const Sum32 r = sum32_warp_reduce(fin);
             if ((threadIdx.x & 31) == 0) s64[threadIdx.x >> 5] = sum32_wide(r);
         }
-        if (gram) {
-            double acc[11];
-            block_sum_df<11>(hi, lo, scratch, sres, acc);
-            if (threadIdx.x == 0) {
-#pragma unroll
-                for (int q = 0; q < 11; ++q) part_a[chunk].v[q] = acc[q];
-            }
-        }
+        if (gram) block_sum_df<15>(hi, lo, scratch, sres, out);
     }
     if (last) {
         if constexpr (PREC == 0) {
@@ -405,110 +637,47 @@ __global__ void __launch_bounds__(kLsmThreads)
             __syncthreads();
             if (threadIdx.x == 0) final_part[chunk] = sum64_fold<kLsmThreads / 32>(s64);
         }
-    }
-}
-
-// Upper-triangular index of (r, c), r <= c, in the packed 10-entry layout.
-__device__ __forceinline__ int tri(int r, int col) {
-    const int base[4] = {0, 4, 7, 9};
-    return base[r] + (col - r);
-}
-
-// Per contract: fold pass-A partials in chunk order, Cholesky, T = R^{-1}.
-__global__ void lsm_solve_a(int k, const LsmDev* __restrict__ cs, int n_contracts,
-                            const LsmPartial* __restrict__ part_a, LsmReg* __restrict__ reg) {
-    const int ci = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (ci >= n_contracts) return;
-    const LsmDev c = cs[ci];
-    const int date = c.n_steps - k - 1;  // regression date of this iteration
-    if (date < 1) return;
-    double s[11];
-#pragma unroll
-    for (int q = 0; q < 11; ++q) s[q] = 0.0;
-    for (uint32_t ch = lane; ch < c.n_chunks; ch += 32)
-#pragma unroll
-        for (int q = 0; q < 11; ++q) s[q] += part_a[c.chunk_begin + ch].v[q];
-#pragma unroll
-    for (int q = 0; q < 11; ++q)
-        for (int off = 16; off >= 1; off >>= 1) s[q] += __shfl_down_sync(0xffffffffu, s[q], off);
-    if (lane != 0) return;
-    LsmReg& r = reg[c.reg_offset + date];
-    r.has = 0;
-    r.degenerate = 0;
-    if (s[0] < 4.0) {  // too few in-the-money paths (src/pricers/lsm.cpp:102-104)
-        r.has = -1;
         return;
     }
-    double G[4][4];
-    for (int a = 0; a < 4; ++a)
-        for (int b2 = a; b2 < 4; ++b2) G[a][b2] = G[b2][a] = s[1 + tri(a, b2)];
-    double R[4][4] = {};
-    // R only preconditions pass B, so when the Gram matrix of the raw basis
-    // (condition up to ~1e13) is not numerically positive definite -- its
-    // sums carry ~44 bits on the FP32 path -- the factorisation is retried
-    // with a diagonal shift of 1e-10 of its trace (shifted Cholesky QR,
-    // Fukaya, Kannan, Nakatsukasa, Zhang and Yamamoto, SIAM J. Sci. Comput.
-    // 42 (2020)); pass B and the Householder solve then fit the unshifted
-    // problem.  A date that factorises without the shift is unaffected.
-    const double shift_step = 1e-10 * (G[0][0] + G[1][1] + G[2][2] + G[3][3]);
-    bool ok = false;
-    for (int attempt = 0; attempt < 2 && !ok; ++attempt) {
-        const double shift = attempt == 0 ? 0.0 : shift_step;
-        ok = true;
-        for (int j = 0; j < 4 && ok; ++j) {
-            double d = G[j][j] + shift;
-            for (int p = 0; p < j; ++p) d -= R[p][j] * R[p][j];
-            if (!(d > 0.0)) {
-                ok = false;
-                break;
-            }
-            R[j][j] = sqrt(d);
-            for (int l = j + 1; l < 4; ++l) {
-                double x = G[j][l];
-                for (int p = 0; p < j; ++p) x -= R[p][j] * R[p][l];
-                R[j][l] = x / R[j][j];
-            }
-        }
-        if (ok && attempt == 1) r.degenerate = 2;  // factorised with the shift
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < 15; ++q) part[chunk].v[q] = out[q];
     }
-    double T[4][4] = {};
-    if (ok) {
-        for (int j = 3; j >= 0; --j) {
-            T[j][j] = 1.0 / R[j][j];
-            for (int l = j + 1; l < 4; ++l) {
-                double x = 0.0;
-                for (int p = j; p < l; ++p) x += T[j][p] * R[p][l];
-                T[j][l] = -x / R[l][l];
-            }
+    if (!last_chunk_of_contract(&counters[2 * ci], c.n_chunks, &s_last)) return;
+    double tot[15];
+    fold_partials<15>(part, c.chunk_begin, c.n_chunks, tot, smem);
+    if (threadIdx.x == 0) {
+        double L[4][4];
+        if (init) {
+            for (int a = 0; a < 4; ++a)
+                for (int b2 = 0; b2 < 4; ++b2) L[a][b2] = a == b2 ? 1.0 : 0.0;
+        } else {
+            unpack_upper(re->T, L);
         }
-    } else {
-        for (int j = 0; j < 4; ++j) T[j][j] = 1.0;
-        r.degenerate = 1;
+        solve_lagged(tot, L, kappa_max, reg[c.reg_offset + e - 1]);
     }
-    for (int a = 0; a < 4; ++a)
-        for (int b2 = a; b2 < 4; ++b2) {
-            r.T[tri(a, b2)] = T[a][b2];
-            r.T_f[tri(a, b2)] = static_cast<float>(T[a][b2]);
-        }
 }
 
-// Pass B: Gram sums and right-hand side in the preconditioned basis b' = b T.
+// Second pass for the dates solve_lagged marked (has = 2): the sums in the
+// basis of that date's own preconditioner T, then the contract's last CTA
+// solves (has = 1).  CTAs of other contracts return at once.
 template <int PREC>
-__global__ void __launch_bounds__(kLsmThreads)
-    lsm_gram_b(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
+__global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
+    lsm_refine(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
                uint32_t total_chunks, const void* __restrict__ store, const double* __restrict__ cf,
-               const LsmReg* __restrict__ reg, LsmPartial* __restrict__ part_b) {
+               LsmReg* __restrict__ reg, LsmPartial* __restrict__ part, uint32_t* __restrict__ counters) {
     __shared__ double smem[kLsmThreads / 32][15];
     __shared__ float2 scratch[15][kLsmThreads];  // FP32 path: the sums' per-thread pairs
     __shared__ double sres[15];
+    __shared__ int s_last;
     const uint32_t chunk = blockIdx.x;
     if (chunk >= total_chunks) return;
-    const LsmDev c = cs[chunk_contract[chunk]];
+    const uint32_t ci = chunk_contract[chunk];
+    const LsmDev c = cs[ci];
     const int date = c.n_steps - k - 1;
     if (date < 1) return;
-    const LsmReg& r = reg[c.reg_offset + date];
-    if (r.has == -1) return;  // no regression at this date
+    LsmReg& r = reg[c.reg_offset + date];
+    if (r.has != 2) return;  // solved by the first pass, or no regression at this date
     const uint32_t local = chunk - c.chunk_begin;
     double out[15];
     if constexpr (PREC == 0) {
@@ -525,11 +694,10 @@ __global__ void __launch_bounds__(kLsmThreads)
             if (!(intrinsic(s, c.strike, c.type) > 0.0)) continue;
             double b[4];
             basis64(s, c.strike, b);
-            // b'_l = sum_{j <= l} b_j T[j][l]
-            double q0 = b[0] * T[0];
-            double q1 = b[0] * T[1] + b[1] * T[4];
-            double q2 = b[0] * T[2] + b[1] * T[5] + b[2] * T[7];
-            double q3 = b[0] * T[3] + b[1] * T[6] + b[2] * T[8] + b[3] * T[9];
+            const double q0 = b[0] * T[0];
+            const double q1 = b[0] * T[1] + b[1] * T[4];
+            const double q2 = b[0] * T[2] + b[1] * T[5] + b[2] * T[7];
+            const double q3 = b[0] * T[3] + b[1] * T[6] + b[2] * T[8] + b[3] * T[9];
             const double y = cf[c.cf_offset + i];
             acc[0] += 1.0;
             acc[1] += q0 * q0;
@@ -600,78 +768,21 @@ __global__ void __launch_bounds__(kLsmThreads)
     }
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int q = 0; q < 15; ++q) part_b[chunk].v[q] = out[q];
+        for (int q = 0; q < 15; ++q) part[chunk].v[q] = out[q];
     }
-}
-
-// 4x4 Householder least squares (the reference's algorithm, src/core/linalg.cpp:7-71,
-// on a square system): A is overwritten, y too.
-__device__ void householder4(double A[4][4], double y[4], double beta[4]) {
-    for (int kk = 0; kk < 4; ++kk) {
-        double norm_sq = 0.0;
-        for (int i = kk; i < 4; ++i) norm_sq += A[i][kk] * A[i][kk];
-        const double norm = sqrt(norm_sq);
-        if (norm == 0.0) continue;
-        const double akk = A[kk][kk];
-        const double alpha = akk >= 0.0 ? -norm : norm;
-        double v[4] = {0, 0, 0, 0};
-        v[kk] = akk - alpha;
-        for (int i = kk + 1; i < 4; ++i) v[i] = A[i][kk];
-        double vn = 0.0;
-        for (int i = kk; i < 4; ++i) vn += v[i] * v[i];
-        if (vn == 0.0) continue;
-        for (int jj = kk; jj < 4; ++jj) {
-            double dot = 0.0;
-            for (int i = kk; i < 4; ++i) dot += v[i] * A[i][jj];
-            const double f = 2.0 * dot / vn;
-            for (int i = kk; i < 4; ++i) A[i][jj] -= f * v[i];
+    if (!last_chunk_of_contract(&counters[2 * ci + 1], c.n_chunks, &s_last)) return;
+    double tot[15];
+    fold_partials<15>(part, c.chunk_begin, c.n_chunks, tot, smem);
+    if (threadIdx.x == 0) {
+        double T[4][4], gamma[4];
+        unpack_upper(r.T, T);
+        solve_preconditioned(tot, T, gamma);
+        for (int a = 0; a < 4; ++a) {
+            r.gamma[a] = gamma[a];
+            r.gamma_f[a] = static_cast<float>(gamma[a]);
         }
-        double dy = 0.0;
-        for (int i = kk; i < 4; ++i) dy += v[i] * y[i];
-        const double fy = 2.0 * dy / vn;
-        for (int i = kk; i < 4; ++i) y[i] -= fy * v[i];
+        r.has = 1;
     }
-    for (int i = 3; i >= 0; --i) {
-        double sum = y[i];
-        for (int jj = i + 1; jj < 4; ++jj) sum -= A[i][jj] * beta[jj];
-        const double diag = A[i][i];
-        beta[i] = diag != 0.0 ? sum / diag : 0.0;
-    }
-}
-
-__global__ void lsm_solve_b(int k, const LsmDev* __restrict__ cs, int n_contracts,
-                            const LsmPartial* __restrict__ part_b, LsmReg* __restrict__ reg) {
-    const int ci = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (ci >= n_contracts) return;
-    const LsmDev c = cs[ci];
-    const int date = c.n_steps - k - 1;
-    if (date < 1) return;
-    LsmReg& r = reg[c.reg_offset + date];
-    if (r.has == -1) return;
-    double s[15];
-#pragma unroll
-    for (int q = 0; q < 15; ++q) s[q] = 0.0;
-    for (uint32_t ch = lane; ch < c.n_chunks; ch += 32)
-#pragma unroll
-        for (int q = 0; q < 15; ++q) s[q] += part_b[c.chunk_begin + ch].v[q];
-#pragma unroll
-    for (int q = 0; q < 15; ++q)
-        for (int off = 16; off >= 1; off >>= 1) s[q] += __shfl_down_sync(0xffffffffu, s[q], off);
-    if (lane != 0) return;
-    double G[4][4], y[4], beta[4] = {0, 0, 0, 0};
-    for (int a = 0; a < 4; ++a)
-        for (int b2 = a; b2 < 4; ++b2) G[a][b2] = G[b2][a] = s[1 + tri(a, b2)];
-    for (int a = 0; a < 4; ++a) y[a] = s[11 + a];
-    householder4(G, y, beta);
-    // gamma = T beta
-    for (int a = 0; a < 4; ++a) {
-        double x = 0.0;
-        for (int b2 = a; b2 < 4; ++b2) x += r.T[tri(a, b2)] * beta[b2];
-        r.gamma[a] = x;
-        r.gamma_f[a] = static_cast<float>(x);
-    }
-    r.has = 1;
 }
 
 __global__ void lsm_finish(const LsmDev* __restrict__ cs, int n_contracts,
@@ -714,24 +825,25 @@ cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
 cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_contracts,
                                  const uint32_t* chunk_contract, uint32_t total_chunks, const void* s_store,
                                  double* cf, LsmReg* reg, LsmPartial* part_a, LsmPartial* part_b,
-                                 Welford* final_part, cudaStream_t stream) {
+                                 Welford* final_part, uint32_t* counters, cudaStream_t stream) {
+    (void)n_contracts;
     cudaGetLastError();
     if (total_chunks == 0) return cudaSuccess;
-    const int solve_blocks = (n_contracts * 32 + 127) / 128;
-    if (precision == 0)
-        lsm_exercise<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
-                                                                  reg, part_a, final_part);
-    else
-        lsm_exercise<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
-                                                                  reg, part_a, final_part);
-    lsm_solve_a<<<solve_blocks, 128, 0, stream>>>(k, c, n_contracts, part_a, reg);
-    if (precision == 0)
-        lsm_gram_b<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf, reg,
-                                                                part_b);
-    else
-        lsm_gram_b<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf, reg,
-                                                                part_b);
-    lsm_solve_b<<<solve_blocks, 128, 0, stream>>>(k, c, n_contracts, part_b, reg);
+    // Condition bound below which a date is solved from its lagged sums: FP64
+    // sums are good to ~1e-15, so 1e2 keeps the solve near FP64 accuracy; the
+    // FP32 path's compensated sums carry ~44 bits, and 1e4 keeps its
+    // coefficients far inside the FP32 basis' own rounding.
+    if (precision == 0) {
+        lsm_step<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
+                                                              reg, part_a, final_part, counters, 1e2);
+        lsm_refine<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
+                                                                reg, part_b, counters);
+    } else {
+        lsm_step<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
+                                                              reg, part_a, final_part, counters, 1e4);
+        lsm_refine<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
+                                                                reg, part_b, counters);
+    }
     return cudaGetLastError();
 }
 

@@ -35,20 +35,21 @@ constexpr int kLsmMaxGroups = 256;  // learned-regression CTAs per contract at m
 constexpr int kLsmMinGroupChunks = 32;  // chunks per learned-regression CTA at least (amortises its set-up)
 constexpr int kGramPacked = 66 * 67 / 2;  // upper triangle of the 66 x 66 Gram matrix, row-major
 
-// Regression state of one (contract, date): T = R1^{-1} (upper triangular,
+// Regression state of one (contract, date): T, the date's preconditioner
+// (upper triangular, T^T X^T X T = I for its in-the-money basis matrix X;
 // packed row-major: (0,0) (0,1) (0,2) (0,3) (1,1) (1,2) (1,3) (2,2) (2,3) (3,3)),
 // the Laguerre coefficients gamma, and flags.
 struct LsmReg {
     double T[10];
     double gamma[4];
-    int32_t has;          // coefficients valid at this date (>= 4 ITM paths)
-    int32_t degenerate;   // first-pass Cholesky: 0 plain, 2 with a diagonal shift, 1 failed (no preconditioning)
+    int32_t has;          // 1 coefficients valid (>= 4 ITM paths), -1 no regression, 2 second pass pending
+    int32_t degenerate;   // Cholesky of the lagged Gram matrix: 0 plain, 2 with a diagonal shift, 1 failed
     float T_f[10];        // FP32 copies for the FP32-path kernels (written with T and gamma)
     float gamma_f[4];
 };
 
-// Per-chunk partial sums.  Pass A: count + 10 Gram entries.  Pass B: count +
-// 10 preconditioned Gram entries + 4 right-hand side entries.  Final: Welford.
+// Per-chunk partial sums of one date's regression: count + 10 Gram entries +
+// 4 right-hand side entries in a preconditioned basis.
 struct LsmPartial {
     double v[16];
 };
@@ -75,7 +76,8 @@ cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
 cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_contracts,
                                  const uint32_t* chunk_contract, uint32_t total_chunks, const void* s_store,
                                  double* cf, LsmReg* reg, LsmPartial* part_a, LsmPartial* part_b,
-                                 Welford* final_part, cudaStream_t stream);
+                                 Welford* final_part, uint32_t* counters /* 2 per contract, zeroed */,
+                                 cudaStream_t stream);
 cudaError_t launch_lsm_finish(const LsmDev* c, int n_contracts, const Welford* final_part,
                               double* out /* n x 6: price, se, count, inception, mean, se */,
                               cudaStream_t stream);
