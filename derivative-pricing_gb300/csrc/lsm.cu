@@ -130,6 +130,28 @@ __device__ void block_sum_df(const float (&hi)[N], const float (&lo)[N], float2 
     }
 }
 
+// Chunk reduction of plain FP32 per-thread sums (the FP32 step's sums in a
+// well-conditioned basis): thread partials go to shared memory, warp w folds
+// sums w, w + W, ... (W warps): lane l adds threads l, l + 32, ... in that
+// order, then a shuffle tree; lane 0 widens the chunk's sum to FP64 in res.
+// FP32 up to the chunk (1024 paths), FP64 above.
+template <int N>
+__device__ void block_sum_f32(const float (&v)[N], float (*scratch)[kLsmThreads], double* res) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+#pragma unroll
+    for (int i = 0; i < N; ++i) scratch[i][t] = v[i];
+    __syncthreads();
+    for (int i = warp; i < N; i += kLsmThreads / 32) {
+        float x = scratch[i][lane];
+#pragma unroll
+        for (int u = 1; u < kLsmThreads / 32; ++u) x += scratch[i][lane + 32 * u];
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+        if (lane == 0) res[i] = static_cast<double>(x);
+    }
+    __syncthreads();
+}
+
 template <int PREC>
 __device__ __forceinline__ double load_s(const void* store, uint64_t idx) {
     if (PREC == 0) return static_cast<const double*>(store)[idx];
@@ -433,16 +455,19 @@ __device__ __forceinline__ bool last_chunk_of_contract(uint32_t* counter, uint32
 // e-1 in the lagged basis -- or, when e = 1, the final Welford partial.  The
 // contract's last CTA folds the sums and solves date e-1.
 // ---------------------------------------------------------------------------
-// FP32: four CTAs per SM (64 registers; the rare per-date solve of thread 0
-// takes the few spills).
-template <int PREC>
-__global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
+// COMP (FP32 path): the sums are compensated FP32 per thread and chunk (the
+// first iteration, whose basis is the raw Laguerre one); otherwise plain FP32
+// per thread and chunk -- the lagged basis is close to orthonormal, where
+// FP32 sums lose nothing the FP32 path data does not already carry.
+template <int PREC, bool COMP>
+__global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 8)
     lsm_step(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
              uint32_t total_chunks, const void* __restrict__ store, double* __restrict__ cf,
              LsmReg* __restrict__ reg, LsmPartial* __restrict__ part, Welford* __restrict__ final_part,
              uint32_t* __restrict__ counters, double kappa_max) {
     __shared__ double smem[kLsmThreads / 32][15];
-    __shared__ float2 scratch[15][kLsmThreads];  // FP32 path: the sums' per-thread pairs
+    __shared__ float2 scratch[COMP ? 15 : 1][kLsmThreads];  // compensated sums' per-thread pairs
+    __shared__ float pscratch[COMP ? 1 : 15][kLsmThreads];  // plain sums' per-thread values
     __shared__ double sres[15];
     __shared__ Welford swf[kLsmThreads / 32];
     __shared__ Sum64 s64[kLsmThreads / 32];
@@ -599,6 +624,24 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
                     const float q1 = __fmaf_rn(b[1], T[4], b[0] * T[1]);
                     const float q2 = __fmaf_rn(b[2], T[7], __fmaf_rn(b[1], T[5], b[0] * T[2]));
                     const float q3 = __fmaf_rn(b[3], T[9], __fmaf_rn(b[2], T[8], __fmaf_rn(b[1], T[6], b[0] * T[3])));
+                    if constexpr (!COMP) {
+                        hi[0] += 1.0f;  // exact: a chunk holds fewer than 2^24 paths
+                        hi[1] = __fmaf_rn(q0, q0, hi[1]);
+                        hi[2] = __fmaf_rn(q0, q1, hi[2]);
+                        hi[3] = __fmaf_rn(q0, q2, hi[3]);
+                        hi[4] = __fmaf_rn(q0, q3, hi[4]);
+                        hi[5] = __fmaf_rn(q1, q1, hi[5]);
+                        hi[6] = __fmaf_rn(q1, q2, hi[6]);
+                        hi[7] = __fmaf_rn(q1, q3, hi[7]);
+                        hi[8] = __fmaf_rn(q2, q2, hi[8]);
+                        hi[9] = __fmaf_rn(q2, q3, hi[9]);
+                        hi[10] = __fmaf_rn(q3, q3, hi[10]);
+                        hi[11] = __fmaf_rn(q0, v, hi[11]);
+                        hi[12] = __fmaf_rn(q1, v, hi[12]);
+                        hi[13] = __fmaf_rn(q2, v, hi[13]);
+                        hi[14] = __fmaf_rn(q3, v, hi[14]);
+                        continue;
+                    }
                     df_add(hi[0], lo[0], 1.0f);
                     df_add(hi[1], lo[1], q0 * q0);
                     df_add(hi[2], lo[2], q0 * q1);
@@ -621,7 +664,15 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
             const Sum32 r = sum32_warp_reduce(fin);
             if ((threadIdx.x & 31) == 0) s64[threadIdx.x >> 5] = sum32_wide(r);
         }
-        if (gram) block_sum_df<15>(hi, lo, scratch, sres, out);
+        if (gram) {
+            if constexpr (COMP) {
+                block_sum_df<15>(hi, lo, scratch, sres, out);
+            } else {
+                block_sum_f32<15>(hi, pscratch, sres);
+#pragma unroll
+                for (int q = 0; q < 15; ++q) out[q] = sres[q];
+            }
+        }
     }
     if (last) {
         if constexpr (PREC == 0) {
@@ -659,8 +710,9 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
 }
 
 // Second pass for the dates solve_lagged marked (has = 2): the sums in the
-// basis of that date's own preconditioner T, then the contract's last CTA
-// solves (has = 1).  CTAs of other contracts return at once.
+// basis of that date's own preconditioner T (compensated FP32 on the FP32
+// path), then the contract's last chunk solves (has = 1).  A small
+// persistent grid walks the chunks and skips those of other contracts.
 template <int PREC>
 __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
     lsm_refine(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
@@ -670,14 +722,13 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
     __shared__ float2 scratch[15][kLsmThreads];  // FP32 path: the sums' per-thread pairs
     __shared__ double sres[15];
     __shared__ int s_last;
-    const uint32_t chunk = blockIdx.x;
-    if (chunk >= total_chunks) return;
+    for (uint32_t chunk = blockIdx.x; chunk < total_chunks; chunk += gridDim.x) {
     const uint32_t ci = chunk_contract[chunk];
     const LsmDev c = cs[ci];
     const int date = c.n_steps - k - 1;
-    if (date < 1) return;
+    if (date < 1) continue;
     LsmReg& r = reg[c.reg_offset + date];
-    if (r.has != 2) return;  // solved by the first pass, or no regression at this date
+    if (r.has != 2) continue;  // solved by the first pass, or no regression at this date
     const uint32_t local = chunk - c.chunk_begin;
     double out[15];
     if constexpr (PREC == 0) {
@@ -770,18 +821,21 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
 #pragma unroll
         for (int q = 0; q < 15; ++q) part[chunk].v[q] = out[q];
     }
-    if (!last_chunk_of_contract(&counters[2 * ci + 1], c.n_chunks, &s_last)) return;
-    double tot[15];
-    fold_partials<15>(part, c.chunk_begin, c.n_chunks, tot, smem);
-    if (threadIdx.x == 0) {
-        double T[4][4], gamma[4];
-        unpack_upper(r.T, T);
-        solve_preconditioned(tot, T, gamma);
-        for (int a = 0; a < 4; ++a) {
-            r.gamma[a] = gamma[a];
-            r.gamma_f[a] = static_cast<float>(gamma[a]);
+    if (last_chunk_of_contract(&counters[2 * ci + 1], c.n_chunks, &s_last)) {
+        double tot[15];
+        fold_partials<15>(part, c.chunk_begin, c.n_chunks, tot, smem);
+        if (threadIdx.x == 0) {
+            double T[4][4], gamma[4];
+            unpack_upper(r.T, T);
+            solve_preconditioned(tot, T, gamma);
+            for (int a = 0; a < 4; ++a) {
+                r.gamma[a] = gamma[a];
+                r.gamma_f[a] = static_cast<float>(gamma[a]);
+            }
+            r.has = 1;
         }
-        r.has = 1;
+    }
+    __syncthreads();  // shared memory is reused by the next chunk
     }
 }
 
@@ -831,18 +885,30 @@ cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_co
     if (total_chunks == 0) return cudaSuccess;
     // Condition bound below which a date is solved from its lagged sums: FP64
     // sums are good to ~1e-15, so 1e2 keeps the solve near FP64 accuracy; the
-    // FP32 path's compensated sums carry ~44 bits, and 1e4 keeps its
-    // coefficients far inside the FP32 basis' own rounding.
+    // FP32 path's plain chunk sums are good to ~1e-8 relative once summed
+    // over the chunks, and 1e3 keeps its coefficients inside the rounding the
+    // FP32 basis values carry anyway.
+    // The second pass runs on a small persistent grid: its CTAs walk the
+    // chunks and skip those of contracts whose date needs no second pass.
+    const unsigned refine_grid = total_chunks < kRefineGrid ? total_chunks : kRefineGrid;
     if (precision == 0) {
-        lsm_step<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
-                                                              reg, part_a, final_part, counters, 1e2);
-        lsm_refine<0><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
-                                                                reg, part_b, counters);
+        if (k == 0)
+            lsm_step<0, true><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store,
+                                                                        cf, reg, part_a, final_part, counters, 1e2);
+        else
+            lsm_step<0, false><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store,
+                                                                         cf, reg, part_a, final_part, counters, 1e2);
+        lsm_refine<0><<<refine_grid, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
+                                                               reg, part_b, counters);
     } else {
-        lsm_step<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
-                                                              reg, part_a, final_part, counters, 1e4);
-        lsm_refine<1><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
-                                                                reg, part_b, counters);
+        if (k == 0)
+            lsm_step<1, true><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store,
+                                                                        cf, reg, part_a, final_part, counters, 1e3);
+        else
+            lsm_step<1, false><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store,
+                                                                         cf, reg, part_a, final_part, counters, 1e3);
+        lsm_refine<1><<<refine_grid, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
+                                                               reg, part_b, counters);
     }
     return cudaGetLastError();
 }

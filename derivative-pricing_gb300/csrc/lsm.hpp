@@ -9,7 +9,8 @@
 namespace mcdg {
 
 constexpr int kLsmChunk = 1024;      // paths per chunk (fixed reduction unit)
-constexpr int kLsmThreads = 256;     // 4 paths per thread per chunk
+constexpr int kLsmThreads = 128;     // 8 paths per thread per chunk
+constexpr unsigned kRefineGrid = 1216;  // CTAs of the second regression pass (8 per SM)
 constexpr int kLsmBasis = 4;         // weighted Laguerre, degree 3 (src/pricers/lsm.cpp:16-25)
 
 // One American contract.  Paths are stored date-major: S[d-1][i] for dates

@@ -193,11 +193,11 @@ __device__ void replay32(const LsmDev& c, const FrozenDev& f, const LsmReg* __re
 
 // Per chunk: NS scenario averages (and, for the five-scenario form, the
 // per-path central differences of delta, gamma and vega) as Welford partials.
-// The FP32 five-scenario form runs 3 CTAs per SM (80 registers; measured
-// 1.3x faster than 2 CTAs at 106 registers on the 20-put grid: paths that
-// exercise early leave the pass latency-bound).
+// The FP32 five-scenario form runs 384 threads per SM at most 85 registers
+// each (measured 1.3x faster than 512 threads at 106 registers on the 20-put
+// grid: paths that exercise early leave the pass latency-bound).
 template <int PREC, int NS>
-__global__ void __launch_bounds__(kLsmThreads, (PREC == 1 && NS > 1) ? 3 : 2)
+__global__ void __launch_bounds__(kLsmThreads, ((PREC == 1 && NS > 1) ? 3 : 2) * (256 / kLsmThreads))
     lsm_frozen_stream(const LsmDev* __restrict__ cs, const FrozenDev* __restrict__ fz,
                       const uint32_t* __restrict__ chunk_contract, uint32_t total_chunks,
                       const LsmReg* __restrict__ reg, Welford* __restrict__ part) {
