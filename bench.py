@@ -98,6 +98,35 @@ def path_steps(c):
     return float((steps * c["path_count"].astype(np.float64)).sum())
 
 
+# The path kernel's instruction count and DRAM traffic, measured by ncu on the
+# 256-contract case (`bench.py --case path --launch-shape V,0`: the second
+# price_batch launch, metrics smsp__inst_executed.sum, dram__bytes_read.sum and
+# dram__bytes_write.sum) for each register variant V, together with the digest
+# of the sources they were measured on.  The roofline below uses them only
+# while the sources still have that digest; otherwise it reports the
+# instruction-based figures as unmeasured (null) rather than stale.
+PATH_KERNEL_SOURCES = ("derivative-pricing_gb300/csrc/gbm_paths.cu",
+                       "derivative-pricing_gb300/csrc/device_common.cuh",
+                       "derivative-pricing_gb300/csrc/engine.hpp")
+PATH_KERNEL_PROFILE = {
+    "sources": "cf6ad0a85d243b5d",
+    "case_path_steps": 6807363601.0,
+    # variant -> smsp__inst_executed.sum of one launch
+    "warp_inst": {"0": 15676824749, "1": 17989424263, "2": 20430087044, "3": 15839904527, "4": 16405233406},
+    # variant -> dram__bytes_read.sum + dram__bytes_write.sum of one launch
+    "dram_bytes": {"0": 181760, "1": 353792, "2": 587776, "3": 9074432, "4": 153344},
+}
+
+
+def sources_digest(paths=PATH_KERNEL_SOURCES):
+    import hashlib
+    h = hashlib.sha256()
+    for rel in paths:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
 
@@ -149,7 +178,10 @@ class ClockSampler:
 def cpu_baseline_sample(c, budget_s=12.0):
     """Times the CPU port (bit-identical restatement of the reference) on a
     stratified sample of the batch, each contract on all host threads over the
-    reference's fixed chunk partition (its own multithreaded path)."""
+    reference's fixed chunk partition (its own multithreaded path).  The rate
+    is measured in path-steps/s, which does not depend on the sample's mix of
+    step counts, and turned into the full batch's paths/s through the batch's
+    own path-steps per path (the time the CPU would take for the whole batch)."""
     import oracle as O
     orc = O.load()
     threads = os.cpu_count() or 1
@@ -170,10 +202,16 @@ def cpu_baseline_sample(c, budget_s=12.0):
     orc.orc_price_batch(arr, len(sample), threads, 0, out)
     dt = time.perf_counter() - t0
     paths = float(sample["path_count"].astype(np.float64).sum())
-    return {"value": paths / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{len(sample)} of 4096 contracts (every {k}th by cost), {paths:.3g} paths, "
-                      f"{path_steps(sample):.3g} path-steps, {dt:.2f} s",
-            "path_steps_per_s": path_steps(sample) / dt}
+    rate = path_steps(sample) / dt
+    full_s = path_steps(c) / rate
+    return {"value": float(c["path_count"].astype(np.float64).sum()) / full_s, "unit": UNIT, "cores": threads,
+            "kind": "port",
+            "sample": f"{len(sample)} of {len(c)} contracts (every {k}th by cost), {paths:.3g} paths, "
+                      f"{path_steps(sample):.3g} path-steps, {dt:.2f} s; paths/s of the whole batch at the "
+                      f"sample's path-steps/s",
+            "path_steps_per_s": rate, "full_batch_s_extrapolated": full_s,
+            "build": "oracle/Makefile: -O3, -mcpu=native on aarch64 (-march=native elsewhere), "
+                     "-ffp-contract=off"}
 
 
 def lsm_grid():
@@ -196,11 +234,32 @@ def _timed(fn, reps=2):
     return out, min(ts)
 
 
-def bench_lsm(eng):
+def lsm_algorithmic_bytes(g):
+    """Algorithmic HBM bytes of Longstaff-Schwartz per contract: N (4 (D+1) +
+    20 D) -- the FP32 paths written once, one date column read and FP64 cash
+    flows read and written per date."""
+    n = g["path_count"].astype(np.float64)
+    d = g["monitoring_points"].astype(np.float64)
+    return float((n * (4.0 * (d + 1) + 20.0 * d)).sum())
+
+
+def hbm_roofline(bytes_, seconds, peaks):
+    peak = peaks.get("hbm_gbs")
+    achieved = bytes_ / seconds / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if peak else None, "algorithmic_bytes": bytes_,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peak else None,
+            "note": "algorithmic bytes over the wall time of the whole call (forward simulation, "
+                    "backward pass, copies)"}
+
+
+def bench_lsm(eng, peaks):
     """Time-to-price of the 20-put grid: plain FP64 GPU path (QR, FP64 paths),
     FP32 QR, and the learned regression (FP32 paths, BF16 tensor-core network).
     Errors are measured against the FP64 result (the reference's arithmetic,
-    parity-tested to 1e-10) in units of its standard error."""
+    parity-tested to 1e-12 at this size) in units of its standard error, and
+    against the exact 50-date Bermudan value (a 5000-step CRR lattice with
+    exercise at the LSM dates)."""
     g = lsm_grid()
     r64, t64 = _timed(lambda: eng.lsm_batch(g, "fp64", "qr"))
     r32, t32 = _timed(lambda: eng.lsm_batch(g, "fp32", "qr"))
@@ -211,6 +270,8 @@ def bench_lsm(eng):
     eml = np.abs(rml["price"] - r64["price"]) / se
     tree = np.array([M.crr_binomial_american(r["spot"], r["strike"], r["rate"], r["carry_yield"], r["vol"],
                                              r["time"], 2000, 1) for r in g])
+    berm = np.array([M.crr_binomial_bermudan(r["spot"], r["strike"], r["rate"], r["carry_yield"], r["vol"],
+                                             r["time"], int(r["monitoring_points"]), 100, 1) for r in g])
     # Out of sample: both fitted policies replayed on the same fresh paths
     # (seed + 10^7), so foresight bias is gone and the better policy earns more.
     mlp_pol = [eng.mlp_policy(i, int(r["monitoring_points"])) for i, r in enumerate(g)]
@@ -226,12 +287,27 @@ def bench_lsm(eng):
         oos_ml.append(ml_oos.price)
         oos_se.append(ml_oos.standard_error)
     gain = (np.array(oos_ml) - np.array(oos_qr)) / np.array(oos_se)
+    zb = lambda p: (p - berm) / se  # noqa: E731
+    nbytes = lsm_algorithmic_bytes(g)
     return {"workload": "20 American puts (S0 36..44, sigma .2/.4, T 1/2), 50 dates, 2^20 paths each",
             "fp64_qr_s": t64, "fp32_qr_s": t32, "learned_s": tml,
             "speedup_learned_over_fp64": t64 / tml, "speedup_fp32_qr_over_fp64": t64 / t32,
             "learned_err_vs_fp64_max_se": float(eml.max()), "learned_err_vs_fp64_mean_se": float(eml.mean()),
+            "learned_minus_fp64_mean_se": float(((rml["price"] - r64["price"]) / se).mean()),
             "fp32_qr_err_vs_fp64_max_se": float(e32.max()),
             "learned_fallbacks": int((rml["reserved"] != 0).sum()),
+            "roofline_fp32_qr": hbm_roofline(nbytes, t32, peaks),
+            "roofline_learned": hbm_roofline(nbytes, tml, peaks),
+            "vs_bermudan_lattice": {
+                "note": "z = (in-sample LSM price - exact 50-date Bermudan value) / SE; the lattice is the "
+                        "value LSM estimates, so |z| follows the Monte Carlo error plus each regression's "
+                        "policy loss and foresight bias",
+                "fp64_qr_max_abs_z": float(np.abs(zb(r64["price"])).max()),
+                "fp64_qr_mean_abs_z": float(np.abs(zb(r64["price"])).mean()),
+                "fp32_qr_max_abs_z": float(np.abs(zb(r32["price"])).max()),
+                "learned_max_abs_z": float(np.abs(zb(rml["price"])).max()),
+                "learned_mean_abs_z": float(np.abs(zb(rml["price"])).mean()),
+                "learned_mean_z": float(zb(rml["price"]).mean()), "fp64_qr_mean_z": float(zb(r64["price"]).mean())},
             "vs_crr_tree_2000": {
                 "note": "in-sample LSM prices against the American lattice price; the 50-date Bermudan "
                         "and the in-sample foresight bias both enter",
@@ -244,8 +320,8 @@ def bench_lsm(eng):
                         "fresh 2^20 paths per put; difference learned - QR in units of the replay's standard error",
                 "learned_minus_qr_min_se": float(gain.min()), "learned_minus_qr_mean_se": float(gain.mean()),
                 "learned_minus_qr_max_se": float(gain.max()),
-                "learned_mean_abs_err_vs_tree": float(np.mean(np.abs(np.array(oos_ml) - tree))),
-                "qr_mean_abs_err_vs_tree": float(np.mean(np.abs(np.array(oos_qr) - tree)))},
+                "learned_mean_abs_err_vs_bermudan": float(np.mean(np.abs(np.array(oos_ml) - berm))),
+                "qr_mean_abs_err_vs_bermudan": float(np.mean(np.abs(np.array(oos_qr) - berm)))},
             "timing": "wall clock of one mcd_lsm_batch call (host arrays, graph capture and copies included), "
                       "best of 2 after a warm-up"}
 
@@ -259,7 +335,7 @@ def risk_batch(n=1024, seed=42):
     return c
 
 
-def bench_risk(eng):
+def bench_risk(eng, peaks):
     """Batched risk: price, CRN finite-difference delta/gamma/vega (bump 1e-4
     relative), pathwise and likelihood-ratio Greeks of 1024 Asian/barrier
     contracts in one graph launch; learned LSM on 512 American puts with
@@ -285,10 +361,23 @@ def bench_risk(eng):
     ml, tl = _timed(lambda: eng.lsm_batch(puts, "fp32", "mlp"), reps=1)
     qr, tq = _timed(lambda: eng.lsm_batch(puts, "fp32", "qr"), reps=1)
     ag, ta = _timed(lambda: eng.lsm_greeks_batch(puts, 0.01, 0.01, "fp32"), reps=1)
+    # FP32 against FP64 (the reference's arithmetic, same draws) on every 32nd contract
+    sub = c[::32]
+    g32 = eng.greeks_batch(sub, 1e-4, 1e-4, "fp32")
+    g64 = eng.greeks_batch(sub, 1e-4, 1e-4, "fp64")
+    fp32_err = {}
+    for name in M.GREEK_NAMES:
+        ok = g64[name][:, 1] > 0
+        if ok.any():
+            fp32_err[name] = float((np.abs(g32[name][ok, 0] - g64[name][ok, 0]) / g64[name][ok, 1]).max())
     return {"greeks": {"contracts": len(c), "s": tg, "contracts_per_second": len(c) / tg,
                        "path_steps_per_second": steps / tg, "launch_shape": {"variant": v, "ctas_per_sm": ctas},
-                       "outputs": "price, FD delta/gamma/vega, pathwise delta/vega/rho, LR delta/gamma/vega/rho"},
+                       "outputs": "price, FD delta/gamma/vega, pathwise delta/vega/rho, LR delta/gamma/vega/rho",
+                       "fp32_err_vs_fp64_max_se": fp32_err,
+                       "fp32_err_sample": f"{len(sub)} contracts (every 32nd), same launch in FP64"},
             "learned_lsm_512": {"s": tl, "contracts_per_second": n / tl, "qr_s": tq,
+                                "roofline": hbm_roofline(lsm_algorithmic_bytes(puts), tl, peaks),
+                                "roofline_qr": hbm_roofline(lsm_algorithmic_bytes(puts), tq, peaks),
                                 "max_abs_diff_vs_qr_in_se": float(np.max(np.abs(ml["price"] - qr["price"]) /
                                                                          qr["standard_error"])),
                                 "fallbacks": int((ml["reserved"] != 0).sum())},
@@ -315,8 +404,17 @@ def bench_heston(eng, n_sets=256):
     strikes = np.linspace(70.0, 130.0, 64)
     out, t = _timed(lambda: eng.heston_qe_batch(sets, strikes, 0, 252, 1 << 20, 42, "fp32"), reps=1)
     steps = float(n_sets) * 252 * (1 << 20)
+    # every price against the semi-analytic Heston price (the configuration's check)
+    z = np.zeros((n_sets, len(strikes)))
+    for i, row in enumerate(sets):
+        hp = M.HestonParams(*[float(row[f]) for f in M.HESTON_DTYPE.names])
+        for j, k in enumerate(strikes):
+            z[i, j] = (out["price"][i, j] - M.heston_semi_analytic(hp, float(k), 0)) / out["standard_error"][i, j]
     return {"sets": n_sets, "strikes": 64, "s": t, "paths_per_second": n_sets * (1 << 20) / t,
-            "path_steps_per_second": steps / t, "prices_per_second": n_sets * 64 / t}
+            "path_steps_per_second": steps / t, "prices_per_second": n_sets * 64 / t,
+            "vs_semi_analytic": {"prices": int(z.size), "max_abs_z": float(np.abs(z).max()),
+                                 "mean_z": float(z.mean()), "share_abs_z_over_3": float((np.abs(z) > 3).mean()),
+                                 "note": "z = (QE price - semi-analytic price) / SE, FP32 paths, 252 steps"}}
 
 
 def bench_qmc(eng, c):
@@ -350,7 +448,7 @@ def bench_european_1e6(eng):
 PROFILE_CASES = ("path", "greeks", "qmc", "heston", "lsm", "lsm_grid", "mlp", "mlp_grid", "american_greeks")
 
 
-def run_case(case):
+def run_case(case, launch_shape=None):
     """Small fixed workloads for profiling one kernel family (each priced twice:
     the second launch is the one to capture).  Sizes keep an ncu capture short:
       path      256 contracts of the batch configuration (FP32)
@@ -364,6 +462,9 @@ def run_case(case):
       american_greeks  the 20-put grid: QR fit, then frozen-boundary Greeks (FP32)"""
     import mcd_gpu as M
     eng = M.Engine(0)
+    if launch_shape:
+        v, cps = (int(x) for x in launch_shape.split(","))
+        eng.set_launch_shape("fp32", v, cps)
     for _ in range(2):
         if case == "path":
             r = eng.price_batch(make_batch(256), "fp32")["price"]
@@ -443,7 +544,7 @@ def main():
                     help="batch size (the configuration is 4096; smaller only for profiling)")
     args = ap.parse_args()
     if args.case:
-        return run_case(args.case)
+        return run_case(args.case, args.launch_shape)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -542,17 +643,17 @@ def main():
                    "launch_shape": {"variant": variant, "ctas_per_sm": ctas}},
         "contracts_per_second": world * n / (ms / 1e3),
         "path_steps_per_second": world * total_steps / (ms / 1e3),
-        "gpu_launches": 2 * args.steps,
+        # per step: the contract digest, the persistent path kernel and the merge
+        "gpu_launches": 3 * args.steps,
         "e2e": {"value": world * total_paths / (e2e / 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": n * 152 + (n + 1) * 4,
                 "d2h_bytes_per_step": n * M.RESULT_DTYPE.itemsize + 8},
     }
     # Roofline of the persistent path kernel.  It is ALU-bound (no path data in
     # memory), so the bound is instruction issue: 4 SMSPs x 1 warp-instruction
-    # per clock per SM.  Instructions per path-step are measured by ncu on the
-    # same kernel without register spills (profiles/path_kernel_fp32_batch.md:
-    # 1.5677e10 warp instructions for 6.807e9 path-steps = 73.7 thread-instructions
-    # each; the spilling variants issue ~1 % more).
+    # per clock per SM at the SM clock sampled during the timed region.  The
+    # instructions per path-step and the DRAM bytes per contract come from the
+    # ncu capture of the same sources and register variant (PATH_KERNEL_PROFILE).
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -562,20 +663,22 @@ def main():
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     clk = clocks.summary()
     mhz = clk["sm_mhz"] or peaks.get("sm_max_mhz", 2070.0)
-    inst_per_step = 73.7
-    achieved = total_steps * inst_per_step / 32.0 / (kernel_ms / 1e3) / 1e12
     peak = sm_count * 4 * mhz * 1e6 / 1e12
+    prof = PATH_KERNEL_PROFILE
+    digest = sources_digest()
+    fresh = prof["sources"] == digest and str(variant) in prof["warp_inst"]
+    inst_per_step = (prof["warp_inst"][str(variant)] * 32.0 / prof["case_path_steps"]) if fresh else None
+    achieved = (total_steps * inst_per_step / 32.0 / (kernel_ms / 1e3) / 1e12) if fresh else None
     line["roofline"] = {
         "bound": "alu", "achieved": achieved, "peak": peak, "unit": "Twarp-inst/s",
-        "frac": achieved / peak,
-        # DRAM bytes of the 256-contract ncu capture at the tuned launch shape
-        # (2,798,336 B: contract records, slab partials and register spills of the
-        # 32-register variant), scaled by contracts.
-        "traffic": 2798336.0 * n / 256.0,
+        "frac": (achieved / peak) if fresh else None,
+        "traffic": (prof["dram_bytes"][str(variant)] * n / 256.0) if fresh else None,
         "kernel_ms": kernel_ms, "launches": launches,
         "path_steps_per_second_kernel": total_steps / (kernel_ms / 1e3),
-        "note": "issue-slot roofline (4 warp-inst/clk/SM at the sampled SM clock); "
-                "73.7 thread-instructions per path-step measured by ncu; "
+        "inst_per_path_step": inst_per_step, "sources_digest": digest, "profiled_digest": prof["sources"],
+        "note": "issue-slot roofline (4 warp-inst/clk/SM at the sampled SM clock); thread-instructions per "
+                "path-step and DRAM bytes from an ncu capture of these sources and this register variant "
+                "(256 contracts, traffic scaled by contracts); null when the sources changed since; "
                 "no HBM or tensor-core bound applies to this kernel"}
     line["clocks"] = clk
 
@@ -595,17 +698,23 @@ def main():
             "sample": f"{len(sub)} contracts (every 64th by cost)",
             "fp64_kernel_ms": k64, "fp32_kernel_ms": k32, "speedup_fp32_over_fp64": k64 / k32,
             "fp64_paths_per_second": float(sub["path_count"].astype(np.float64).sum()) / (k64 / 1e3),
+            "fp64_path_steps_per_second": path_steps(sub) / (k64 / 1e3),
             "fp32_err_vs_fp64_max_se": float(err.max()), "fp32_err_vs_fp64_mean_se": float(err.mean()),
             "fp64_wall_s": t64}
         assert r32b.tobytes() == r32.tobytes()
     if not args.no_extra and rank == 0:
-        line["lsm"] = bench_lsm(eng)
-        line["risk"] = bench_risk(eng)
+        line["lsm"] = bench_lsm(eng, peaks)
+        line["risk"] = bench_risk(eng, peaks)
         line["heston"] = bench_heston(eng)
         line["qmc"] = bench_qmc(eng, c)
         line["european_1e6"] = bench_european_1e6(eng)
     if not args.no_cpu and rank == 0:
         line["cpu_baseline"] = cpu_baseline_sample(c)
+        if "fp64_gpu" in line:
+            # like for like: the reference's FP64 arithmetic on the GPU against
+            # the same algorithm on the host cores, in path-steps/s
+            g = line["fp64_gpu"]["fp64_path_steps_per_second"]
+            line["cpu_baseline"]["fp64_gpu_over_cpu"] = g / line["cpu_baseline"]["path_steps_per_s"]
     if rank == 0:
         print(json.dumps(line))
     eng.close()

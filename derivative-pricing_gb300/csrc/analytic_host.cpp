@@ -273,6 +273,38 @@ int mcd_crr_binomial(double spot, double strike, double rate, double carry_yield
     return MCD_ERR_OUT_OF_MEMORY;
 }
 
+// Bermudan CRR lattice (no reference counterpart): exercise only at the
+// levels steps_per_date * j, j = 0..dates-1 (t = 0 included, as the
+// reference's LSM decides at inception), the European payoff at maturity.
+// Node values come from a table of powers of u (one pow per level offset).
+double mcd_crr_binomial_bermudan(double spot, double strike, double rate, double carry_yield, double vol,
+                                 double time, int exercise_dates, int steps_per_date, int type) try {
+    if (exercise_dates < 1 || steps_per_date < 1 || exercise_dates > (1 << 20) / steps_per_date)
+        return std::nan("");
+    const int steps = exercise_dates * steps_per_date;
+    const double dt = time / static_cast<double>(steps);
+    const double u = std::exp(vol * std::sqrt(dt));
+    const double d = 1.0 / u;
+    const double p = (std::exp((rate - carry_yield) * dt) - d) / (u - d);
+    const double disc = std::exp(-rate * dt);
+    const double phi = sgn(type);
+    std::vector<double> upow(2 * static_cast<size_t>(steps) + 1);
+    for (int k = -steps; k <= steps; ++k) upow[static_cast<size_t>(k + steps)] = std::pow(u, static_cast<double>(k));
+    auto node = [&](int level, int i) { return spot * upow[static_cast<size_t>(2 * i - level + steps)]; };
+    std::vector<double> v(static_cast<size_t>(steps) + 1);
+    for (int i = 0; i <= steps; ++i) v[i] = std::max(phi * (node(steps, i) - strike), 0.0);
+    for (int level = steps - 1; level >= 0; --level) {
+        const bool exercise = level % steps_per_date == 0;
+        for (int i = 0; i <= level; ++i) {
+            const double cont = disc * (p * v[i + 1] + (1.0 - p) * v[i]);
+            v[i] = exercise ? std::max(cont, std::max(phi * (node(level, i) - strike), 0.0)) : cont;
+        }
+    }
+    return v[0];
+} catch (...) {
+    return std::nan("");
+}
+
 // heston.cpp:48-82: Heston (1993) P1/P2 as integrals over [0, 200] by
 // 128-point Gauss-Legendre; the put from parity.
 double mcd_heston_semi_analytic(const mcd_heston_params* params, double strike, int type) try {

@@ -268,6 +268,42 @@ __device__ bool chol4(const double G[4][4], double shift, double R[4][4]) {
     return true;
 }
 
+// The same factorisation without divisions (FP64 division and square root
+// are long software sequences on this GPU's FP64 pipe): one reciprocal square
+// root per pivot, rinv[j] = 1 / R[j][j].
+__device__ bool chol4_rsqrt(const double G[4][4], double R[4][4], double rinv[4]) {
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = 0; b2 < 4; ++b2) R[a][b2] = 0.0;
+    for (int j = 0; j < 4; ++j) {
+        double d = G[j][j];
+        for (int p = 0; p < j; ++p) d -= R[p][j] * R[p][j];
+        if (!(d > 0.0)) return false;
+        const double r = rsqrt(d);
+        rinv[j] = r;
+        R[j][j] = d * r;
+        for (int l = j + 1; l < 4; ++l) {
+            double x = G[j][l];
+            for (int p = 0; p < j; ++p) x -= R[p][j] * R[p][l];
+            R[j][l] = x * r;
+        }
+    }
+    return true;
+}
+
+// T = R^{-1} from the pivots' reciprocals.
+__device__ void inv_upper4_rinv(const double R[4][4], const double rinv[4], double T[4][4]) {
+    for (int a = 0; a < 4; ++a)
+        for (int b2 = 0; b2 < 4; ++b2) T[a][b2] = 0.0;
+    for (int j = 3; j >= 0; --j) {
+        T[j][j] = rinv[j];
+        for (int l = j + 1; l < 4; ++l) {
+            double x = 0.0;
+            for (int p = j; p < l; ++p) x += T[j][p] * R[p][l];
+            T[j][l] = -x * rinv[l];
+        }
+    }
+}
+
 // T = R^{-1} for upper-triangular R.
 __device__ void inv_upper4(const double R[4][4], double T[4][4]) {
     for (int a = 0; a < 4; ++a)
@@ -352,15 +388,17 @@ __device__ void solve_preconditioned(const double s[15], const double P[4][4], d
 // preconditioner L (the next later date's T).  Cholesky of G' = R^T R gives
 // this date's preconditioner T = L R^{-1} (so that T^T X^T X T = I).  When G'
 // is well conditioned (cond bound ||R||_F^2 ||R^-1||_F^2 <= kappa_max) the
-// date is solved here: has = 1.  Otherwise T is stored and the date is marked
-// for a second pass in the basis X T (has = 2): that pass and its solve are
-// Cholesky-QR2.  The first regression date (L = I, the raw Laguerre Gram
-// matrix, condition up to ~1e13) always takes it; where that raw matrix is not
-// numerically positive definite (its FP32-path sums carry ~44 bits) the
+// date is solved here from the same factor, beta = R^{-1} R^{-T} h and
+// gamma = L beta: has = 1.  Otherwise T is stored and the date is marked for
+// a second pass in the basis X T (has = 2): that pass and its Householder
+// solve are Cholesky-QR2.  The first regression date (L = I, the raw Laguerre
+// Gram matrix, condition up to ~1e13) always takes it; where that raw matrix
+// is not numerically positive definite (its FP32-path sums carry ~44 bits) the
 // factorisation is retried with a diagonal shift of 1e-10 of the trace --
 // shifted Cholesky QR (Fukaya, Kannan, Nakatsukasa, Zhang and Yamamoto, SIAM
 // J. Sci. Comput. 42 (2020)) -- and the second pass fits the unshifted problem.
-__device__ void solve_lagged(const double s[15], const double L[4][4], double kappa_max, LsmReg& r) {
+__device__ void solve_lagged(const double s[15], const double L[4][4], double kappa_max, LsmReg& r,
+                             uint32_t* need_second_pass) {
     if (s[0] < 4.0) {  // too few in-the-money paths (src/pricers/lsm.cpp:102-104)
         r.has = -1;
         r.degenerate = 0;
@@ -370,11 +408,11 @@ __device__ void solve_lagged(const double s[15], const double L[4][4], double ka
     double G[4][4];
     for (int a = 0; a < 4; ++a)
         for (int b2 = a; b2 < 4; ++b2) G[a][b2] = G[b2][a] = s[1 + tri(a, b2)];
-    double R[4][4], Ri[4][4], T[4][4];
-    bool ok = chol4(G, 0.0, R);
+    double R[4][4], Ri[4][4], T[4][4], rinv[4];
+    bool ok = chol4_rsqrt(G, R, rinv);
     double kappa = 1e300;
     if (ok) {
-        inv_upper4(R, Ri);
+        inv_upper4_rinv(R, rinv, Ri);
         double fr = 0.0, fi = 0.0;
         for (int a = 0; a < 4; ++a)
             for (int b2 = a; b2 < 4; ++b2) {
@@ -403,15 +441,27 @@ __device__ void solve_lagged(const double s[15], const double L[4][4], double ka
     }
     store_T(r, T);
     if (r.degenerate == 0 && kappa <= kappa_max) {
-        double gamma[4];
-        solve_preconditioned(s, L, gamma);
-        for (int a = 0; a < 4; ++a) {
-            r.gamma[a] = gamma[a];
-            r.gamma_f[a] = static_cast<float>(gamma[a]);
+        double w[4], beta[4];
+        for (int l = 0; l < 4; ++l) {  // w = R^{-T} h
+            double x = 0.0;
+            for (int p = 0; p <= l; ++p) x += Ri[p][l] * s[11 + p];
+            w[l] = x;
+        }
+        for (int a = 0; a < 4; ++a) {  // beta = R^{-1} w
+            double x = 0.0;
+            for (int b2 = a; b2 < 4; ++b2) x += Ri[a][b2] * w[b2];
+            beta[a] = x;
+        }
+        for (int a = 0; a < 4; ++a) {  // gamma = L beta
+            double x = 0.0;
+            for (int b2 = a; b2 < 4; ++b2) x += L[a][b2] * beta[b2];
+            r.gamma[a] = x;
+            r.gamma_f[a] = static_cast<float>(x);
         }
         r.has = 1;
     } else {
         r.has = 2;
+        atomicAdd(need_second_pass, 1u);
     }
 }
 
@@ -431,16 +481,15 @@ __device__ void fold_partials(const LsmPartial* __restrict__ part, uint32_t begi
     block_sum<N>(v, smem);
 }
 
-// Publishes this CTA's chunk partial (written by thread 0 before the call)
-// and tells whether this CTA is the contract's last to do so: the partial is
-// fenced before the counter is bumped, the last CTA fences again before it
-// reads the others', and resets the counter for the next launch.  No CTA
-// waits on another.
-__device__ __forceinline__ bool last_chunk_of_contract(uint32_t* counter, uint32_t n_chunks, int* s_flag) {
+// One arrival at a completion counter; true in the CTA that arrives last.
+// The arriving CTA's writes (thread 0's) are fenced before the counter is
+// bumped, the last arrival fences again before it reads the others', and
+// resets the counter for the next launch.  No CTA waits on another.
+__device__ __forceinline__ bool last_arrival(uint32_t* counter, uint32_t expected, int* s_flag) {
     if (threadIdx.x == 0) {
         __threadfence();
         const uint32_t prev = atomicAdd(counter, 1u);
-        const bool last = prev == n_chunks - 1;
+        const bool last = prev == expected - 1;
         if (last) *counter = 0u;
         *s_flag = last ? 1 : 0;
     }
@@ -448,6 +497,34 @@ __device__ __forceinline__ bool last_chunk_of_contract(uint32_t* counter, uint32
     const bool last = *s_flag != 0;
     if (last) __threadfence();
     return last;
+}
+
+// Publishes this CTA's chunk partial (thread 0 wrote part[chunk]) and climbs
+// the two-level tree of the contract's sums: the last chunk of a group of
+// LsmDev::group_chunks chunks folds the group's partials in chunk order into
+// the group partial, the last group of the contract folds the group partials
+// in group order.  Every fold is short (a few dozen to a few hundred rows over
+// the whole CTA), so the contract's totals are ready soon after its last
+// chunk.  Returns true in the CTA holding the totals (valid in thread 0).
+// counters: the group counter of group g at group_counters[2 g], the
+// contract's at *contract_counter.
+__device__ bool publish_and_fold(uint32_t chunk, const LsmDev& c, const LsmPartial* __restrict__ part,
+                                 LsmPartial* __restrict__ gpart, uint32_t* group_counters,
+                                 uint32_t* contract_counter, double (&tot)[15], double (*smem)[15],
+                                 int* s_flag) {
+    const uint32_t local = chunk - c.chunk_begin;
+    const uint32_t g = local / c.group_chunks;
+    const uint32_t first = g * c.group_chunks;
+    const uint32_t count = min(c.group_chunks, c.n_chunks - first);
+    if (!last_arrival(&group_counters[2 * (c.group_begin + g)], count, s_flag)) return false;
+    fold_partials<15>(part, c.chunk_begin + first, count, tot, smem);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < 15; ++q) gpart[c.group_begin + g].v[q] = tot[q];
+    }
+    if (!last_arrival(contract_counter, c.n_groups, s_flag)) return false;
+    fold_partials<15>(gpart, c.group_begin, c.n_groups, tot, smem);
+    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -463,8 +540,9 @@ template <int PREC, bool COMP>
 __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 8)
     lsm_step(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
              uint32_t total_chunks, const void* __restrict__ store, double* __restrict__ cf,
-             LsmReg* __restrict__ reg, LsmPartial* __restrict__ part, Welford* __restrict__ final_part,
-             uint32_t* __restrict__ counters, double kappa_max) {
+             LsmReg* __restrict__ reg, LsmPartial* __restrict__ part, LsmPartial* __restrict__ gpart,
+             Welford* __restrict__ final_part, uint32_t* __restrict__ counters,
+             uint32_t* __restrict__ group_counters, uint32_t* __restrict__ need_second_pass, double kappa_max) {
     __shared__ double smem[kLsmThreads / 32][15];
     __shared__ float2 scratch[COMP ? 15 : 1][kLsmThreads];  // compensated sums' per-thread pairs
     __shared__ float pscratch[COMP ? 1 : 15][kLsmThreads];  // plain sums' per-thread values
@@ -694,9 +772,8 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 8)
 #pragma unroll
         for (int q = 0; q < 15; ++q) part[chunk].v[q] = out[q];
     }
-    if (!last_chunk_of_contract(&counters[2 * ci], c.n_chunks, &s_last)) return;
     double tot[15];
-    fold_partials<15>(part, c.chunk_begin, c.n_chunks, tot, smem);
+    if (!publish_and_fold(chunk, c, part, gpart, group_counters, &counters[2 * ci], tot, smem, &s_last)) return;
     if (threadIdx.x == 0) {
         double L[4][4];
         if (init) {
@@ -705,7 +782,7 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 8)
         } else {
             unpack_upper(re->T, L);
         }
-        solve_lagged(tot, L, kappa_max, reg[c.reg_offset + e - 1]);
+        solve_lagged(tot, L, kappa_max, reg[c.reg_offset + e - 1], need_second_pass + k);
     }
 }
 
@@ -717,11 +794,14 @@ template <int PREC>
 __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
     lsm_refine(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
                uint32_t total_chunks, const void* __restrict__ store, const double* __restrict__ cf,
-               LsmReg* __restrict__ reg, LsmPartial* __restrict__ part, uint32_t* __restrict__ counters) {
+               LsmReg* __restrict__ reg, LsmPartial* __restrict__ part, LsmPartial* __restrict__ gpart,
+               uint32_t* __restrict__ counters, uint32_t* __restrict__ group_counters,
+               const uint32_t* __restrict__ need_second_pass) {
     __shared__ double smem[kLsmThreads / 32][15];
     __shared__ float2 scratch[15][kLsmThreads];  // FP32 path: the sums' per-thread pairs
     __shared__ double sres[15];
     __shared__ int s_last;
+    if (__ldcg(need_second_pass + k) == 0) return;  // no date of this iteration needs it
     for (uint32_t chunk = blockIdx.x; chunk < total_chunks; chunk += gridDim.x) {
     const uint32_t ci = chunk_contract[chunk];
     const LsmDev c = cs[ci];
@@ -821,9 +901,8 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
 #pragma unroll
         for (int q = 0; q < 15; ++q) part[chunk].v[q] = out[q];
     }
-    if (last_chunk_of_contract(&counters[2 * ci + 1], c.n_chunks, &s_last)) {
-        double tot[15];
-        fold_partials<15>(part, c.chunk_begin, c.n_chunks, tot, smem);
+    double tot[15];
+    if (publish_and_fold(chunk, c, part, gpart, group_counters + 1, &counters[2 * ci + 1], tot, smem, &s_last)) {
         if (threadIdx.x == 0) {
             double T[4][4], gamma[4];
             unpack_upper(r.T, T);
@@ -877,38 +956,48 @@ cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
 }
 
 cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_contracts,
-                                 const uint32_t* chunk_contract, uint32_t total_chunks, const void* s_store,
-                                 double* cf, LsmReg* reg, LsmPartial* part_a, LsmPartial* part_b,
-                                 Welford* final_part, uint32_t* counters, cudaStream_t stream) {
-    (void)n_contracts;
+                                 const uint32_t* chunk_contract, uint32_t total_chunks, uint32_t total_groups,
+                                 const void* s_store, double* cf, LsmReg* reg, LsmPartial* part,
+                                 LsmPartial* gpart, Welford* final_part, uint32_t* counters, cudaStream_t stream) {
     cudaGetLastError();
     if (total_chunks == 0) return cudaSuccess;
+    // counters: 2 per contract (first pass, second pass), 2 per group, then
+    // one word per iteration counting the dates marked for the second pass.
+    uint32_t* group_counters = counters + 2 * static_cast<size_t>(n_contracts);
+    uint32_t* need = group_counters + 2 * static_cast<size_t>(total_groups);
+    // The second pass always runs after the first iteration (its lag is the
+    // identity), on a CTA per chunk; later it is rare and runs on a small
+    // persistent grid whose CTAs walk the chunks and skip those of contracts
+    // whose date needs no second pass (all of them return at once when no
+    // date does).
+    const unsigned refine_grid = (k == 0 || total_chunks < kRefineGrid) ? total_chunks : kRefineGrid;
     // Condition bound below which a date is solved from its lagged sums: FP64
     // sums are good to ~1e-15, so 1e2 keeps the solve near FP64 accuracy; the
     // FP32 path's plain chunk sums are good to ~1e-8 relative once summed
     // over the chunks, and 1e3 keeps its coefficients inside the rounding the
     // FP32 basis values carry anyway.
-    // The second pass runs on a small persistent grid: its CTAs walk the
-    // chunks and skip those of contracts whose date needs no second pass.
-    const unsigned refine_grid = total_chunks < kRefineGrid ? total_chunks : kRefineGrid;
     if (precision == 0) {
         if (k == 0)
-            lsm_step<0, true><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store,
-                                                                        cf, reg, part_a, final_part, counters, 1e2);
+            lsm_step<0, true><<<total_chunks, kLsmThreads, 0, stream>>>(
+                k, c, chunk_contract, total_chunks, s_store, cf, reg, part, gpart, final_part, counters,
+                group_counters, need, 1e2);
         else
-            lsm_step<0, false><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store,
-                                                                         cf, reg, part_a, final_part, counters, 1e2);
+            lsm_step<0, false><<<total_chunks, kLsmThreads, 0, stream>>>(
+                k, c, chunk_contract, total_chunks, s_store, cf, reg, part, gpart, final_part, counters,
+                group_counters, need, 1e2);
         lsm_refine<0><<<refine_grid, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
-                                                               reg, part_b, counters);
+                                                               reg, part, gpart, counters, group_counters, need);
     } else {
         if (k == 0)
-            lsm_step<1, true><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store,
-                                                                        cf, reg, part_a, final_part, counters, 1e3);
+            lsm_step<1, true><<<total_chunks, kLsmThreads, 0, stream>>>(
+                k, c, chunk_contract, total_chunks, s_store, cf, reg, part, gpart, final_part, counters,
+                group_counters, need, 1e3);
         else
-            lsm_step<1, false><<<total_chunks, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store,
-                                                                         cf, reg, part_a, final_part, counters, 1e3);
+            lsm_step<1, false><<<total_chunks, kLsmThreads, 0, stream>>>(
+                k, c, chunk_contract, total_chunks, s_store, cf, reg, part, gpart, final_part, counters,
+                group_counters, need, 1e3);
         lsm_refine<1><<<refine_grid, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
-                                                               reg, part_b, counters);
+                                                               reg, part, gpart, counters, group_counters, need);
     }
     return cudaGetLastError();
 }

@@ -21,7 +21,7 @@ namespace {
 enum { kDev = 4, kChunkMap = 5, kStore = 6, kCf = 7, kReg = 8, kPartA = 9, kPartB = 10,
        kFinal = 11, kOut = 12, kNets = 13, kSnaps = 14, kSnapOk = 15, kAdamT = 16, kErr = 17,
        kGroupMap = 18, kGramPart = 19, kFeats = 20, kMomPart = 35, kFzDev = 36, kFzPart = 37,
-       kFzOut = 38, kETab = 39, kCounters = 40 };
+       kFzOut = 38, kETab = 39, kCounters = 40 };  // kPartB: group partials
 
 struct LsmPlan {
     std::vector<LsmDev> dev;
@@ -118,10 +118,11 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
     if (!rc) rc = ctx.reserve(ctx.ext[kCf], sizeof(double) * std::max<uint64_t>(p.cf_elems, 1), "lsm cash flows");
     if (!rc) rc = ctx.reserve(ctx.ext[kReg], sizeof(LsmReg) * p.reg_rows, "lsm regression table");
     if (!rc) rc = ctx.reserve(ctx.ext[kPartA], sizeof(LsmPartial) * std::max<size_t>(p.total_chunks, 1), "lsm partials");
-    if (!rc) rc = ctx.reserve(ctx.ext[kPartB], sizeof(LsmPartial) * std::max<size_t>(p.total_chunks, 1), "lsm partials");
+    if (!rc) rc = ctx.reserve(ctx.ext[kPartB], sizeof(LsmPartial) * std::max<size_t>(p.total_groups, 1), "lsm group partials");
     if (!rc) rc = ctx.reserve(ctx.ext[kFinal], sizeof(Welford) * std::max<size_t>(p.total_chunks, 1), "lsm final partials");
     if (!rc) rc = ctx.reserve(ctx.ext[kOut], sizeof(double) * 6 * n, "lsm results");
-    if (!rc) rc = ctx.reserve(ctx.ext[kCounters], sizeof(uint32_t) * 2 * n, "lsm chunk counters");
+    const size_t n_counters = 2 * n + 2 * static_cast<size_t>(p.total_groups) + static_cast<size_t>(p.max_steps) + 1;
+    if (!rc) rc = ctx.reserve(ctx.ext[kCounters], sizeof(uint32_t) * n_counters, "lsm chunk counters");
     if (!rc && mlp) {
         rc = ctx.reserve(ctx.ext[kNets], sizeof(float) * 3 * mlp::kParamStride * n, "mlp networks");
         if (!rc) rc = ctx.reserve(ctx.ext[kSnaps], sizeof(float) * mlp::kParamStride * p.reg_rows, "mlp snapshots");
@@ -146,7 +147,7 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
         e = cudaMemcpyAsync(ctx.ext[kChunkMap].ptr, p.chunk_contract.data(), sizeof(uint32_t) * p.total_chunks,
                             cudaMemcpyHostToDevice, ctx.stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx.ext[kReg].ptr, 0, sizeof(LsmReg) * p.reg_rows, ctx.stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctx.ext[kCounters].ptr, 0, sizeof(uint32_t) * 2 * n, ctx.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx.ext[kCounters].ptr, 0, sizeof(uint32_t) * n_counters, ctx.stream);
     if (e == cudaSuccess && mlp) {
         e = cudaMemsetAsync(ctx.ext[kErr].ptr, 0, 256, ctx.stream);
         if (e == cudaSuccess && p.total_groups)
@@ -193,7 +194,7 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
                                           static_cast<uint32_t*>(ctx.ext[kErr].ptr), ctx.stream);
         else
             le = launch_lsm_iteration(precision, k, d_dev, static_cast<int>(n), d_map, p.total_chunks,
-                                      ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
+                                      p.total_groups, ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
                                       static_cast<LsmReg*>(ctx.ext[kReg].ptr),
                                       static_cast<LsmPartial*>(ctx.ext[kPartA].ptr),
                                       static_cast<LsmPartial*>(ctx.ext[kPartB].ptr),

@@ -222,6 +222,7 @@ def lib():
     sig("mcd_draws", vp, u64, u64, u64, u32, u32, i32, i32, P(dbl))
     sig("mcd_kernel_timing", vp, i32, P(dbl), P(u64))
     sig("mcd_crr_binomial_american", *D6, i32, i32, res=dbl)
+    sig("mcd_crr_binomial_bermudan", *D6, i32, i32, i32, res=dbl)
     sig("mcd_crr_binomial", *D6, i32, i32, P(dbl))
     sig("mcd_black_scholes_merton", *D6, i32, res=dbl)
     sig("mcd_black76", *([dbl] * 5), i32, res=dbl)
@@ -708,6 +709,13 @@ def crr_binomial(spot, strike, rate, carry_yield, vol, time, steps, type) -> Bin
     if rc != 0:
         raise McdError(rc, "crr_binomial: steps must be >= 1")
     return BinomialResult(*out)
+
+
+def crr_binomial_bermudan(spot, strike, rate, carry_yield, vol, time, exercise_dates, steps_per_date,
+                          type) -> float:
+    """Bermudan CRR price, exercise at the LSM dates (mcd_crr_binomial_bermudan)."""
+    return lib().mcd_crr_binomial_bermudan(spot, strike, rate, carry_yield, vol, time, int(exercise_dates),
+                                           int(steps_per_date), int(type))
 
 
 def crr_binomial_american(spot, strike, rate, carry_yield, vol, time, steps, type) -> float:

@@ -498,6 +498,13 @@ int mcd_draws(mcd_ctx* ctx, uint64_t seed, uint64_t path_begin, uint64_t n_paths
  * NaN when steps < 1. */
 double mcd_crr_binomial_american(double spot, double strike, double rate, double carry_yield, double vol,
                                  double time, int steps, int type);
+/* No counterpart in the reference.  The Bermudan CRR price with exercise only
+ * at t = j T / exercise_dates, j = 0 .. exercise_dates - 1 (the dates at which
+ * Longstaff-Schwartz with that many monitoring points decides), steps_per_date
+ * tree steps between dates: the exact value that LSM's in-sample estimate
+ * approximates.  NaN for non-positive counts or more than 2^20 steps. */
+double mcd_crr_binomial_bermudan(double spot, double strike, double rate, double carry_yield, double vol,
+                                 double time, int exercise_dates, int steps_per_date, int type);
 /* replaces mcd::pricers::crr_binomial (src/pricers/binomial.cpp:9-37): European
  * CRR tree; writes {price, risk-neutral probability, up factor, down factor}. */
 int mcd_crr_binomial(double spot, double strike, double rate, double carry_yield, double vol, double time,

@@ -102,3 +102,19 @@ def test_put_call_parity_of_closed_forms(gpu_lib):
         ki = gpu_lib.reiner_rubinstein(s, k, h, r, q, v, t, gpu_lib.CALL, d, gpu_lib.IN)
         ko = gpu_lib.reiner_rubinstein(s, k, h, r, q, v, t, gpu_lib.CALL, d, gpu_lib.OUT)
         assert abs(ki + ko - c) < 1e-10
+
+
+def test_bermudan_lattice_brackets():
+    """mcd_crr_binomial_bermudan (no reference counterpart): with an exercise
+    date on every tree step it is the reference's American CRR price; with one
+    date (t = 0 only) it is max(intrinsic, European); otherwise in between."""
+    import mcd_gpu as M
+    args = (36.0, 40.0, 0.06, 0.0, 0.2, 1.0)
+    amer = M.crr_binomial_american(*args, 2000, 1)
+    assert abs(M.crr_binomial_bermudan(*args, 2000, 1, 1) - amer) <= 1e-12 * amer
+    euro = M.crr_binomial(*args, 2000, 1).price
+    assert abs(M.crr_binomial_bermudan(*args, 1, 2000, 1) - max(4.0, euro)) <= 1e-12
+    berm = M.crr_binomial_bermudan(*args, 50, 40, 1)
+    assert euro < berm < amer
+    import math
+    assert math.isnan(M.crr_binomial_bermudan(*args, 0, 10, 1))

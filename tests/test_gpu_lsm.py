@@ -11,8 +11,9 @@ Bars:
     coincides.  The full-size grid is tests/test_gpu_lsm_grid.py.
   * Frozen-policy repricing with the reference's own policy: within 1e-12.
   * FP32 paths: within 0.5 SE of the FP64 price on the same draws.
-  * Within 3 SE of the CRR American tree (tests/lsm_test.cpp:78-98 grid) and
-    American call without dividends == Black-Scholes (lsm_test.cpp:26-38).
+  * Within 3 SE of the 4000-step CRR American tree (tests/lsm_test.cpp:78-98:
+    its grid, path count and seed), FP64 and FP32, and American call without
+    dividends == Black-Scholes (lsm_test.cpp:26-38).
 """
 from __future__ import annotations
 
@@ -74,16 +75,21 @@ def test_fp32_tracks_fp64(engine):
 
 
 def test_against_binomial_tree(engine, orc):
+    """tests/lsm_test.cpp:78-98 as the reference runs it: 50 dates, 100,000
+    paths, seed 909, a 4000-step CRR tree, strictly within 3 SE -- on the FP64
+    path (the reference's arithmetic) and on the FP32 batch."""
     grid = [(100, 100, .05, 0, .25, 1.0, 1), (100, 80, .05, 0, .25, 1.0, 1),
             (100, 120, .05, 0, .25, 1.0, 1), (100, 100, .05, .03, .30, .5, 1),
             (100, 100, .05, .03, .30, .5, 0), (100, 100, .03, .06, .20, 2.0, 1)]
     c = np.zeros(len(grid), dtype=__import__("mcd_gpu").LSM_CONTRACT_DTYPE)
     for i, (s, k, r, q, v, t, ty) in enumerate(grid):
         c[i] = (s, k, r, q, v, t, ty, 50, 100000, 909)
-    out = engine.lsm_batch(c, "fp32")
+    out32 = engine.lsm_batch(c, "fp32")
     for i, (s, k, r, q, v, t, ty) in enumerate(grid):
-        tree = orc.orc_crr_binomial_american(s, k, r, q, v, t, 2000, ty)
-        assert abs(out["price"][i] - tree) < 3 * out["standard_error"][i] + 2e-3, (grid[i], out[i], tree)
+        tree = orc.orc_crr_binomial_american(s, k, r, q, v, t, 4000, ty)
+        r64 = engine.monte_carlo_lsm_american(s, k, r, q, v, t, ty, 50, 100000, 909, precision="fp64")
+        assert abs(r64.price - tree) < 3 * r64.standard_error, (grid[i], r64, tree)
+        assert abs(out32["price"][i] - tree) < 3 * out32["standard_error"][i], (grid[i], out32[i], tree)
     call = engine.monte_carlo_lsm_american(100, 100, .05, 0, .25, 1, 0, 50, 100000, 909, precision="fp32")
     assert abs(call.price - orc.orc_bsm(100, 100, .05, 0, .25, 1, 0)) < 3 * call.standard_error
 
