@@ -151,8 +151,7 @@ extern "C" int mcd_price_batch_static(const mcd_contract* contracts, size_t n, i
     if (e != cudaSuccess) return report_cuda(error_message, error_capacity, e, "stage contracts");
     if (total > 0) {
         e = mcdg::launch_path_kernel(precision, 1, g_grid[device][precision], d_contracts, static_cast<int>(n),
-                                     d_prefix, static_cast<uint32_t>(total), d_flags, d_partials,
-                                     d_flags + 1, s);
+                                     d_prefix, d_flags, d_partials, d_flags + 1, s);
         if (e != cudaSuccess) return report_cuda(error_message, error_capacity, e, "path kernel");
     }
     e = mcdg::launch_merge_kernel(d_contracts, static_cast<int>(n), d_prefix, d_partials, d_results, s);

@@ -42,7 +42,9 @@ int Ctx::reserve(DeviceBuffer& b, size_t bytes, const char* what) {
     if (b.ptr) cudaFree(b.ptr);
     b.ptr = nullptr;
     b.bytes = 0;
-    size_t want = std::max<size_t>(bytes, 256);
+    // At least 1 MiB: small and medium calls then never reallocate (a
+    // cudaFree/cudaMalloc pair waits for the whole device).
+    size_t want = std::max<size_t>(bytes, size_t(1) << 20);
     want = want + want / 4;  // grow with headroom
     cudaError_t e = cudaMalloc(&b.ptr, want);
     if (e != cudaSuccess) {
@@ -58,7 +60,7 @@ int Ctx::reserve_host(HostBuffer& b, size_t bytes, const char* what) {
     if (b.ptr) cudaFreeHost(b.ptr);
     b.ptr = nullptr;
     b.bytes = 0;
-    size_t want = std::max<size_t>(bytes, 256);
+    size_t want = std::max<size_t>(bytes, size_t(64) << 10);
     want = want + want / 4;
     cudaError_t e = cudaMallocHost(&b.ptr, want);
     if (e != cudaSuccess) {
@@ -277,7 +279,7 @@ int get_graph(Ctx& ctx, int precision, const BatchPlan& plan, void* results, cud
     int variant = 0, grid = 0;
     int rc = launch_shape(ctx, precision, variant, grid);
     if (rc) return rc;
-    GraphKey key{precision, variant, grid, plan.n, plan.total_items, ctx.d_contracts.ptr,
+    GraphKey key{precision, variant, grid, plan.n, 0u, ctx.d_contracts.ptr,
                  ctx.d_prefix.ptr, ctx.d_partials.ptr, results};
     for (auto& g : ctx.graphs) {
         if (g.key == key && g.exec) {
@@ -295,8 +297,7 @@ int get_graph(Ctx& ctx, int precision, const BatchPlan& plan, void* results, cud
     cudaError_t e2 = launch_path_kernel(precision, variant, grid,
                                         static_cast<const DevContract*>(ctx.d_contracts.ptr),
                                         static_cast<int>(plan.n),
-                                        static_cast<const uint32_t*>(ctx.d_prefix.ptr),
-                                        plan.total_items, ticket,
+                                        static_cast<const uint32_t*>(ctx.d_prefix.ptr), ticket,
                                         static_cast<Welford*>(ctx.d_partials.ptr), err, ctx.stream);
     cudaError_t e3 = launch_merge_kernel(static_cast<const DevContract*>(ctx.d_contracts.ptr),
                                          static_cast<int>(plan.n),

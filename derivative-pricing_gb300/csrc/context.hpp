@@ -34,15 +34,18 @@ struct LaunchShape {
     int ctas_per_sm = 0;  // 0: occupancy limit
 };
 
+// Key of a captured graph.  items: the work items the captured launch was
+// given; 0 for the path engine, whose kernel reads its item count from the
+// uploaded prefix (one graph serves every path count; the partials buffer's
+// address changes whenever it has to grow).
 struct GraphKey {
     int precision, variant, grid;
     size_t n;
-    uint32_t total_items;
+    uint32_t items;
     const void *contracts, *prefix, *partials, *results;
     bool operator==(const GraphKey& o) const {
-        return precision == o.precision && variant == o.variant && grid == o.grid && n == o.n &&
-               total_items == o.total_items && contracts == o.contracts && prefix == o.prefix &&
-               partials == o.partials && results == o.results;
+        return precision == o.precision && variant == o.variant && grid == o.grid && n == o.n && items == o.items &&
+               contracts == o.contracts && prefix == o.prefix && partials == o.partials && results == o.results;
     }
 };
 

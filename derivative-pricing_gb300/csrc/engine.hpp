@@ -65,10 +65,12 @@ struct DevContract {
 const char* convert_contract(const mcd_contract& in, uint32_t index, DevContract& out);
 
 // Launches (all asynchronous on `stream`).
+// The persistent path kernel over items [0, item_prefix[n_contracts]) (the
+// item count is read on the device, so one captured launch serves every path
+// count of the same number of contracts).
 cudaError_t launch_path_kernel(int precision, int variant, int grid, const DevContract* contracts,
-                               int n_contracts, const uint32_t* item_prefix, uint32_t total_items,
-                               uint32_t* ticket, Welford* partials, uint32_t* error_flag,
-                               cudaStream_t stream);
+                               int n_contracts, const uint32_t* item_prefix, uint32_t* ticket,
+                               Welford* partials, uint32_t* error_flag, cudaStream_t stream);
 cudaError_t launch_merge_kernel(const DevContract* contracts, int n_contracts,
                                 const uint32_t* item_prefix, const Welford* partials,
                                 void* results /* mcd_mc_result[] */, cudaStream_t stream);

@@ -360,19 +360,21 @@ __device__ Welford run_slab(const DevContract& c, uint64_t base) {
 template <int PREC, int MINB>
 __global__ void __launch_bounds__(kSlabThreads, MINB)
     path_kernel(const DevContract* __restrict__ contracts, int n_contracts,
-                const uint32_t* __restrict__ item_prefix, uint32_t total_items,
-                uint32_t* __restrict__ ticket, Welford* __restrict__ partials,
-                uint32_t* __restrict__ error_flag) {
-    __shared__ uint32_t s_item;
+                const uint32_t* __restrict__ item_prefix, uint32_t* __restrict__ ticket,
+                Welford* __restrict__ partials, uint32_t* __restrict__ error_flag) {
+    __shared__ uint32_t s_item, s_total;
     __shared__ Welford s_warp[kSlabThreads / 32];
     __shared__ DevContract s_contract;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    // The batch's item count is the prefix's last entry (read from memory, so
+    // a captured launch serves every path count of the same contract count).
+    if (threadIdx.x == 0) s_total = item_prefix[n_contracts];
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(ticket, 1u);
         __syncthreads();
         const uint32_t item = s_item;
-        if (item >= total_items) return;
+        if (item >= s_total) return;
         // Largest contract index c with item_prefix[c] <= item (empty
         // contracts share their successor's prefix and are skipped).
         int lo = 0, hi = n_contracts;
@@ -463,24 +465,22 @@ __global__ void draws_kernel(uint64_t seed, uint64_t path_begin, uint64_t n_path
 }
 
 template <int PREC, int MINB>
-cudaError_t launch_one(int grid, const DevContract* c, int n, const uint32_t* prefix, uint32_t total,
-                       uint32_t* ticket, Welford* partials, uint32_t* err, cudaStream_t stream) {
+cudaError_t launch_one(int grid, const DevContract* c, int n, const uint32_t* prefix, uint32_t* ticket,
+                       Welford* partials, uint32_t* err, cudaStream_t stream) {
     cudaGetLastError();  // report this launch only
-    path_kernel<PREC, MINB><<<grid, kSlabThreads, 0, stream>>>(c, n, prefix, total, ticket,
-                                                               partials, err);
+    path_kernel<PREC, MINB><<<grid, kSlabThreads, 0, stream>>>(c, n, prefix, ticket, partials, err);
     return cudaGetLastError();
 }
 
 template <int PREC>
 cudaError_t launch_prec(int variant, int grid, const DevContract* c, int n, const uint32_t* prefix,
-                        uint32_t total, uint32_t* ticket, Welford* partials, uint32_t* err,
-                        cudaStream_t stream) {
+                        uint32_t* ticket, Welford* partials, uint32_t* err, cudaStream_t stream) {
     switch (variant) {
-        case 0: return launch_one<PREC, 4>(grid, c, n, prefix, total, ticket, partials, err, stream);
-        case 1: return launch_one<PREC, 8>(grid, c, n, prefix, total, ticket, partials, err, stream);
-        case 2: return launch_one<PREC, 12>(grid, c, n, prefix, total, ticket, partials, err, stream);
-        case 3: return launch_one<PREC, 16>(grid, c, n, prefix, total, ticket, partials, err, stream);
-        default: return launch_one<PREC, 6>(grid, c, n, prefix, total, ticket, partials, err, stream);
+        case 0: return launch_one<PREC, 4>(grid, c, n, prefix, ticket, partials, err, stream);
+        case 1: return launch_one<PREC, 8>(grid, c, n, prefix, ticket, partials, err, stream);
+        case 2: return launch_one<PREC, 12>(grid, c, n, prefix, ticket, partials, err, stream);
+        case 3: return launch_one<PREC, 16>(grid, c, n, prefix, ticket, partials, err, stream);
+        default: return launch_one<PREC, 6>(grid, c, n, prefix, ticket, partials, err, stream);
     }
 }
 
@@ -529,14 +529,13 @@ cudaError_t launch_words_digest(const uint64_t* words, size_t n_words, uint64_t*
 }
 
 cudaError_t launch_path_kernel(int precision, int variant, int grid, const DevContract* contracts,
-                               int n_contracts, const uint32_t* item_prefix, uint32_t total_items,
-                               uint32_t* ticket, Welford* partials, uint32_t* error_flag,
-                               cudaStream_t stream) {
+                               int n_contracts, const uint32_t* item_prefix, uint32_t* ticket,
+                               Welford* partials, uint32_t* error_flag, cudaStream_t stream) {
     if (precision == 0)
-        return launch_prec<0>(variant, grid, contracts, n_contracts, item_prefix, total_items,
-                              ticket, partials, error_flag, stream);
-    return launch_prec<1>(variant, grid, contracts, n_contracts, item_prefix, total_items, ticket,
-                          partials, error_flag, stream);
+        return launch_prec<0>(variant, grid, contracts, n_contracts, item_prefix, ticket, partials,
+                              error_flag, stream);
+    return launch_prec<1>(variant, grid, contracts, n_contracts, item_prefix, ticket, partials,
+                          error_flag, stream);
 }
 
 cudaError_t path_kernel_occupancy(int precision, int variant, int* blocks_per_sm) {

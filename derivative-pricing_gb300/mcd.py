@@ -8,9 +8,10 @@ What differs, because a GPU sits underneath:
 * every Monte Carlo call runs on the GPU (FP64 arithmetic by default, the
   reference's; ``set_precision("fp32")`` switches the calling thread to FP32
   paths with FP64 accumulation);
-* calls take an engine context (device ``MCD_GPU_DEVICE``, default 0) from a pool,
-  so calls from several threads run concurrently; ctypes releases the GIL
-  around every foreign call, as the reference's ``gil_scoped_release`` does;
+* calls take an engine context (device ``MCD_GPU_DEVICE``, default 0) from a pool
+  of warmed contexts (``MCD_GPU_POOL``, default 2, more on demand), so calls from
+  several threads run concurrently; ctypes releases the GIL around every foreign
+  call, as the reference's ``gil_scoped_release`` does;
 * ``McOptions.num_threads`` is accepted and ignored (the path loop is on the GPU);
 * ``HAS_NEON`` is False: the reference's NEON batch path does not exist here,
   and ``benchmark_european`` reports ``simd_enabled`` accordingly;
@@ -142,19 +143,36 @@ HestonMcResult = McResult
 # A context serves one call at a time; a call takes an idle context from the pool
 # (creating one when every context is busy) and returns it afterwards, so calls
 # from several threads run concurrently, and threads that come and go reuse the
-# contexts (and the graphs captured in them) of earlier ones.
+# contexts (and the graphs captured in them) of earlier ones.  The first call
+# creates MCD_GPU_POOL contexts (default 2) at once, and every context is warmed
+# when created (one small call per precision: its buffers are sized and its
+# graphs captured), so a thread that arrives while the others are pricing does
+# not pay that set-up -- whose allocations would wait for the whole device --
+# inside its call.
 
 _pool: list = []
 _pool_lock = threading.Lock()
+_pool_started = False
 _tls = threading.local()
+
+
+def _new_engine() -> _g.Engine:
+    eng = _g.Engine(int(os.environ.get("MCD_GPU_DEVICE", "0")))
+    for prec in ("fp64", "fp32"):
+        eng.monte_carlo_european(100.0, 100.0, 0.05, 0.0, 0.2, 1.0, 0, 4096, 1, precision=prec)
+    return eng
 
 
 class _Lease:
     def __enter__(self) -> _g.Engine:
+        global _pool_started
         with _pool_lock:
+            if not _pool_started:
+                _pool_started = True
+                _pool.extend(_new_engine() for _ in range(max(1, int(os.environ.get("MCD_GPU_POOL", "2")))))
             self.eng = _pool.pop() if _pool else None
         if self.eng is None:
-            self.eng = _g.Engine(int(os.environ.get("MCD_GPU_DEVICE", "0")))
+            self.eng = _new_engine()
         return self.eng
 
     def __exit__(self, *exc):

@@ -89,3 +89,65 @@ def test_fp32_qr_grid_tracks_reference(engine, grid):
     err = np.abs(out["price"] - [p["price"] for p in puts]) / [p["se"] for p in puts]
     print("FP32 QR grid, error in reference standard errors: max", err.max(), "mean", err.mean())
     assert err.max() <= 0.1
+
+
+def test_learned_grid_against_the_exact_bermudan_value(engine, grid, gpu_lib):
+    """The learned regression (BF16 tensor-core network, FP32 paths) on the
+    full grid, judged against the exact value of the 50-date Bermudan put (CRR
+    lattice with exercise at the LSM dates) and against the FP64 QR price.
+
+    * Every learned price within 3 SE of the exact value (as every Monte Carlo
+      price here must be of its analytic or lattice oracle), and on average
+      no farther from it than the QR regression's.
+    * The learned price sits above the FP64 QR price by up to ~1.2 SE.  That
+      gap is the better exercise policy, not an error: replayed on fresh paths
+      (no foresight), the learned policy earns more than the QR policy on
+      every put."""
+    c, puts = grid
+    M = gpu_lib
+    ml = engine.lsm_batch(c, "fp32", "mlp")
+    qr = engine.lsm_batch(c, "fp64", "qr")
+    se = qr["standard_error"]
+    berm = np.array([M.crr_binomial_bermudan(r["spot"], r["strike"], r["rate"], r["carry_yield"], r["vol"], r["time"],
+                                             int(r["monitoring_points"]), 100, 1) for r in c])
+    z_ml, z_qr = (ml["price"] - berm) / se, (qr["price"] - berm) / se
+    gap = (ml["price"] - qr["price"]) / se
+    print(f"vs exact Bermudan: learned max|z| {np.abs(z_ml).max():.2f} mean|z| {np.abs(z_ml).mean():.2f}; "
+          f"QR max|z| {np.abs(z_qr).max():.2f} mean|z| {np.abs(z_qr).mean():.2f}; "
+          f"learned - QR: mean {gap.mean():+.2f} max {gap.max():+.2f} SE")
+    assert (ml["reserved"] == 0).all()  # no fallback to QR
+    assert np.abs(z_ml).max() < 3.0
+    assert np.abs(z_ml).mean() <= np.abs(z_qr).mean() + 0.1
+    gains = []
+    for i, r in enumerate(c):
+        w, has = engine.mlp_policy(i, int(r["monitoring_points"]))
+        args = (r["spot"], r["strike"], r["rate"], r["carry_yield"], r["vol"], r["time"], int(r["type"]),
+                int(r["monitoring_points"]))
+        _, co, hq = engine.monte_carlo_lsm_american(*args, int(r["path_count"]), int(r["seed"]),
+                                                    precision="fp64", policy=True)
+        fresh = int(r["seed"]) + 10_000_000
+        q_oos = engine.reprice_against_frozen_policy(*args, int(r["path_count"]), fresh, co, hq, False, "fp64")
+        m_oos = engine.reprice_mlp(*args, int(r["path_count"]), fresh, w, has, "fp32")
+        gains.append((m_oos.price - q_oos) / m_oos.standard_error)
+    gains = np.array(gains)
+    print(f"out of sample, learned - QR policy: min {gains.min():+.2f} mean {gains.mean():+.2f} SE")
+    assert (gains > 0).all()
+    assert (gap > -0.5).all() and gap.max() < 2.0
+
+
+def test_learned_per_date_fine_tuning_changes_little(engine, grid):
+    """The hidden layers are trained once, on the latest date; every date
+    refits the output layer exactly on all its in-the-money paths.  Fine-tuning
+    the hidden layers at every date as well (Adam steps warm-started from the
+    later date) moves no price by more than a fraction of its SE: the features
+    learned once already span each date's continuation value."""
+    c, _ = grid
+    base = engine.lsm_batch(c, "fp32", "mlp")
+    try:
+        engine.set_mlp_config(300, 5, 3e-3, 3e-4)
+        tuned = engine.lsm_batch(c, "fp32", "mlp")
+    finally:
+        engine.set_mlp_config()
+    d = np.abs(tuned["price"] - base["price"]) / base["standard_error"]
+    print(f"per-date fine-tuning (5 steps): max change {d.max():.3f} SE, mean {d.mean():.3f} SE")
+    assert d.max() < 0.5 and d.mean() < 0.2
