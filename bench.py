@@ -109,12 +109,12 @@ PATH_KERNEL_SOURCES = ("derivative-pricing_gb300/csrc/gbm_paths.cu",
                        "derivative-pricing_gb300/csrc/device_common.cuh",
                        "derivative-pricing_gb300/csrc/engine.hpp")
 PATH_KERNEL_PROFILE = {
-    "sources": "cf6ad0a85d243b5d",
+    "sources": "99217b851c742b16",
     "case_path_steps": 6807363601.0,
     # variant -> smsp__inst_executed.sum of one launch
-    "warp_inst": {"0": 15676824749, "1": 17989424263, "2": 20430087044, "3": 15839904527, "4": 16405233406},
+    "warp_inst": {"0": 15677221671, "1": 17947643629, "2": 20430146604, "3": 15840244686, "4": 16407956191},
     # variant -> dram__bytes_read.sum + dram__bytes_write.sum of one launch
-    "dram_bytes": {"0": 181760, "1": 353792, "2": 587776, "3": 9074432, "4": 153344},
+    "dram_bytes": {"0": 694528, "1": 369152, "2": 536832, "3": 8030976, "4": 459520},
 }
 
 
