@@ -53,6 +53,14 @@ __device__ __forceinline__ float expm1_small(float a) {
     return __expf(a) - 1.0f;
 }
 
+// expm1 by its cubic Taylor polynomial, for exponents the host bounds by
+// 1e-2 (DevGreeks::vol_series): the first omitted term is below a^3 / 24 <
+// 5e-8 of the result, under an FP32 rounding, in three instructions and
+// without the range test of expm1_small.
+__device__ __forceinline__ float expm1_series(float a) {
+    return __fmaf_rn(__fmaf_rn(a, 1.0f / 6.0f, 0.5f) * a, a, a);
+}
+
 // Likelihood-ratio scores of the first step (likelihood_ratio.cpp:45-49,
 // :140-142), with sqrt_t = sqrt(dt) of that step.
 __device__ __forceinline__ void lr_first_step(double h, double z1, double spot, double vol, double sqrt_t, double t,
@@ -215,7 +223,7 @@ __device__ void greeks64(const DevContract& c, const DevGreeks& g, const PhiloxK
 // ===========================================================================
 // FP32: one log-path, differential vol states, FP64 payoffs of the states
 // ===========================================================================
-template <int KIND>
+template <int KIND, bool SER>
 __device__ void greeks32(const DevContract& c, const DevGreeks& g, const PhiloxKeys& k, uint64_t path,
                          double (&o)[kNumGreeks]) {
 #pragma unroll
@@ -280,46 +288,52 @@ __device__ void greeks32(const DevContract& c, const DevGreeks& g, const PhiloxK
         const float sqdt = static_cast<float>(g.sqrt_dt);
         const float vdt = static_cast<float>(g.vol * g.dt);
         const float inv_vol = static_cast<float>(1.0 / g.vol);
-        float x = 0.0f, D = 0.0f, z1 = 0.0f, lr_vega = 0.0f, zsum = 0.0f;
+        // Per step: the log-spot x (as the path engine), the running sums of
+        // the draws and of their squares (the likelihood-ratio vega and rho
+        // scores follow from them), D = dx/dvol = sqrt(dt) sum z - vol i dt,
+        // and the vol-bump exponents +/- h D - h^2 i dt / 2.  A barrier or
+        // lookback state needs only the running extremes of x, x + e_up and
+        // x + e_dn: a barrier is touched on some date exactly when the extreme
+        // over the dates reaches it.
+        float x = 0.0f, D = 0.0f, z1 = 0.0f, zsum = 0.0f, zsq = 0.0f, fi = 0.0f;
         float acc = 0.0f, acc2 = 0.0f, xmax = 0.0f, xmin = 0.0f;  // as the path engine
         float a_d = 0.0f, a_r = 0.0f, a_up = 0.0f, a_dn = 0.0f, sd = 0.0f;
         float xmax_up = 0.0f, xmin_up = 0.0f, xmax_dn = 0.0f, xmin_dn = 0.0f;
         float e_up = 0.0f, e_dn = 0.0f;  // bump exponents of the last step
-        bool br = false, br_su = false, br_sd = false, br_vu = false, br_vd = false;
+        if constexpr (KIND == kBarrier) {  // extremes over the monitoring dates only
+            const float start = c.up ? -3.0e38f : 3.0e38f;
+            xmax = xmin = xmax_up = xmin_up = xmax_dn = xmin_dn = start;
+        }
         for (int step = 0; step < c.n_steps; ++step) {
             const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(step), k));
             if (step == 0) z1 = z;
             x = __fmaf_rn(sg, z, x + mu);
-            D = D + __fmaf_rn(sqdt, z, -vdt);
-            lr_vega = lr_vega + (__fmaf_rn(z, z, -1.0f) * inv_vol - sqdt * z);
             zsum += z;
-            const float fi = static_cast<float>(step + 1);
-            e_up = __fmaf_rn(hvf, D, -cq * fi);
-            e_dn = __fmaf_rn(-hvf, D, -cq * fi);
+            zsq = __fmaf_rn(z, z, zsq);
+            fi += 1.0f;
+            D = __fmaf_rn(sqdt, zsum, -vdt * fi);
+            const float q = cq * fi;
+            e_up = __fmaf_rn(hvf, D, -q);
+            e_dn = __fmaf_rn(-hvf, D, -q);
             if constexpr (KIND == kAsianArith) {
                 const float e = __expf(x);
                 acc += e;
                 a_d = __fmaf_rn(e, D, a_d);
                 a_r = __fmaf_rn(e, fi, a_r);
-                a_up = __fmaf_rn(e, expm1_small(e_up), a_up);
-                a_dn = __fmaf_rn(e, expm1_small(e_dn), a_dn);
+                a_up = __fmaf_rn(e, SER ? expm1_series(e_up) : expm1_small(e_up), a_up);
+                a_dn = __fmaf_rn(e, SER ? expm1_series(e_dn) : expm1_small(e_dn), a_dn);
             } else if constexpr (KIND == kAsianGeo) {
                 acc2 += x;
                 sd += D;
             } else if constexpr (KIND == kBarrier) {
-                const float xu = x + e_up, xd = x + e_dn;
                 if (c.up) {
-                    br = br || x >= lnh;
-                    br_su = br_su || x >= lnh_su;
-                    br_sd = br_sd || x >= lnh_sd;
-                    br_vu = br_vu || xu >= lnh;
-                    br_vd = br_vd || xd >= lnh;
+                    xmax = fmaxf(xmax, x);
+                    xmax_up = fmaxf(xmax_up, x + e_up);
+                    xmax_dn = fmaxf(xmax_dn, x + e_dn);
                 } else {
-                    br = br || x <= lnh;
-                    br_su = br_su || x <= lnh_su;
-                    br_sd = br_sd || x <= lnh_sd;
-                    br_vu = br_vu || xu <= lnh;
-                    br_vd = br_vd || xd <= lnh;
+                    xmin = fminf(xmin, x);
+                    xmin_up = fminf(xmin_up, x + e_up);
+                    xmin_dn = fminf(xmin_dn, x + e_dn);
                 }
             } else {
                 xmax = fmaxf(xmax, x);
@@ -328,6 +342,24 @@ __device__ void greeks32(const DevContract& c, const DevGreeks& g, const PhiloxK
                 xmin_up = fminf(xmin_up, x + e_up);
                 xmax_dn = fmaxf(xmax_dn, x + e_dn);
                 xmin_dn = fminf(xmin_dn, x + e_dn);
+            }
+        }
+        // sum over steps of (z^2 - 1) / vol - sqrt(dt) z
+        const float lr_vega = __fmaf_rn(zsq - fi, inv_vol, -sqdt * zsum);
+        bool br = false, br_su = false, br_sd = false, br_vu = false, br_vd = false;
+        if constexpr (KIND == kBarrier) {
+            if (c.up) {
+                br = xmax >= lnh;
+                br_su = xmax >= lnh_su;
+                br_sd = xmax >= lnh_sd;
+                br_vu = xmax_up >= lnh;
+                br_vd = xmax_dn >= lnh;
+            } else {
+                br = xmin <= lnh;
+                br_su = xmin <= lnh_su;
+                br_sd = xmin <= lnh_sd;
+                br_vu = xmin_up <= lnh;
+                br_vd = xmin_dn <= lnh;
             }
         }
         // price: the path engine's FP32 payoff
@@ -446,7 +478,7 @@ __device__ void greeks32(const DevContract& c, const DevGreeks& g, const PhiloxK
 // pairs live in shared memory (acc[0][i][t], acc[1][i][t]) rather than
 // registers: they are touched once per path, and the registers go to the
 // path state instead.
-template <int PREC, int KIND>
+template <int PREC, int KIND, bool SER = false>
 __device__ void slab_greeks(const DevContract& c, const DevGreeks& g, const PhiloxKeys& k, uint64_t base,
                             double (*acc)[kNumGreeks][kSlabThreads], Welford (&w)[kNumGreeks]) {
     const int t = threadIdx.x;
@@ -470,7 +502,7 @@ __device__ void slab_greeks(const DevContract& c, const DevGreeks& g, const Phil
                 acc[1][i][t] += delta * (o[i] - m);
             }
         } else {
-            greeks32<KIND>(c, g, k, path, o);
+            greeks32<KIND, SER>(c, g, k, path, o);
 #pragma unroll
             for (int i = 0; i < kNumGreeks; ++i) {
                 acc[0][i][t] += o[i];
@@ -494,7 +526,10 @@ __device__ void run_greeks_slab(const DevContract& c, const DevGreeks& g, uint64
     switch (c.kind) {
         case kEuropean: slab_greeks<PREC, kEuropean>(c, g, k, base, acc, w); break;
         case kDigital: slab_greeks<PREC, kDigital>(c, g, k, base, acc, w); break;
-        case kAsianArith: slab_greeks<PREC, kAsianArith>(c, g, k, base, acc, w); break;
+        case kAsianArith:
+            if (g.vol_series) slab_greeks<PREC, kAsianArith, true>(c, g, k, base, acc, w);
+            else slab_greeks<PREC, kAsianArith, false>(c, g, k, base, acc, w);
+            break;
         case kAsianGeo: slab_greeks<PREC, kAsianGeo>(c, g, k, base, acc, w); break;
         case kBarrier: slab_greeks<PREC, kBarrier>(c, g, k, base, acc, w); break;
         case kLookbackFixed: slab_greeks<PREC, kLookbackFixed>(c, g, k, base, acc, w); break;

@@ -41,6 +41,8 @@ struct DevGreeks {
     double lr_delta_scale;     // 1 / (S0 vol sqrt(dt1)), dt1 = first-step length
     double lr_gamma_scale;     // 1 / (S0^2 vol^2 dt1)
     double sqrt_dt_over_vol, inv_vol, inv_n, inv_spot, inv_2t, mu_over_vol_sqrt_t;
+    int32_t vol_series;        // |vol-bump exponent| <= 1e-2 on all but > 8-sigma paths: cubic expm1
+    int32_t pad;
 };
 
 cudaError_t launch_greeks_kernel(int precision, int variant, int grid, const DevContract* contracts,

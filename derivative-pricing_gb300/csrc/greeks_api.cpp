@@ -80,6 +80,9 @@ int plan_greeks(Ctx& ctx, const mcd_contract* cs, size_t n, double spot_rel, dou
         g.inv_spot = 1.0 / in.spot;
         g.inv_2t = 1.0 / (2.0 * in.time);
         g.mu_over_vol_sqrt_t = g.mu / (in.vol * g.sqrt_dt);
+        // The vol-bump exponent is h_vol D - h_vol^2 i dt / 2 with |D| below
+        // 8 sqrt(T) + vol T on all but > 8-sigma paths.
+        g.vol_series = g.h_vol * (8.0 * std::sqrt(in.time) + in.vol * in.time) <= 1e-2 ? 1 : 0;
     }
     return MCD_OK;
 }
