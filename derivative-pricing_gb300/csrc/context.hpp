@@ -107,7 +107,7 @@ struct Ctx {
     GraphKey greeks_key{};
 
     // Training schedule of the learned LSM regression (mcd_lsm_set_mlp_config).
-    int mlp_steps_first = 300;
+    int mlp_steps_first = 100;
     int mlp_steps = 0;
     float mlp_lr_first = 3e-3f;
     float mlp_lr = 1e-3f;

@@ -433,7 +433,7 @@ class Engine:
         return out
 
     # -- learned regression ----------------------------------------------------------------
-    def set_mlp_config(self, steps_first=300, steps=0, lr_first=3e-3, lr=1e-3):
+    def set_mlp_config(self, steps_first=100, steps=0, lr_first=3e-3, lr=1e-3):
         """Training schedule of the learned regression (see mcd_lsm_set_mlp_config)."""
         self._check(self._lib.mcd_lsm_set_mlp_config(self.handle, steps_first, steps, lr_first, lr))
 

@@ -144,7 +144,7 @@ def test_learned_per_date_fine_tuning_changes_little(engine, grid):
     c, _ = grid
     base = engine.lsm_batch(c, "fp32", "mlp")
     try:
-        engine.set_mlp_config(300, 5, 3e-3, 3e-4)
+        engine.set_mlp_config(100, 5, 3e-3, 3e-4)
         tuned = engine.lsm_batch(c, "fp32", "mlp")
     finally:
         engine.set_mlp_config()
