@@ -1,0 +1,4 @@
+// Forwarding header: the reference's mcd/pricers/lsm.hpp resolves to the GPU shim, so
+// reference code that includes it builds unchanged against libmcd_shim.so.
+#pragma once
+#include "../../../mcd_shim.hpp"
