@@ -36,6 +36,12 @@ enum class AverageStyle : std::uint8_t { Arithmetic, Geometric };
 // include/mcd/core/sobol.hpp:14 (this engine: 256 dimensions)
 constexpr unsigned kSobolMaxDimensions = 256;
 
+// include/mcd/core/rng_simd.hpp:14-18: whether the reference's NEON batch
+// draw path is compiled in.  The draws here come from the GPU on any host, so
+// the flag is false (the Python module's HAS_NEON and the JSON CLI's
+// simd_enabled say the same).
+inline constexpr bool kHasNeon = false;
+
 namespace gpu {
 
 enum class Precision : int { FP64 = 0, FP32 = 1 };

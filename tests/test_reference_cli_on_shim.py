@@ -2,8 +2,9 @@
 against the GPU shim.
 
 derivative-pricing_gb300/cpp/compat holds forwarding headers: each of the
-reference's mcd/pricers/*, mcd/greeks/*, mcd/models/heston, mcd/core/types and
-mcd/core/sobol headers resolves to cpp/mcd_shim.hpp, so a reference caller
+reference's mcd/pricers/*, mcd/greeks/*, mcd/models/heston, mcd/core/types,
+mcd/core/sobol and mcd/core/rng_simd headers resolves to cpp/mcd_shim.hpp, so a
+reference caller
 builds without an edit and links libmcd_shim.so (the GPU engine) instead of
 libmcd_core.a.  Only the CLI's JSON reader (src/core/json.cpp) still comes from
 the reference.  The recipe is oracle/Makefile's ``refcli-on-shim`` target; it
