@@ -85,6 +85,11 @@ Ctx::~Ctx() {
         if (ev_start[i]) cudaEventDestroy(ev_start[i]);
         if (ev_stop[i]) cudaEventDestroy(ev_stop[i]);
     }
+    for (int i = 0; i < kAuxStreams; ++i) {
+        if (aux_stream[i]) cudaStreamDestroy(aux_stream[i]);
+        if (ev_join[i]) cudaEventDestroy(ev_join[i]);
+    }
+    if (ev_fork) cudaEventDestroy(ev_fork);
     if (stream) cudaStreamDestroy(stream);
     release_extensions();
 }
@@ -817,6 +822,18 @@ void Ctx::collect_timing(bool block) {
         ev_head = (ev_head + 1) % kEventPairs;
         --ev_count;
     }
+}
+
+int Ctx::ensure_aux() {
+    if (ev_fork) return MCD_OK;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < kAuxStreams && e == cudaSuccess; ++i) {
+        e = cudaStreamCreateWithFlags(&aux_stream[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_join[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "auxiliary streams");
+    return MCD_OK;
 }
 
 void Ctx::release_extensions() {

@@ -83,6 +83,13 @@ struct Ctx {
     LaunchShape shape[2];
     std::vector<CachedGraph> graphs;
 
+    // Extra streams and events for graphs captured as concurrent chains
+    // (fork from and join to `stream`); created on first use.
+    static constexpr int kAuxStreams = 3;
+    cudaStream_t aux_stream[kAuxStreams] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[kAuxStreams] = {};
+    int ensure_aux();
+
     // Per-launch timing: a ring of (start, stop) event pairs recorded around
     // each graph launch on the launching stream; completed pairs are folded
     // into kernel_ms_sum by collect_timing().

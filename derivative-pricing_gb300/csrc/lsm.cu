@@ -191,9 +191,9 @@ __device__ void block_sum(double (&v)[N], double (*smem)[N]) {
 template <int PREC>
 __global__ void __launch_bounds__(kLsmThreads)
     lsm_forward(const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
-                uint32_t total_chunks, void* __restrict__ store) {
-    const uint32_t chunk = blockIdx.x;
-    if (chunk >= total_chunks) return;
+                uint32_t chunk_first, uint32_t chunk_end, void* __restrict__ store) {
+    const uint32_t chunk = chunk_first + blockIdx.x;
+    if (chunk >= chunk_end) return;
     const LsmDev c = cs[chunk_contract[chunk]];
     const uint32_t local = chunk - c.chunk_begin;
     const PhiloxKeys k = philox_keys(c.seed);
@@ -539,7 +539,7 @@ __device__ bool publish_and_fold(uint32_t chunk, const LsmDev& c, const LsmParti
 template <int PREC, bool COMP>
 __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 8)
     lsm_step(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
-             uint32_t total_chunks, const void* __restrict__ store, double* __restrict__ cf,
+             uint32_t chunk_first, uint32_t chunk_end, const void* __restrict__ store, double* __restrict__ cf,
              LsmReg* __restrict__ reg, LsmPartial* __restrict__ part, LsmPartial* __restrict__ gpart,
              Welford* __restrict__ final_part, uint32_t* __restrict__ counters,
              uint32_t* __restrict__ group_counters, uint32_t* __restrict__ need_second_pass, double kappa_max) {
@@ -550,8 +550,8 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 8)
     __shared__ Welford swf[kLsmThreads / 32];
     __shared__ Sum64 s64[kLsmThreads / 32];
     __shared__ int s_last;
-    const uint32_t chunk = blockIdx.x;
-    if (chunk >= total_chunks) return;
+    const uint32_t chunk = chunk_first + blockIdx.x;
+    if (chunk >= chunk_end) return;
     const uint32_t ci = chunk_contract[chunk];
     const LsmDev c = cs[ci];
     const int n = c.n_steps;
@@ -793,7 +793,7 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 8)
 template <int PREC>
 __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
     lsm_refine(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ chunk_contract,
-               uint32_t total_chunks, const void* __restrict__ store, const double* __restrict__ cf,
+               uint32_t chunk_first, uint32_t chunk_end, const void* __restrict__ store, const double* __restrict__ cf,
                LsmReg* __restrict__ reg, LsmPartial* __restrict__ part, LsmPartial* __restrict__ gpart,
                uint32_t* __restrict__ counters, uint32_t* __restrict__ group_counters,
                const uint32_t* __restrict__ need_second_pass) {
@@ -802,7 +802,7 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
     __shared__ double sres[15];
     __shared__ int s_last;
     if (__ldcg(need_second_pass + k) == 0) return;  // no date of this iteration needs it
-    for (uint32_t chunk = blockIdx.x; chunk < total_chunks; chunk += gridDim.x) {
+    for (uint32_t chunk = chunk_first + blockIdx.x; chunk < chunk_end; chunk += gridDim.x) {
     const uint32_t ci = chunk_contract[chunk];
     const LsmDev c = cs[ci];
     const int date = c.n_steps - k - 1;
@@ -943,26 +943,31 @@ __global__ void lsm_finish(const LsmDev* __restrict__ cs, int n_contracts,
 }  // namespace
 
 cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
-                               const uint32_t* chunk_contract, uint32_t total_chunks, void* s_store,
-                               cudaStream_t stream) {
+                               const uint32_t* chunk_contract, uint32_t chunk_first, uint32_t chunk_count,
+                               void* s_store, cudaStream_t stream) {
     (void)n_contracts;
     cudaGetLastError();
-    if (total_chunks == 0) return cudaSuccess;
+    if (chunk_count == 0) return cudaSuccess;
+    const uint32_t end = chunk_first + chunk_count;
     if (precision == 0)
-        lsm_forward<0><<<total_chunks, kLsmThreads, 0, stream>>>(c, chunk_contract, total_chunks, s_store);
+        lsm_forward<0><<<chunk_count, kLsmThreads, 0, stream>>>(c, chunk_contract, chunk_first, end, s_store);
     else
-        lsm_forward<1><<<total_chunks, kLsmThreads, 0, stream>>>(c, chunk_contract, total_chunks, s_store);
+        lsm_forward<1><<<chunk_count, kLsmThreads, 0, stream>>>(c, chunk_contract, chunk_first, end, s_store);
     return cudaGetLastError();
 }
 
 cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_contracts,
-                                 const uint32_t* chunk_contract, uint32_t total_chunks, uint32_t total_groups,
-                                 const void* s_store, double* cf, LsmReg* reg, LsmPartial* part,
-                                 LsmPartial* gpart, Welford* final_part, uint32_t* counters, cudaStream_t stream) {
+                                 const uint32_t* chunk_contract, uint32_t chunk_first, uint32_t chunk_count,
+                                 uint32_t total_groups, const void* s_store, double* cf, LsmReg* reg,
+                                 LsmPartial* part, LsmPartial* gpart, Welford* final_part, uint32_t* counters,
+                                 cudaStream_t stream) {
     cudaGetLastError();
-    if (total_chunks == 0) return cudaSuccess;
+    if (chunk_count == 0) return cudaSuccess;
+    const uint32_t end = chunk_first + chunk_count;
     // counters: 2 per contract (first pass, second pass), 2 per group, then
-    // one word per iteration counting the dates marked for the second pass.
+    // one word per iteration counting the dates marked for the second pass
+    // (shared by concurrent chains: a chain's second pass reads it after its
+    // own first pass, and only adds are made to it).
     uint32_t* group_counters = counters + 2 * static_cast<size_t>(n_contracts);
     uint32_t* need = group_counters + 2 * static_cast<size_t>(total_groups);
     // The second pass always runs after the first iteration (its lag is the
@@ -970,7 +975,7 @@ cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_co
     // persistent grid whose CTAs walk the chunks and skip those of contracts
     // whose date needs no second pass (all of them return at once when no
     // date does).
-    const unsigned refine_grid = (k == 0 || total_chunks < kRefineGrid) ? total_chunks : kRefineGrid;
+    const unsigned refine_grid = (k == 0 || chunk_count < kRefineGrid) ? chunk_count : kRefineGrid;
     // Condition bound below which a date is solved from its lagged sums: FP64
     // sums are good to ~1e-15, so 1e2 keeps the solve near FP64 accuracy; the
     // FP32 path's plain chunk sums are good to ~1e-8 relative once summed
@@ -978,25 +983,25 @@ cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_co
     // FP32 basis values carry anyway.
     if (precision == 0) {
         if (k == 0)
-            lsm_step<0, true><<<total_chunks, kLsmThreads, 0, stream>>>(
-                k, c, chunk_contract, total_chunks, s_store, cf, reg, part, gpart, final_part, counters,
+            lsm_step<0, true><<<chunk_count, kLsmThreads, 0, stream>>>(
+                k, c, chunk_contract, chunk_first, end, s_store, cf, reg, part, gpart, final_part, counters,
                 group_counters, need, 1e2);
         else
-            lsm_step<0, false><<<total_chunks, kLsmThreads, 0, stream>>>(
-                k, c, chunk_contract, total_chunks, s_store, cf, reg, part, gpart, final_part, counters,
+            lsm_step<0, false><<<chunk_count, kLsmThreads, 0, stream>>>(
+                k, c, chunk_contract, chunk_first, end, s_store, cf, reg, part, gpart, final_part, counters,
                 group_counters, need, 1e2);
-        lsm_refine<0><<<refine_grid, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
+        lsm_refine<0><<<refine_grid, kLsmThreads, 0, stream>>>(k, c, chunk_contract, chunk_first, end, s_store, cf,
                                                                reg, part, gpart, counters, group_counters, need);
     } else {
         if (k == 0)
-            lsm_step<1, true><<<total_chunks, kLsmThreads, 0, stream>>>(
-                k, c, chunk_contract, total_chunks, s_store, cf, reg, part, gpart, final_part, counters,
+            lsm_step<1, true><<<chunk_count, kLsmThreads, 0, stream>>>(
+                k, c, chunk_contract, chunk_first, end, s_store, cf, reg, part, gpart, final_part, counters,
                 group_counters, need, 1e3);
         else
-            lsm_step<1, false><<<total_chunks, kLsmThreads, 0, stream>>>(
-                k, c, chunk_contract, total_chunks, s_store, cf, reg, part, gpart, final_part, counters,
+            lsm_step<1, false><<<chunk_count, kLsmThreads, 0, stream>>>(
+                k, c, chunk_contract, chunk_first, end, s_store, cf, reg, part, gpart, final_part, counters,
                 group_counters, need, 1e3);
-        lsm_refine<1><<<refine_grid, kLsmThreads, 0, stream>>>(k, c, chunk_contract, total_chunks, s_store, cf,
+        lsm_refine<1><<<refine_grid, kLsmThreads, 0, stream>>>(k, c, chunk_contract, chunk_first, end, s_store, cf,
                                                                reg, part, gpart, counters, group_counters, need);
     }
     return cudaGetLastError();

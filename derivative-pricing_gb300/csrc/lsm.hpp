@@ -71,17 +71,21 @@ struct FrozenDev {
     float inv_2hs_f, inv_hs2_f, inv_2hv_f, pad;
 };
 
+// Forward simulation of chunks [chunk_first, chunk_first + chunk_count).
 cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
-                               const uint32_t* chunk_contract, uint32_t total_chunks, void* s_store,
-                               cudaStream_t stream);
-// One backward iteration k of every contract (see lsm.cu).  part: one
+                               const uint32_t* chunk_contract, uint32_t chunk_first, uint32_t chunk_count,
+                               void* s_store, cudaStream_t stream);
+// One backward iteration k (see lsm.cu) of the contracts whose chunks are
+// [chunk_first, chunk_first + chunk_count) -- whole contracts.  part: one
 // partial per chunk, gpart: one per group (LsmDev::group_begin/n_groups),
 // counters zeroed before the first iteration: 2 per contract, 2 per group,
-// then one word per iteration.
+// then one word per iteration.  Launches for disjoint sets of contracts may
+// run concurrently on different streams.
 cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_contracts,
-                                 const uint32_t* chunk_contract, uint32_t total_chunks, uint32_t total_groups,
-                                 const void* s_store, double* cf, LsmReg* reg, LsmPartial* part,
-                                 LsmPartial* gpart, Welford* final_part, uint32_t* counters, cudaStream_t stream);
+                                 const uint32_t* chunk_contract, uint32_t chunk_first, uint32_t chunk_count,
+                                 uint32_t total_groups, const void* s_store, double* cf, LsmReg* reg,
+                                 LsmPartial* part, LsmPartial* gpart, Welford* final_part, uint32_t* counters,
+                                 cudaStream_t stream);
 cudaError_t launch_lsm_finish(const LsmDev* c, int n_contracts, const Welford* final_part,
                               double* out /* n x 6: price, se, count, inception, mean, se */,
                               cudaStream_t stream);

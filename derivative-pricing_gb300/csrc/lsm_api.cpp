@@ -23,6 +23,10 @@ enum { kDev = 4, kChunkMap = 5, kStore = 6, kCf = 7, kReg = 8, kPartA = 9, kPart
        kGroupMap = 18, kGramPart = 19, kFeats = 20, kMomPart = 35, kFzDev = 36, kFzPart = 37,
        kFzOut = 38, kETab = 39, kCounters = 40 };  // kPartB: group partials
 
+// Concurrent chains of the QR backward pass (at most Ctx::kAuxStreams + 1).
+constexpr int kLsmChains = 2;
+static_assert(kLsmChains <= Ctx::kAuxStreams + 1, "one stream per chain");
+
 struct LsmPlan {
     std::vector<LsmDev> dev;
     std::vector<uint32_t> chunk_contract;
@@ -169,38 +173,79 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
     const MlpConfig cfg{ctx.mlp_steps_first, ctx.mlp_steps, ctx.mlp_lr_first, ctx.mlp_lr};
 
     // Capture forward pass + every backward iteration + finish into one graph.
+    // The QR regression runs its contracts as up to kLsmChains independent
+    // chains (contiguous ranges of about equal chunk counts), each captured on
+    // its own stream: a date's pass ends with a tail -- the last chunks' folds
+    // and the contract's solve, which its next date waits for -- and another
+    // chain's work fills the GPU meanwhile.  Chains share no data but the
+    // second-pass counters (see launch_lsm_iteration).
+    struct Chain {
+        uint32_t chunk_first, chunk_count;
+        int max_steps;
+    };
+    std::vector<Chain> chains;
+    if (!mlp) {
+        int rc2 = ctx.ensure_aux();
+        if (rc2) return rc2;
+        const int want = static_cast<int>(std::min<size_t>(n, static_cast<size_t>(kLsmChains)));
+        size_t ci = 0;
+        for (int j = 0; j < want && ci < n; ++j) {
+            const uint64_t target = static_cast<uint64_t>(p.total_chunks) * (j + 1) / want;
+            Chain ch{p.dev[ci].chunk_begin, 0, 0};
+            while (ci < n && (j == want - 1 || ch.chunk_first + ch.chunk_count < target || ch.chunk_count == 0)) {
+                ch.chunk_count += p.dev[ci].n_chunks;
+                ch.max_steps = std::max(ch.max_steps, p.dev[ci].n_steps);
+                ++ci;
+            }
+            chains.push_back(ch);
+        }
+    } else {
+        chains.push_back(Chain{0, p.total_chunks, p.max_steps});
+    }
     cudaGetLastError();
     cudaGraph_t graph = nullptr;
     e = cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return ctx.cuda_fail(e, "lsm begin capture");
     const LsmDev* d_dev = static_cast<const LsmDev*>(ctx.ext[kDev].ptr);
     const uint32_t* d_map = static_cast<const uint32_t*>(ctx.ext[kChunkMap].ptr);
-    cudaError_t le = launch_lsm_forward(precision, d_dev, static_cast<int>(n), d_map, p.total_chunks,
-                                        ctx.ext[kStore].ptr, ctx.stream);
-    for (int k = 0; k < p.max_steps && le == cudaSuccess; ++k) {
-        if (mlp)
-            le = launch_lsm_mlp_iteration(precision, k, !frozen, d_dev, static_cast<int>(n),
-                                          static_cast<const uint32_t*>(ctx.ext[kGroupMap].ptr), p.total_groups,
-                                          ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
-                                          static_cast<float*>(ctx.ext[kNets].ptr),
-                                          static_cast<float*>(ctx.ext[kSnaps].ptr),
-                                          static_cast<int*>(ctx.ext[kSnapOk].ptr),
-                                          static_cast<int*>(ctx.ext[kAdamT].ptr),
-                                          static_cast<float*>(ctx.ext[kGramPart].ptr),
-                                          static_cast<float*>(ctx.ext[kFeats].ptr),
-                                          static_cast<float*>(ctx.ext[kETab].ptr),
-                                          static_cast<unsigned long long*>(ctx.ext[kMomPart].ptr), cfg,
+    cudaError_t le = cudaSuccess;
+    if (chains.size() > 1) le = cudaEventRecord(ctx.ev_fork, ctx.stream);
+    for (size_t j = 0; j < chains.size() && le == cudaSuccess; ++j) {
+        const Chain& ch = chains[j];
+        cudaStream_t cs = j == 0 ? ctx.stream : ctx.aux_stream[j - 1];
+        if (j > 0) le = cudaStreamWaitEvent(cs, ctx.ev_fork, 0);
+        if (le == cudaSuccess)
+            le = launch_lsm_forward(precision, d_dev, static_cast<int>(n), d_map, ch.chunk_first, ch.chunk_count,
+                                    ctx.ext[kStore].ptr, cs);
+        for (int k = 0; k < ch.max_steps && le == cudaSuccess; ++k) {
+            if (mlp)
+                le = launch_lsm_mlp_iteration(precision, k, !frozen, d_dev, static_cast<int>(n),
+                                              static_cast<const uint32_t*>(ctx.ext[kGroupMap].ptr), p.total_groups,
+                                              ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
+                                              static_cast<float*>(ctx.ext[kNets].ptr),
+                                              static_cast<float*>(ctx.ext[kSnaps].ptr),
+                                              static_cast<int*>(ctx.ext[kSnapOk].ptr),
+                                              static_cast<int*>(ctx.ext[kAdamT].ptr),
+                                              static_cast<float*>(ctx.ext[kGramPart].ptr),
+                                              static_cast<float*>(ctx.ext[kFeats].ptr),
+                                              static_cast<float*>(ctx.ext[kETab].ptr),
+                                              static_cast<unsigned long long*>(ctx.ext[kMomPart].ptr), cfg,
+                                              static_cast<Welford*>(ctx.ext[kFinal].ptr),
+                                              static_cast<uint32_t*>(ctx.ext[kErr].ptr), cs);
+            else
+                le = launch_lsm_iteration(precision, k, d_dev, static_cast<int>(n), d_map, ch.chunk_first,
+                                          ch.chunk_count, p.total_groups, ctx.ext[kStore].ptr,
+                                          static_cast<double*>(ctx.ext[kCf].ptr),
+                                          static_cast<LsmReg*>(ctx.ext[kReg].ptr),
+                                          static_cast<LsmPartial*>(ctx.ext[kPartA].ptr),
+                                          static_cast<LsmPartial*>(ctx.ext[kPartB].ptr),
                                           static_cast<Welford*>(ctx.ext[kFinal].ptr),
-                                          static_cast<uint32_t*>(ctx.ext[kErr].ptr), ctx.stream);
-        else
-            le = launch_lsm_iteration(precision, k, d_dev, static_cast<int>(n), d_map, p.total_chunks,
-                                      p.total_groups, ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
-                                      static_cast<LsmReg*>(ctx.ext[kReg].ptr),
-                                      static_cast<LsmPartial*>(ctx.ext[kPartA].ptr),
-                                      static_cast<LsmPartial*>(ctx.ext[kPartB].ptr),
-                                      static_cast<Welford*>(ctx.ext[kFinal].ptr),
-                                      static_cast<uint32_t*>(ctx.ext[kCounters].ptr), ctx.stream);
+                                          static_cast<uint32_t*>(ctx.ext[kCounters].ptr), cs);
+        }
+        if (j > 0 && le == cudaSuccess) le = cudaEventRecord(ctx.ev_join[j - 1], cs);
     }
+    for (size_t j = 1; j < chains.size() && le == cudaSuccess; ++j)
+        le = cudaStreamWaitEvent(ctx.stream, ctx.ev_join[j - 1], 0);
     if (le == cudaSuccess)
         le = launch_lsm_finish(d_dev, static_cast<int>(n), static_cast<const Welford*>(ctx.ext[kFinal].ptr),
                                static_cast<double*>(ctx.ext[kOut].ptr), ctx.stream);
