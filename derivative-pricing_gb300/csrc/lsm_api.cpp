@@ -23,7 +23,7 @@ enum { kDev = 4, kChunkMap = 5, kStore = 6, kCf = 7, kReg = 8, kPartA = 9, kPart
        kGroupMap = 18, kGramPart = 19, kFeats = 20, kMomPart = 35, kFzDev = 36, kFzPart = 37,
        kFzOut = 38, kETab = 39, kCounters = 40 };  // kPartB: group partials
 
-// Concurrent chains of the QR backward pass (at most Ctx::kAuxStreams + 1).
+// Concurrent chains of the backward pass (at most Ctx::kAuxStreams + 1).
 constexpr int kLsmChains = 2;
 static_assert(kLsmChains <= Ctx::kAuxStreams + 1, "one stream per chain");
 
@@ -173,34 +173,37 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
     const MlpConfig cfg{ctx.mlp_steps_first, ctx.mlp_steps, ctx.mlp_lr_first, ctx.mlp_lr};
 
     // Capture forward pass + every backward iteration + finish into one graph.
-    // The QR regression runs its contracts as up to kLsmChains independent
-    // chains (contiguous ranges of about equal chunk counts), each captured on
-    // its own stream: a date's pass ends with a tail -- the last chunks' folds
-    // and the contract's solve, which its next date waits for -- and another
-    // chain's work fills the GPU meanwhile.  Chains share no data but the
-    // second-pass counters (see launch_lsm_iteration).
+    // The contracts run as up to kLsmChains independent chains (contiguous
+    // ranges of about equal chunk counts), each captured on its own stream: a
+    // date ends with a tail of little parallelism -- the QR pass's last chunk
+    // folds and per-contract solve, the learned fit's per-contract node
+    // tables, Gram slices and solve -- and another chain's work fills the GPU
+    // meanwhile.  Chains share no data but the QR second-pass counters (see
+    // launch_lsm_iteration) and the learned kernels' error word.
     struct Chain {
-        uint32_t chunk_first, chunk_count;
-        int max_steps;
+        uint32_t chunk_first = 0, chunk_count = 0, g_first = 0, g_end = 0;
+        int c_first = 0, c_end = 0, max_steps = 0;
     };
     std::vector<Chain> chains;
-    if (!mlp) {
+    {
         int rc2 = ctx.ensure_aux();
         if (rc2) return rc2;
         const int want = static_cast<int>(std::min<size_t>(n, static_cast<size_t>(kLsmChains)));
         size_t ci = 0;
         for (int j = 0; j < want && ci < n; ++j) {
             const uint64_t target = static_cast<uint64_t>(p.total_chunks) * (j + 1) / want;
-            Chain ch{p.dev[ci].chunk_begin, 0, 0};
+            Chain ch;
+            ch.chunk_first = p.dev[ci].chunk_begin;
+            ch.g_first = ch.g_end = p.dev[ci].group_begin;
+            ch.c_first = ch.c_end = static_cast<int>(ci);
             while (ci < n && (j == want - 1 || ch.chunk_first + ch.chunk_count < target || ch.chunk_count == 0)) {
                 ch.chunk_count += p.dev[ci].n_chunks;
+                ch.g_end = p.dev[ci].group_begin + p.dev[ci].n_groups;
                 ch.max_steps = std::max(ch.max_steps, p.dev[ci].n_steps);
-                ++ci;
+                ch.c_end = static_cast<int>(++ci);
             }
             chains.push_back(ch);
         }
-    } else {
-        chains.push_back(Chain{0, p.total_chunks, p.max_steps});
     }
     cudaGetLastError();
     cudaGraph_t graph = nullptr;
@@ -219,9 +222,9 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
                                     ctx.ext[kStore].ptr, cs);
         for (int k = 0; k < ch.max_steps && le == cudaSuccess; ++k) {
             if (mlp)
-                le = launch_lsm_mlp_iteration(precision, k, !frozen, d_dev, static_cast<int>(n),
-                                              static_cast<const uint32_t*>(ctx.ext[kGroupMap].ptr), p.total_groups,
-                                              ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
+                le = launch_lsm_mlp_iteration(precision, k, !frozen, d_dev, ch.c_first, ch.c_end,
+                                              static_cast<const uint32_t*>(ctx.ext[kGroupMap].ptr), ch.g_first,
+                                              ch.g_end, ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
                                               static_cast<float*>(ctx.ext[kNets].ptr),
                                               static_cast<float*>(ctx.ext[kSnaps].ptr),
                                               static_cast<int*>(ctx.ext[kSnapOk].ptr),

@@ -365,13 +365,13 @@ __device__ __forceinline__ double path_s(const void* store, uint64_t idx) {
 // ---------------------------------------------------------------------------
 template <int PREC>
 __global__ void __launch_bounds__(128, 1)
-    lsm_mlp_train(int k, const LsmDev* __restrict__ cs, int n_contracts, const void* __restrict__ store,
+    lsm_mlp_train(int k, const LsmDev* __restrict__ cs, int c_first, int n_contracts, const void* __restrict__ store,
                   const double* __restrict__ cf, float* __restrict__ nets, float* __restrict__ snaps,
                   int* __restrict__ snap_ok, int* __restrict__ adam_t, MlpConfig cfg,
                   uint32_t* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
-    const int ci = blockIdx.x;
+    const int ci = c_first + static_cast<int>(blockIdx.x);
     if (ci >= n_contracts) return;
     const LsmDev c = cs[ci];
     const int n = c.n_steps;
@@ -480,13 +480,13 @@ __device__ __forceinline__ void layer1_row(const float* small, float x0, float x
 template <int PREC>
 __global__ void __launch_bounds__(128)
     lsm_mlp_pass(int k, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
-                 uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
+                 uint32_t g_first, uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
                  const float* __restrict__ snaps, const int* __restrict__ snap_ok, Welford* __restrict__ final_part,
                  uint32_t* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     PassSmem& S = *reinterpret_cast<PassSmem*>(smem_raw);
     __shared__ Welford swf[4];
-    const uint32_t g = blockIdx.x;
+    const uint32_t g = g_first + blockIdx.x;
     if (g >= total_groups) return;
     const uint32_t ci = group_contract[g];
     const LsmDev c = cs[ci];
@@ -664,14 +664,14 @@ __device__ void chol_solve_warp(const float* L, const float* inv_diag, const dou
 }
 
 __global__ void __launch_bounds__(kSolveThreads)
-    lsm_mlp_solve(int k, const LsmDev* __restrict__ cs, int n_contracts, const float* __restrict__ gram_part,
+    lsm_mlp_solve(int k, const LsmDev* __restrict__ cs, int c_first, int n_contracts, const float* __restrict__ gram_part,
                   float* __restrict__ nets, float* __restrict__ snaps, int* __restrict__ snap_ok) {
     __shared__ double G[kGramPacked];   // Gram matrix, packed upper triangle; standardised in place
     __shared__ float L[kM * kGramDim];  // FP32: working lower triangle; the factor, transposed, above it
     __shared__ float inv_diag[kM];
     __shared__ double sc[kM], xs[kM], res[kM];
     __shared__ int bad;
-    const int ci = blockIdx.x;
+    const int ci = c_first + static_cast<int>(blockIdx.x);
     if (ci >= n_contracts) return;
     const LsmDev c = cs[ci];
     const int d = c.n_steps - k - 1;
@@ -957,28 +957,30 @@ cudaError_t mlp_prepare() {
     return e;
 }
 
-cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int n_contracts,
-                                     const uint32_t* group_contract, uint32_t total_groups, const void* store,
+cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int c_first, int c_end,
+                                     const uint32_t* group_contract, uint32_t g_first, uint32_t g_end, const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
                                      float* gram_part, float* feats, float* etab, unsigned long long* mom_part,
                                      const MlpConfig& cfg, Welford* final_part, uint32_t* err, cudaStream_t stream) {
     cudaGetLastError();
-    if (total_groups == 0) return cudaSuccess;
+    if (g_end <= g_first || c_end <= c_first) return cudaSuccess;
+    const uint32_t n_groups = g_end - g_first;
+    const int n_contracts = c_end - c_first;
     const size_t pass_smem = sizeof(PassSmem);
     auto step = [&]() {  // the per-path network: terminal step, and replays of given networks
         if (precision == 0)
-            lsm_mlp_pass<0><<<total_groups, 128, pass_smem, stream>>>(k, c, group_contract, total_groups, store, cf,
+            lsm_mlp_pass<0><<<n_groups, 128, pass_smem, stream>>>(k, c, group_contract, g_first, g_end, store, cf,
                                                                       snaps, snap_ok, final_part, err);
         else
-            lsm_mlp_pass<1><<<total_groups, 128, pass_smem, stream>>>(k, c, group_contract, total_groups, store, cf,
+            lsm_mlp_pass<1><<<n_groups, 128, pass_smem, stream>>>(k, c, group_contract, g_first, g_end, store, cf,
                                                                       snaps, snap_ok, final_part, err);
     };
     auto trainer = [&]() {
         if (precision == 0)
-            lsm_mlp_train<0><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, n_contracts, store, cf, nets, snaps,
+            lsm_mlp_train<0><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, c_first, c_end, store, cf, nets, snaps,
                                                                               snap_ok, adam_t, cfg, err);
         else
-            lsm_mlp_train<1><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, n_contracts, store, cf, nets, snaps,
+            lsm_mlp_train<1><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, c_first, c_end, store, cf, nets, snaps,
                                                                               snap_ok, adam_t, cfg, err);
     };
     if (!train) {
@@ -991,11 +993,11 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
         trainer();    // learn the features on the latest date
         mode = kGram;
     }
-    cudaError_t e = launch_lsm_mlp_nodes(precision, k, mode, c, n_contracts, group_contract, total_groups, store, cf,
+    cudaError_t e = launch_lsm_mlp_nodes(precision, k, mode, c, c_first, c_end, group_contract, g_first, g_end, store, cf,
                                          nets, snaps, snap_ok, feats, etab, mom_part, gram_part, final_part, err,
                                          stream);
     if (e != cudaSuccess) return e;
-    lsm_mlp_solve<<<n_contracts, kSolveThreads, 0, stream>>>(k, c, n_contracts, gram_part, nets, snaps, snap_ok);
+    lsm_mlp_solve<<<n_contracts, kSolveThreads, 0, stream>>>(k, c, c_first, c_end, gram_part, nets, snaps, snap_ok);
     if (k > 0 && cfg.steps > 0) trainer();  // optional fine-tuning of the features
     return cudaGetLastError();
 }

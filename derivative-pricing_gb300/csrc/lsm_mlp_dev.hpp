@@ -76,8 +76,10 @@ __host__ __device__ inline NodeGrid node_grid(const LsmDev& c, int date) {
 // its fitted output layer, then the feature table of date n-k-1), the binned
 // path pass (exercise, discount, moments of date n-k-1), and the sliced Gram
 // matrices the solve sums.
-cudaError_t launch_lsm_mlp_nodes(int precision, int k, int mode, const LsmDev* c, int n_contracts,
-                                 const uint32_t* group_contract, uint32_t total_groups, const void* store,
+// Contracts [c_first, c_end) and their groups [g_first, g_end) (whole
+// contracts; launches for disjoint ranges may run concurrently).
+cudaError_t launch_lsm_mlp_nodes(int precision, int k, int mode, const LsmDev* c, int c_first, int c_end,
+                                 const uint32_t* group_contract, uint32_t g_first, uint32_t g_end, const void* store,
                                  double* cf, const float* nets, const float* snaps, const int* snap_ok,
                                  float* feats, float* etab, unsigned long long* mom_part, float* gram_part,
                                  Welford* final_part, uint32_t* err, cudaStream_t stream);
@@ -91,8 +93,9 @@ cudaError_t mlp_prepare();  // opts the kernels into their dynamic shared memory
 // given networks path by path (lsm_mlp_pass).  Buffers: gram_part
 // n x kNodeSlices x kGramPacked floats, feats n x kNodes x 64 floats, etab
 // n x kNodes floats, mom_part groups x kMoments x kNodes.
-cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int n_contracts,
-                                     const uint32_t* group_contract, uint32_t total_groups, const void* store,
+// Contracts [c_first, c_end), groups [g_first, g_end), as launch_lsm_mlp_nodes.
+cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int c_first, int c_end,
+                                     const uint32_t* group_contract, uint32_t g_first, uint32_t g_end, const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
                                      float* gram_part, float* feats, float* etab, unsigned long long* mom_part,
                                      const MlpConfig& cfg, Welford* final_part, uint32_t* err, cudaStream_t stream);

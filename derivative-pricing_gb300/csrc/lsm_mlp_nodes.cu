@@ -116,11 +116,11 @@ __device__ __forceinline__ void layer1_node(const float* w0, const float* c, flo
 }
 
 __global__ void __launch_bounds__(128)
-    lsm_mlp_nodes(int k, const LsmDev* __restrict__ cs, int n_contracts, const float* __restrict__ nets,
+    lsm_mlp_nodes(int k, const LsmDev* __restrict__ cs, int c_first, int n_contracts, const float* __restrict__ nets,
                   const float* __restrict__ snaps, const int* __restrict__ snap_ok, float* __restrict__ feats,
                   float* __restrict__ etab, uint32_t* __restrict__ err) {
     __shared__ NodeSmem S;
-    const int ci = blockIdx.x;
+    const int ci = c_first + static_cast<int>(blockIdx.x);
     if (ci >= n_contracts) return;
     const LsmDev c = cs[ci];
     const int n = c.n_steps;
@@ -227,7 +227,7 @@ constexpr int kBinThreads = 256;  // five CTAs per SM (48 registers): latency-bo
 template <int PREC>
 __global__ void __launch_bounds__(kBinThreads, 5)
     lsm_mlp_binned(int k, int mode, const LsmDev* __restrict__ cs, const uint32_t* __restrict__ group_contract,
-                   uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
+                   uint32_t g_first, uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
                    const int* __restrict__ snap_ok, const float* __restrict__ etab,
                    unsigned long long* __restrict__ mom_part, Welford* __restrict__ final_part) {
     __shared__ float tab[kNodes];                              // continuation table of date e
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(kBinThreads, 5)
     __shared__ Welford swf[kBinThreads / 32];
     __shared__ Sum64 s64[kBinThreads / 32];
     __shared__ NodeGrid s_grid[2];                             // dates e and e-1
-    const uint32_t g = blockIdx.x;
+    const uint32_t g = g_first + blockIdx.x;
     if (g >= total_groups) return;
     const uint32_t ci = group_contract[g];
     const LsmDev c = cs[ci];
@@ -380,13 +380,13 @@ constexpr int kBlockTasks = kBlocks * (kBlocks + 1) / 2;      // upper-triangula
 static_assert(kBlockTasks + kBlocks <= kGramThreads, "one task per thread");
 
 __global__ void __launch_bounds__(kGramThreads)
-    lsm_mlp_gram_slices(int k, const LsmDev* __restrict__ cs, int n_contracts,
+    lsm_mlp_gram_slices(int k, const LsmDev* __restrict__ cs, int c_first, int n_contracts,
                         const unsigned long long* __restrict__ mom_part, const float* __restrict__ feats,
                         float* __restrict__ gram_part) {
     __shared__ __align__(16) float F[kBinsPerSlice + 1][kFStride];
     __shared__ float wgt[5][kBinsPerSlice];  // Saa, Sab, Sbb, Say, Sby of each bin
     __shared__ double s_yb;
-    const int ci = blockIdx.x, slice = blockIdx.y;
+    const int ci = c_first + static_cast<int>(blockIdx.x), slice = blockIdx.y;
     if (ci >= n_contracts) return;
     const LsmDev c = cs[ci];
     const int d = c.n_steps - k - 1;
@@ -497,22 +497,24 @@ __global__ void __launch_bounds__(kGramThreads)
 
 }  // namespace
 
-cudaError_t launch_lsm_mlp_nodes(int precision, int k, int mode, const LsmDev* c, int n_contracts,
-                                 const uint32_t* group_contract, uint32_t total_groups, const void* store,
+cudaError_t launch_lsm_mlp_nodes(int precision, int k, int mode, const LsmDev* c, int c_first, int c_end,
+                                 const uint32_t* group_contract, uint32_t g_first, uint32_t g_end, const void* store,
                                  double* cf, const float* nets, const float* snaps, const int* snap_ok,
                                  float* feats, float* etab, unsigned long long* mom_part, float* gram_part,
                                  Welford* final_part, uint32_t* err, cudaStream_t stream) {
     cudaGetLastError();
-    if (n_contracts <= 0 || total_groups == 0) return cudaSuccess;
-    lsm_mlp_nodes<<<n_contracts, 128, 0, stream>>>(k, c, n_contracts, nets, snaps, snap_ok, feats, etab, err);
+    if (c_end <= c_first || g_end <= g_first) return cudaSuccess;
+    const int n_contracts = c_end - c_first;
+    const uint32_t n_groups = g_end - g_first;
+    lsm_mlp_nodes<<<n_contracts, 128, 0, stream>>>(k, c, c_first, c_end, nets, snaps, snap_ok, feats, etab, err);
     if (precision == 0)
-        lsm_mlp_binned<0><<<total_groups, kBinThreads, 0, stream>>>(k, mode, c, group_contract, total_groups, store, cf,
+        lsm_mlp_binned<0><<<n_groups, kBinThreads, 0, stream>>>(k, mode, c, group_contract, g_first, g_end, store, cf,
                                                                      snap_ok, etab, mom_part, final_part);
     else
-        lsm_mlp_binned<1><<<total_groups, kBinThreads, 0, stream>>>(k, mode, c, group_contract, total_groups, store, cf,
+        lsm_mlp_binned<1><<<n_groups, kBinThreads, 0, stream>>>(k, mode, c, group_contract, g_first, g_end, store, cf,
                                                                      snap_ok, etab, mom_part, final_part);
     if (mode & kGram)
-        lsm_mlp_gram_slices<<<dim3(n_contracts, kNodeSlices), kGramThreads, 0, stream>>>(k, c, n_contracts, mom_part,
+        lsm_mlp_gram_slices<<<dim3(n_contracts, kNodeSlices), kGramThreads, 0, stream>>>(k, c, c_first, c_end, mom_part,
                                                                                          feats, gram_part);
     return cudaGetLastError();
 }
