@@ -501,7 +501,7 @@ __device__ __forceinline__ bool last_arrival(uint32_t* counter, uint32_t expecte
 
 // Publishes this CTA's chunk partial (thread 0 wrote part[chunk]) and climbs
 // the two-level tree of the contract's sums: the last chunk of a group of
-// LsmDev::group_chunks chunks folds the group's partials in chunk order into
+// LsmDev::fold_chunks chunks folds the group's partials in chunk order into
 // the group partial, the last group of the contract folds the group partials
 // in group order.  Every fold is short (a few dozen to a few hundred rows over
 // the whole CTA), so the contract's totals are ready soon after its last
@@ -513,17 +513,17 @@ __device__ bool publish_and_fold(uint32_t chunk, const LsmDev& c, const LsmParti
                                  uint32_t* contract_counter, double (&tot)[15], double (*smem)[15],
                                  int* s_flag) {
     const uint32_t local = chunk - c.chunk_begin;
-    const uint32_t g = local / c.group_chunks;
-    const uint32_t first = g * c.group_chunks;
-    const uint32_t count = min(c.group_chunks, c.n_chunks - first);
-    if (!last_arrival(&group_counters[2 * (c.group_begin + g)], count, s_flag)) return false;
+    const uint32_t g = local / c.fold_chunks;
+    const uint32_t first = g * c.fold_chunks;
+    const uint32_t count = min(c.fold_chunks, c.n_chunks - first);
+    if (!last_arrival(&group_counters[2 * (c.fold_begin + g)], count, s_flag)) return false;
     fold_partials<15>(part, c.chunk_begin + first, count, tot, smem);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int q = 0; q < 15; ++q) gpart[c.group_begin + g].v[q] = tot[q];
+        for (int q = 0; q < 15; ++q) gpart[c.fold_begin + g].v[q] = tot[q];
     }
-    if (!last_arrival(contract_counter, c.n_groups, s_flag)) return false;
-    fold_partials<15>(gpart, c.group_begin, c.n_groups, tot, smem);
+    if (!last_arrival(contract_counter, c.n_folds, s_flag)) return false;
+    fold_partials<15>(gpart, c.fold_begin, c.n_folds, tot, smem);
     return true;
 }
 
@@ -958,18 +958,18 @@ cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
 
 cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_contracts,
                                  const uint32_t* chunk_contract, uint32_t chunk_first, uint32_t chunk_count,
-                                 uint32_t total_groups, const void* s_store, double* cf, LsmReg* reg,
+                                 uint32_t total_folds, const void* s_store, double* cf, LsmReg* reg,
                                  LsmPartial* part, LsmPartial* gpart, Welford* final_part, uint32_t* counters,
                                  cudaStream_t stream) {
     cudaGetLastError();
     if (chunk_count == 0) return cudaSuccess;
     const uint32_t end = chunk_first + chunk_count;
-    // counters: 2 per contract (first pass, second pass), 2 per group, then
+    // counters: 2 per contract (first pass, second pass), 2 per fold group, then
     // one word per iteration counting the dates marked for the second pass
     // (shared by concurrent chains: a chain's second pass reads it after its
     // own first pass, and only adds are made to it).
     uint32_t* group_counters = counters + 2 * static_cast<size_t>(n_contracts);
-    uint32_t* need = group_counters + 2 * static_cast<size_t>(total_groups);
+    uint32_t* need = group_counters + 2 * static_cast<size_t>(total_folds);
     // The second pass always runs after the first iteration (its lag is the
     // identity), on a CTA per chunk; later it is rare and runs on a small
     // persistent grid whose CTAs walk the chunks and skip those of contracts

@@ -29,11 +29,15 @@ struct LsmDev {
     int32_t n_steps, type;
     uint32_t group_begin, n_groups;  // learned regression: CTAs of group_chunks chunks each
     uint32_t group_chunks;
+    uint32_t fold_begin, n_folds;    // QR regression: second level of the chunk-sum tree,
+    uint32_t fold_chunks;            // groups of fold_chunks chunks
     float strike_f, inv_strike_f, disc_f, phi_f;  // FP32 copies for the FP32-path kernels
 };
 
 constexpr int kLsmMaxGroups = 256;  // learned-regression CTAs per contract at most
-constexpr int kLsmMinGroupChunks = 32;  // chunks per learned-regression CTA at least (amortises its set-up)
+constexpr int kLsmMinGroupChunks = 16;  // chunks per learned-regression CTA at least (amortises its set-up)
+constexpr int kLsmMaxFolds = 256;       // QR: fold groups per contract at most
+constexpr int kLsmMinFoldChunks = 32;   // QR: chunks per fold group at least
 constexpr int kGramPacked = 66 * 67 / 2;  // upper triangle of the 66 x 66 Gram matrix, row-major
 
 // Regression state of one (contract, date): T, the date's preconditioner
@@ -77,13 +81,13 @@ cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
                                void* s_store, cudaStream_t stream);
 // One backward iteration k (see lsm.cu) of the contracts whose chunks are
 // [chunk_first, chunk_first + chunk_count) -- whole contracts.  part: one
-// partial per chunk, gpart: one per group (LsmDev::group_begin/n_groups),
-// counters zeroed before the first iteration: 2 per contract, 2 per group,
+// partial per chunk, gpart: one per fold group (LsmDev::fold_begin/n_folds),
+// counters zeroed before the first iteration: 2 per contract, 2 per fold group,
 // then one word per iteration.  Launches for disjoint sets of contracts may
 // run concurrently on different streams.
 cudaError_t launch_lsm_iteration(int precision, int k, const LsmDev* c, int n_contracts,
                                  const uint32_t* chunk_contract, uint32_t chunk_first, uint32_t chunk_count,
-                                 uint32_t total_groups, const void* s_store, double* cf, LsmReg* reg,
+                                 uint32_t total_folds, const void* s_store, double* cf, LsmReg* reg,
                                  LsmPartial* part, LsmPartial* gpart, Welford* final_part, uint32_t* counters,
                                  cudaStream_t stream);
 cudaError_t launch_lsm_finish(const LsmDev* c, int n_contracts, const Welford* final_part,

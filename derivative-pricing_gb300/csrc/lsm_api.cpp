@@ -32,7 +32,7 @@ struct LsmPlan {
     std::vector<uint32_t> chunk_contract;
     std::vector<uint32_t> group_contract;  // learned regression: group -> contract
     uint64_t store_elems = 0, cf_elems = 0, reg_rows = 0;
-    uint32_t total_chunks = 0, total_groups = 0;
+    uint32_t total_chunks = 0, total_groups = 0, total_folds = 0;
     int max_steps = 0;
 };
 
@@ -94,6 +94,16 @@ int plan_lsm(Ctx& ctx, const mcd_lsm_contract* cs, size_t n, LsmPlan& p) {
         d.n_groups = groups;
         for (uint32_t g = 0; g < groups; ++g) p.group_contract.push_back(static_cast<uint32_t>(i));
         p.total_groups += groups;
+        // QR regression: the chunk sums are folded in groups of at least
+        // kLsmMinFoldChunks chunks (at most kLsmMaxFolds per contract), then
+        // the groups (lsm.cu, publish_and_fold)
+        const uint64_t per_fold =
+            std::max<uint64_t>((chunks + kLsmMaxFolds - 1) / kLsmMaxFolds, kLsmMinFoldChunks);
+        const uint32_t folds = static_cast<uint32_t>((chunks + per_fold - 1) / per_fold);
+        d.fold_chunks = static_cast<uint32_t>(per_fold);
+        d.fold_begin = p.total_folds;
+        d.n_folds = folds;
+        p.total_folds += folds;
         p.max_steps = std::max(p.max_steps, c.monitoring_points);
     }
     return MCD_OK;
@@ -122,10 +132,10 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
     if (!rc) rc = ctx.reserve(ctx.ext[kCf], sizeof(double) * std::max<uint64_t>(p.cf_elems, 1), "lsm cash flows");
     if (!rc) rc = ctx.reserve(ctx.ext[kReg], sizeof(LsmReg) * p.reg_rows, "lsm regression table");
     if (!rc) rc = ctx.reserve(ctx.ext[kPartA], sizeof(LsmPartial) * std::max<size_t>(p.total_chunks, 1), "lsm partials");
-    if (!rc) rc = ctx.reserve(ctx.ext[kPartB], sizeof(LsmPartial) * std::max<size_t>(p.total_groups, 1), "lsm group partials");
+    if (!rc) rc = ctx.reserve(ctx.ext[kPartB], sizeof(LsmPartial) * std::max<size_t>(p.total_folds, 1), "lsm group partials");
     if (!rc) rc = ctx.reserve(ctx.ext[kFinal], sizeof(Welford) * std::max<size_t>(p.total_chunks, 1), "lsm final partials");
     if (!rc) rc = ctx.reserve(ctx.ext[kOut], sizeof(double) * 6 * n, "lsm results");
-    const size_t n_counters = 2 * n + 2 * static_cast<size_t>(p.total_groups) + static_cast<size_t>(p.max_steps) + 1;
+    const size_t n_counters = 2 * n + 2 * static_cast<size_t>(p.total_folds) + static_cast<size_t>(p.max_steps) + 1;
     if (!rc) rc = ctx.reserve(ctx.ext[kCounters], sizeof(uint32_t) * n_counters, "lsm chunk counters");
     if (!rc && mlp) {
         rc = ctx.reserve(ctx.ext[kNets], sizeof(float) * 3 * mlp::kParamStride * n, "mlp networks");
@@ -237,7 +247,7 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
                                               static_cast<uint32_t*>(ctx.ext[kErr].ptr), cs);
             else
                 le = launch_lsm_iteration(precision, k, d_dev, static_cast<int>(n), d_map, ch.chunk_first,
-                                          ch.chunk_count, p.total_groups, ctx.ext[kStore].ptr,
+                                          ch.chunk_count, p.total_folds, ctx.ext[kStore].ptr,
                                           static_cast<double*>(ctx.ext[kCf].ptr),
                                           static_cast<LsmReg*>(ctx.ext[kReg].ptr),
                                           static_cast<LsmPartial*>(ctx.ext[kPartA].ptr),

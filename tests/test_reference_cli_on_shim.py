@@ -31,12 +31,12 @@ CLI = os.path.join(ORACLE, "_ref", "mcd_cli_on_shim")
 
 @pytest.fixture(scope="module")
 def cli():
+    if subprocess.run(["make", "-s", "-C", ORACLE, "has-ref"], capture_output=True).returncode != 0:
+        pytest.skip("the reference's sources are not on this machine")
     import build as B
     B.build()
     r = subprocess.run(["make", "-s", "-C", ORACLE, "refcli-on-shim"], capture_output=True, text=True)
     if r.returncode != 0:
-        if "reference sources not found" in r.stdout + r.stderr:
-            pytest.skip("the reference's sources are not on this machine")
         raise RuntimeError(r.stdout + r.stderr)
     return CLI
 
