@@ -23,9 +23,12 @@ enum { kDev = 4, kChunkMap = 5, kStore = 6, kCf = 7, kReg = 8, kPartA = 9, kPart
        kGroupMap = 18, kGramPart = 19, kFeats = 20, kMomPart = 35, kFzDev = 36, kFzPart = 37,
        kFzOut = 38, kETab = 39, kCounters = 40 };  // kPartB: group partials
 
-// Concurrent chains of the backward pass (at most Ctx::kAuxStreams + 1).
+// Concurrent chains of the backward pass (at most Ctx::kAuxStreams + 1):
+// QR regression, learned regression.
 constexpr int kLsmChains = 2;
-static_assert(kLsmChains <= Ctx::kAuxStreams + 1, "one stream per chain");
+constexpr int kLsmChainsLearned = 2;
+static_assert(kLsmChains <= Ctx::kAuxStreams + 1 && kLsmChainsLearned <= Ctx::kAuxStreams + 1,
+              "one stream per chain");
 
 struct LsmPlan {
     std::vector<LsmDev> dev;
@@ -198,7 +201,7 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
     {
         int rc2 = ctx.ensure_aux();
         if (rc2) return rc2;
-        const int want = static_cast<int>(std::min<size_t>(n, static_cast<size_t>(kLsmChains)));
+        const int want = static_cast<int>(std::min<size_t>(n, static_cast<size_t>(mlp ? kLsmChainsLearned : kLsmChains)));
         size_t ci = 0;
         for (int j = 0; j < want && ci < n; ++j) {
             const uint64_t target = static_cast<uint64_t>(p.total_chunks) * (j + 1) / want;
