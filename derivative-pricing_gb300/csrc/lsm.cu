@@ -458,6 +458,7 @@ __device__ void solve_lagged(const double s[15], const double L[4][4], double ka
             r.gamma[a] = x;
             r.gamma_f[a] = static_cast<float>(x);
         }
+        laguerre_poly(r.gamma, r.poly_f);
         r.has = 1;
     } else {
         r.has = 2;
@@ -647,8 +648,11 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 8)
         // and the final payoff sums up to the warp are compensated FP32,
         // everything above FP64.
         const float phi = c.phi_f, strike = c.strike_f, inv_kf = c.inv_strike_f, disc = c.disc_f;
-        const float g0f = exercise ? re->gamma_f[0] : 0.0f, g1f = exercise ? re->gamma_f[1] : 0.0f,
-                    g2f = exercise ? re->gamma_f[2] : 0.0f, g3f = exercise ? re->gamma_f[3] : 0.0f;
+        float poly[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (exercise) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) poly[q] = re->poly_f[q];
+        }
         float T[10];
 #pragma unroll
         for (int q = 0; q < 10; ++q) T[q] = init ? ((q == 0 || q == 4 || q == 7 || q == 9) ? 1.0f : 0.0f) : re->T_f[q];
@@ -659,42 +663,44 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 8)
         for (int q = 0; q < 15; ++q) hi[q] = lo[q] = 0.0f;
         Sum32 fin{0u, 0.0f, 0.0f, 0.0f, 0.0f};  // final payoffs (last date)
         constexpr int kPer = kLsmChunk / kLsmThreads;
-        // all loads of this thread's paths first (independent, in flight together)
+        // all loads of this thread's paths first (independent, in flight together);
+        // the columns' thread bases once, 32-bit offsets within the chunk
+        const uint64_t cb = static_cast<uint64_t>(local) * kLsmChunk;  // first path of the chunk
+        const uint64_t i0 = cb + threadIdx.x;
+        const uint32_t in_chunk = static_cast<uint32_t>(
+            c.path_count - cb < static_cast<uint64_t>(kLsmChunk) ? c.path_count - cb : static_cast<uint64_t>(kLsmChunk));
+        float* cf_t = cff + i0;
+        const float* col_v = init ? S + static_cast<uint64_t>(n - 1) * c.path_count + i0 : cf_t;
+        const float* col_e = S + static_cast<uint64_t>(exercise ? e - 1 : 0) * c.path_count + i0;
+        const float* col_d = S + static_cast<uint64_t>(gram ? e - 2 : 0) * c.path_count + i0;
         float vv[kPer], se[kPer], sd[kPer];
         bool live[kPer];
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
-            const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
-            live[j] = i < c.path_count;
+            const uint32_t o = static_cast<uint32_t>(j * kLsmThreads);
+            live[j] = o + threadIdx.x < in_chunk;
             vv[j] = 0.0f;
             se[j] = 0.0f;
             sd[j] = 0.0f;
             if (live[j]) {
-                if (init) vv[j] = S[static_cast<uint64_t>(n - 1) * c.path_count + i];
-                else vv[j] = cff[i];
-                if (exercise) se[j] = S[static_cast<uint64_t>(e - 1) * c.path_count + i];
-                if (gram) sd[j] = S[static_cast<uint64_t>(e - 2) * c.path_count + i];
+                vv[j] = col_v[o];
+                if (exercise) se[j] = col_e[o];
+                if (gram) sd[j] = col_d[o];
             }
         }
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
             if (!live[j]) continue;
-            const uint64_t i = static_cast<uint64_t>(local) * kLsmChunk + j * kLsmThreads + threadIdx.x;
             float v = init ? fmaxf(phi * (vv[j] - strike), 0.0f) : vv[j];
             if (exercise) {
                 const float ex = phi * (se[j] - strike);
-                if (ex > 0.0f) {
-                    float b[4];
-                    basis32(se[j], inv_kf, b);
-                    const float cont = __fmaf_rn(g3f, b[3], __fmaf_rn(g2f, b[2], __fmaf_rn(g1f, b[1], g0f * b[0])));
-                    if (ex > cont) v = ex;
-                }
+                if (ex > 0.0f && ex > continuation_poly32(se[j], inv_kf, poly)) v = ex;
             }
             v *= disc;
             if (last) {
                 sum32_add(fin, v);
             } else {
-                cff[i] = v;
+                cf_t[j * kLsmThreads] = v;
                 if (phi * (sd[j] - strike) > 0.0f) {
                     float b[4];
                     basis32(sd[j], inv_kf, b);
@@ -911,6 +917,7 @@ __global__ void __launch_bounds__(kLsmThreads, PREC == 0 ? 1 : 4)
                 r.gamma[a] = gamma[a];
                 r.gamma_f[a] = static_cast<float>(gamma[a]);
             }
+            laguerre_poly(r.gamma, r.poly_f);
             r.has = 1;
         }
     }

@@ -51,6 +51,8 @@ struct LsmReg {
     int32_t degenerate;   // Cholesky of the lagged Gram matrix: 0 plain, 2 with a diagonal shift, 1 failed
     float T_f[10];        // FP32 copies for the FP32-path kernels (written with T and gamma)
     float gamma_f[4];
+    float poly_f[4];      // FP32 path: the continuation value e^{-x/2} (p0 + p1 x + p2 x^2 + p3 x^3),
+                          // x = S/K, the Laguerre combination gamma expanded in FP64 (laguerre_poly)
 };
 
 // Per-chunk partial sums of one date's regression: count + 10 Gram entries +
@@ -76,6 +78,26 @@ struct FrozenDev {
 };
 
 // Forward simulation of chunks [chunk_first, chunk_first + chunk_count).
+// Monomial coefficients of gamma_0 L_0 + ... + gamma_3 L_3 (the weighted
+// Laguerre polynomials of src/pricers/lsm.cpp:21-25 without their common
+// factor e^{-x/2}), computed in FP64 and rounded once.
+__host__ __device__ inline void laguerre_poly(const double gamma[4], float poly[4]) {
+    poly[0] = static_cast<float>(gamma[0] + gamma[1] + gamma[2] + gamma[3]);
+    poly[1] = static_cast<float>(-gamma[1] - 2.0 * gamma[2] - 3.0 * gamma[3]);
+    poly[2] = static_cast<float>(0.5 * gamma[2] + 1.5 * gamma[3]);
+    poly[3] = static_cast<float>(-gamma[3] / 6.0);
+}
+
+#ifdef __CUDACC__
+// FP32 continuation value at S from poly (the FP32 backward pass and the
+// FP32 frozen replay both use this, so their decisions coincide).
+__device__ __forceinline__ float continuation_poly32(float s, float inv_strike, const float p[4]) {
+    const float x = s * inv_strike;
+    const float e = __expf(-0.5f * x);
+    return e * __fmaf_rn(__fmaf_rn(__fmaf_rn(p[3], x, p[2]), x, p[1]), x, p[0]);
+}
+#endif
+
 cudaError_t launch_lsm_forward(int precision, const LsmDev* c, int n_contracts,
                                const uint32_t* chunk_contract, uint32_t chunk_first, uint32_t chunk_count,
                                void* s_store, cudaStream_t stream);

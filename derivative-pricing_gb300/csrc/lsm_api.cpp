@@ -449,6 +449,7 @@ std::vector<LsmReg> policy_table(const LsmPlan& p, int monitoring_points, const 
             reg[d].gamma[b] = coefficients[4 * d + b];
             reg[d].gamma_f[b] = static_cast<float>(coefficients[4 * d + b]);
         }
+        laguerre_poly(reg[d].gamma, reg[d].poly_f);
     }
     return reg;
 }

@@ -48,16 +48,6 @@ __device__ __forceinline__ double continuation64(double s, double strike, const 
     return cont;
 }
 
-__device__ __forceinline__ float continuation32(float s, float inv_strike, const float g[4]) {
-    const float x = s * inv_strike;
-    const float e = __expf(-0.5f * x);
-    const float b0 = e;
-    const float b1 = e * (1.0f - x);
-    const float b2 = e * __fmaf_rn(0.5f * x, x, __fmaf_rn(-2.0f, x, 1.0f));
-    const float b3 = e * __fmaf_rn(__fmaf_rn(-x / 6.0f, x, 1.5f * x), x, __fmaf_rn(-3.0f, x, 1.0f));
-    return __fmaf_rn(g[3], b3, __fmaf_rn(g[2], b2, __fmaf_rn(g[1], b1, g[0] * b0)));
-}
-
 // Scenarios by volatility: {base, spot+h, spot-h} share the base's GBM step
 // constants (and so its growth factors), vol+h and vol-h have their own.
 template <int NS>
@@ -152,10 +142,10 @@ __device__ void replay32(const LsmDev& c, const FrozenDev& f, const LsmReg* __re
         const bool test = date < c.n_steps && rg[date].has == 1;
         float g[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         if (test) {
-            g[0] = rg[date].gamma_f[0];
-            g[1] = rg[date].gamma_f[1];
-            g[2] = rg[date].gamma_f[2];
-            g[3] = rg[date].gamma_f[3];
+            g[0] = rg[date].poly_f[0];
+            g[1] = rg[date].poly_f[1];
+            g[2] = rg[date].poly_f[2];
+            g[3] = rg[date].poly_f[3];
         }
         // the FP32 forward pass's log-space step (lsm.cu, lsm_forward), one
         // log path per volatility group
@@ -175,7 +165,7 @@ __device__ void replay32(const LsmDev& c, const FrozenDev& f, const LsmReg* __re
             s[q] = f.sc[q].spot_f * e[group_of(q)];
             if (test) {
                 const float ex = phi * (s[q] - strike);
-                if (ex > 0.0f && ex > continuation32(s[q], inv_k, g)) {
+                if (ex > 0.0f && ex > continuation_poly32(s[q], inv_k, g)) {
                     v[q] = ex;
                     stop[q] = date;
                     live[q] = false;
