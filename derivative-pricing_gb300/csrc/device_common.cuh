@@ -86,12 +86,12 @@ __device__ __forceinline__ uint32_t philox_word0(const PhiloxPath& pp, uint32_t 
     uint32_t c3 = pp.r0_w3;
 #pragma unroll
     for (int r = 1; r < 10; ++r) {
-        const uint64_t q0 = static_cast<uint64_t>(kPhiloxM0) * c0;
-        const uint64_t q1 = static_cast<uint64_t>(kPhiloxM1) * c2;
-        const uint32_t n0 = static_cast<uint32_t>(q1 >> 32) ^ c1 ^ k.k0[r];
-        const uint32_t n1 = static_cast<uint32_t>(q1);
-        const uint32_t n2 = static_cast<uint32_t>(q0 >> 32) ^ c3 ^ k.k1[r];
-        const uint32_t n3 = static_cast<uint32_t>(q0);
+        // high and low halves as separate 32-bit multiplies (the same bits
+        // as one 32x32->64 product)
+        const uint32_t n0 = __umulhi(kPhiloxM1, c2) ^ c1 ^ k.k0[r];
+        const uint32_t n1 = kPhiloxM1 * c2;
+        const uint32_t n2 = __umulhi(kPhiloxM0, c0) ^ c3 ^ k.k1[r];
+        const uint32_t n3 = kPhiloxM0 * c0;
         c0 = n0;
         c1 = n1;
         c2 = n2;

@@ -219,13 +219,15 @@ __global__ void __launch_bounds__(kLsmThreads)
             if ((j & 1) == 0 && j + 1 < kLsmChunk / kLsmThreads && i2 < c.path_count) {
                 const PhiloxPath pp2 = philox_path(i2, 0u, k);
                 float x = 0.0f, x2 = 0.0f;
+                float* out = S + i;  // date d's column, advanced by one column per date
                 for (int d = 0; d < c.n_steps; ++d) {
                     const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(d), k));
                     const float z2 = normal_from_bits_f32(philox_word0(pp2, static_cast<uint32_t>(d), k));
                     x = __fmaf_rn(sg, z, x + mu);
                     x2 = __fmaf_rn(sg, z2, x2 + mu);
-                    S[static_cast<uint64_t>(d) * c.path_count + i] = s0 * __expf(x);
-                    S[static_cast<uint64_t>(d) * c.path_count + i2] = s0 * __expf(x2);
+                    out[0] = s0 * __expf(x);
+                    out[kLsmThreads] = s0 * __expf(x2);
+                    out += c.path_count;
                 }
                 ++j;  // the partner path is done
                 continue;
