@@ -264,10 +264,14 @@ def bench_lsm(eng, peaks):
     r64, t64 = _timed(lambda: eng.lsm_batch(g, "fp64", "qr"))
     r32, t32 = _timed(lambda: eng.lsm_batch(g, "fp32", "qr"))
     rml, tml = _timed(lambda: eng.lsm_batch(g, "fp32", "mlp"))
+    t0 = time.perf_counter()
+    rml64 = eng.lsm_batch(g, "fp64", "mlp")  # the learned method's own FP64 arithmetic (FP64 paths)
+    tml64 = time.perf_counter() - t0
     import mcd_gpu as M
     se = r64["standard_error"]
     e32 = np.abs(r32["price"] - r64["price"]) / se
     eml = np.abs(rml["price"] - r64["price"]) / se
+    eml64 = np.abs(rml["price"] - rml64["price"]) / rml64["standard_error"]
     tree = np.array([M.crr_binomial_american(r["spot"], r["strike"], r["rate"], r["carry_yield"], r["vol"],
                                              r["time"], 2000, 1) for r in g])
     berm = np.array([M.crr_binomial_bermudan(r["spot"], r["strike"], r["rate"], r["carry_yield"], r["vol"],
@@ -295,6 +299,11 @@ def bench_lsm(eng, peaks):
             "learned_err_vs_fp64_max_se": float(eml.max()), "learned_err_vs_fp64_mean_se": float(eml.mean()),
             "learned_minus_fp64_mean_se": float(((rml["price"] - r64["price"]) / se).mean()),
             "fp32_qr_err_vs_fp64_max_se": float(e32.max()),
+            "learned_vs_learned_fp64": {
+                "note": "the learned regression on FP32 paths against the same method on FP64 paths (its own "
+                        "FP64 oracle: FP64 paths, exercise tests and cash flows), |difference| / SE; the "
+                        "errors above compare against the QR regression's price, a different policy",
+                "max_se": float(eml64.max()), "mean_se": float(eml64.mean()), "fp64_learned_s": tml64},
             "learned_fallbacks": int((rml["reserved"] != 0).sum()),
             "roofline_fp32_qr": hbm_roofline(nbytes, t32, peaks),
             "roofline_learned": hbm_roofline(nbytes, tml, peaks),

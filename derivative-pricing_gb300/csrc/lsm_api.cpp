@@ -148,7 +148,7 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
         if (!rc) rc = ctx.reserve(ctx.ext[kErr], 256, "mlp error word");
         if (!rc) rc = ctx.reserve(ctx.ext[kGroupMap], sizeof(uint32_t) * std::max<uint32_t>(p.total_groups, 1), "mlp group map");
         if (!rc) rc = ctx.reserve(ctx.ext[kGramPart], sizeof(float) * kGramPacked * kNodeSlices * n, "mlp gram partials");
-        if (!rc) rc = ctx.reserve(ctx.ext[kFeats], sizeof(float) * 64 * kNodes * n, "mlp feature tables");
+        if (!rc) rc = ctx.reserve(ctx.ext[kFeats], sizeof(float) * 64 * kNodes * p.reg_rows, "mlp feature tables");
         if (!rc) rc = ctx.reserve(ctx.ext[kETab], sizeof(float) * kNodes * n, "mlp continuation tables");
         if (!rc)
             rc = ctx.reserve(ctx.ext[kMomPart], sizeof(unsigned long long) * kMoments * kNodes *
@@ -235,7 +235,7 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
                                     ctx.ext[kStore].ptr, cs);
         for (int k = 0; k < ch.max_steps && le == cudaSuccess; ++k) {
             if (mlp)
-                le = launch_lsm_mlp_iteration(precision, k, !frozen, d_dev, ch.c_first, ch.c_end,
+                le = launch_lsm_mlp_iteration(precision, k, !frozen, d_dev, ch.c_first, ch.c_end, ch.max_steps,
                                               static_cast<const uint32_t*>(ctx.ext[kGroupMap].ptr), ch.g_first,
                                               ch.g_end, ctx.ext[kStore].ptr, static_cast<double*>(ctx.ext[kCf].ptr),
                                               static_cast<float*>(ctx.ext[kNets].ptr),

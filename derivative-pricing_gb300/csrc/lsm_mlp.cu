@@ -28,7 +28,8 @@
 //                   path by path (Z2 = H1 W2^T on the tensor core).
 //   lsm_mlp_solve   one CTA per contract: scaled ridge Cholesky solve (65 x 65,
 //                   FP32 factor, FP64-residual refinement) for the output
-//                   layer of that date.
+//                   layer of that date, then the date's continuation table
+//                   at the nodes for the next iteration's exercise test.
 //   mlp_grad_kernel / mlp_forward_kernel / umma_selftest_kernel   checks.
 //
 // Every mbarrier wait is bounded (umma.cuh); on a timeout the kernel records
@@ -665,7 +666,8 @@ __device__ void chol_solve_warp(const float* L, const float* inv_diag, const dou
 
 __global__ void __launch_bounds__(kSolveThreads)
     lsm_mlp_solve(int k, const LsmDev* __restrict__ cs, int c_first, int n_contracts, const float* __restrict__ gram_part,
-                  float* __restrict__ nets, float* __restrict__ snaps, int* __restrict__ snap_ok) {
+                  const float* __restrict__ feats, float* __restrict__ nets, float* __restrict__ snaps,
+                  int* __restrict__ snap_ok, float* __restrict__ etab) {
     __shared__ double G[kGramPacked];   // Gram matrix, packed upper triangle; standardised in place
     __shared__ float L[kM * kGramDim];  // FP32: working lower triangle; the factor, transposed, above it
     __shared__ float inv_diag[kM];
@@ -802,8 +804,29 @@ __global__ void __launch_bounds__(kSolveThreads)
         const float val = static_cast<float>(res[s]);
         snap[kW3 + s] = val;
         net[kW3 + s] = val;  // fine-tuning continues from the fit
+        inv_diag[s] = val;   // W3, then b3 (inv_diag is free now)
     }
     if (s == 0) snap_ok[c.reg_offset + d] = ok ? 1 : 0;
+    if (!ok) return;
+    // The continuation table of date d for the exercise test at d (the next
+    // backward iteration): E_i = b3 + W3 . F_i at every node, from the
+    // feature table this fit used.
+    __syncthreads();
+    const float* F = feats + (static_cast<size_t>(c.reg_offset) + d) * kNodes * 64;
+    const float b3 = inv_diag[64];
+    for (int i = s; i < kNodes; i += kSolveThreads) {
+        const float4* row = reinterpret_cast<const float4*>(F + static_cast<size_t>(i) * 64);
+        float y = b3;
+#pragma unroll 4
+        for (int q = 0; q < 16; ++q) {
+            const float4 f = row[q];
+            y = __fmaf_rn(inv_diag[4 * q], f.x, y);
+            y = __fmaf_rn(inv_diag[4 * q + 1], f.y, y);
+            y = __fmaf_rn(inv_diag[4 * q + 2], f.z, y);
+            y = __fmaf_rn(inv_diag[4 * q + 3], f.w, y);
+        }
+        etab[static_cast<size_t>(ci) * kNodes + i] = y;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -958,7 +981,8 @@ cudaError_t mlp_prepare() {
 }
 
 cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int c_first, int c_end,
-                                     const uint32_t* group_contract, uint32_t g_first, uint32_t g_end, const void* store,
+                                     int max_steps, const uint32_t* group_contract, uint32_t g_first, uint32_t g_end,
+                                     const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
                                      float* gram_part, float* feats, float* etab, unsigned long long* mom_part,
                                      const MlpConfig& cfg, Welford* final_part, uint32_t* err, cudaStream_t stream) {
@@ -988,17 +1012,24 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
         return cudaGetLastError();
     }
     int mode = kStep | kGram;  // exercise at date e, discount, regression data of date e-1
+    const bool fine_tune = cfg.steps > 0;
+    cudaError_t e = cudaSuccess;
     if (k == 0) {
         step();       // terminal cash flows, first discount
         trainer();    // learn the features on the latest date
         mode = kGram;
+        // fixed features: every date's table at once, off the per-date chain
+        if (!fine_tune) e = launch_lsm_mlp_features(k, true, max_steps, c, c_first, c_end, nets, feats, err, stream);
     }
-    cudaError_t e = launch_lsm_mlp_nodes(precision, k, mode, c, c_first, c_end, group_contract, g_first, g_end, store, cf,
-                                         nets, snaps, snap_ok, feats, etab, mom_part, gram_part, final_part, err,
-                                         stream);
+    // fine-tuned features: the table of date e-1 from the network as tuned so far
+    if (e == cudaSuccess && fine_tune) e = launch_lsm_mlp_features(k, false, max_steps, c, c_first, c_end, nets, feats, err, stream);
+    if (e == cudaSuccess)
+        e = launch_lsm_mlp_binned(precision, k, mode, c, c_first, c_end, group_contract, g_first, g_end, store, cf,
+                                  snap_ok, feats, etab, mom_part, gram_part, final_part, stream);
     if (e != cudaSuccess) return e;
-    lsm_mlp_solve<<<n_contracts, kSolveThreads, 0, stream>>>(k, c, c_first, c_end, gram_part, nets, snaps, snap_ok);
-    if (k > 0 && cfg.steps > 0) trainer();  // optional fine-tuning of the features
+    lsm_mlp_solve<<<n_contracts, kSolveThreads, 0, stream>>>(k, c, c_first, c_end, gram_part, feats, nets, snaps, snap_ok,
+                                                              etab);
+    if (k > 0 && fine_tune) trainer();  // optional fine-tuning of the features
     return cudaGetLastError();
 }
 

@@ -71,18 +71,23 @@ __host__ __device__ inline NodeGrid node_grid(const LsmDev& c, int date) {
     return g;
 }
 
-// One backward iteration of the learned regression on node tables (k as in
-// launch_lsm_mlp_iteration): lsm_mlp_nodes (continuation table of date n-k from
-// its fitted output layer, then the feature table of date n-k-1), the binned
-// path pass (exercise, discount, moments of date n-k-1), and the sliced Gram
-// matrices the solve sums.
-// Contracts [c_first, c_end) and their groups [g_first, g_end) (whole
-// contracts; launches for disjoint ranges may run concurrently).
-cudaError_t launch_lsm_mlp_nodes(int precision, int k, int mode, const LsmDev* c, int c_first, int c_end,
-                                 const uint32_t* group_contract, uint32_t g_first, uint32_t g_end, const void* store,
-                                 double* cf, const float* nets, const float* snaps, const int* snap_ok,
-                                 float* feats, float* etab, unsigned long long* mom_part, float* gram_part,
-                                 Welford* final_part, uint32_t* err, cudaStream_t stream);
+// Feature tables: the network's 64 last-layer features at the kNodes nodes of
+// a date, for contracts [c_first, c_end), at feats + (reg_offset + d) x
+// kNodes x 64 floats.  all_dates: every regression date 1 .. n-1 of each
+// contract in one launch (the features do not change from date to date when
+// they are not fine-tuned); otherwise the date n-k-1 of backward iteration k.
+cudaError_t launch_lsm_mlp_features(int k, bool all_dates, int max_steps, const LsmDev* c, int c_first, int c_end,
+                                    const float* nets, float* feats, uint32_t* err, cudaStream_t stream);
+// The binned path pass of backward iteration k (exercise at date n-k from the
+// continuation table etab, discount, moments of date n-k-1) and the sliced
+// Gram matrices of date n-k-1 that the solve sums.  Contracts [c_first,
+// c_end) and their groups [g_first, g_end) (whole contracts; launches for
+// disjoint ranges may run concurrently).
+cudaError_t launch_lsm_mlp_binned(int precision, int k, int mode, const LsmDev* c, int c_first, int c_end,
+                                  const uint32_t* group_contract, uint32_t g_first, uint32_t g_end, const void* store,
+                                  double* cf, const int* snap_ok, const float* feats, const float* etab,
+                                  unsigned long long* mom_part, float* gram_part, Welford* final_part,
+                                  cudaStream_t stream);
 
 size_t mlp_train_smem_bytes();
 size_t mlp_infer_smem_bytes();
@@ -91,11 +96,13 @@ cudaError_t mlp_prepare();  // opts the kernels into their dynamic shared memory
 // true) the Gram matrix and output-layer fit of date n-k-1 on node tables; at
 // k = 0 the features are first trained on that date.  train = false replays
 // given networks path by path (lsm_mlp_pass).  Buffers: gram_part
-// n x kNodeSlices x kGramPacked floats, feats n x kNodes x 64 floats, etab
-// n x kNodes floats, mom_part groups x kMoments x kNodes.
-// Contracts [c_first, c_end), groups [g_first, g_end), as launch_lsm_mlp_nodes.
+// n x kNodeSlices x kGramPacked floats, feats (sum of n_steps + 1) x kNodes x
+// 64 floats (rows as the snapshots), etab n x kNodes floats, mom_part groups x
+// kMoments x kNodes.
+// Contracts [c_first, c_end), groups [g_first, g_end), as launch_lsm_mlp_binned.
 cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int c_first, int c_end,
-                                     const uint32_t* group_contract, uint32_t g_first, uint32_t g_end, const void* store,
+                                     int max_steps, const uint32_t* group_contract, uint32_t g_first, uint32_t g_end,
+                                     const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
                                      float* gram_part, float* feats, float* etab, unsigned long long* mom_part,
                                      const MlpConfig& cfg, Welford* final_part, uint32_t* err, cudaStream_t stream);

@@ -9,12 +9,15 @@
 // lsm_mlp_dev.hpp) and every path uses the linear interpolation of those
 // nodes, f(u) = (1 - t) F_i + t F_{i+1} with u in bin i at fraction t:
 //
-//   lsm_mlp_nodes        one CTA per contract: the continuation table of
-//                        date e (E_i = b3 + W3 . F_e,i from the output layer
-//                        fitted at e), then the feature table F of date e-1:
-//                        layer 1 on the CUDA cores, Z2 = H1 W2^T on the tensor
-//                        core (tcgen05, BF16 operands, FP32 accumulator in
-//                        tensor memory), GELU; 128-node tiles.
+//   lsm_mlp_nodes        one CTA per (contract, 128-node tile, date): the
+//                        feature table F of a date: layer 1 on the CUDA
+//                        cores, Z2 = H1 W2^T on the tensor core (tcgen05,
+//                        BF16 operands, FP32 accumulator in tensor memory),
+//                        GELU.  With fixed features every date's table is
+//                        built in one launch after the training; with
+//                        fine-tuned features, one date per backward
+//                        iteration.  (The continuation table of a date, E_i =
+//                        b3 + W3 . F_i, is written by the solve that fits W3.)
 //   lsm_mlp_binned       one CTA per group of chunks: exercise at date e where
 //                        the interpolated continuation value is negative,
 //                        discount, cash-flow update, and for the paths in the
@@ -116,42 +119,20 @@ __device__ __forceinline__ void layer1_node(const float* w0, const float* c, flo
 }
 
 __global__ void __launch_bounds__(128)
-    lsm_mlp_nodes(int k, const LsmDev* __restrict__ cs, int c_first, int n_contracts, const float* __restrict__ nets,
-                  const float* __restrict__ snaps, const int* __restrict__ snap_ok, float* __restrict__ feats,
-                  float* __restrict__ etab, uint32_t* __restrict__ err) {
+    lsm_mlp_nodes(int k, int all_dates, const LsmDev* __restrict__ cs, int c_first, int n_contracts,
+                  const float* __restrict__ nets, float* __restrict__ feats, uint32_t* __restrict__ err) {
     __shared__ NodeSmem S;
     const int ci = c_first + static_cast<int>(blockIdx.x);
     if (ci >= n_contracts) return;
     const LsmDev c = cs[ci];
     const int n = c.n_steps;
-    const int e = n - k;
-    if (e < 1) return;
-    const int d = e - 1;
+    // the date: every regression date 1 .. n-1 (blockIdx.z + 1), or the one
+    // of backward iteration k
+    const int d = all_dates ? static_cast<int>(blockIdx.z) + 1 : n - k - 1;
+    if (d < 1 || d > n - 1) return;
+    const int tile = static_cast<int>(blockIdx.y);
     const int s = threadIdx.x, warp = s >> 5;
-    float* F = feats + static_cast<size_t>(ci) * kNodes * 64;
-    // 1. continuation table of date e, from the features fitted there (still in F)
-    if (k > 0 && e <= n - 1 && snap_ok[c.reg_offset + e] == 1) {
-        const float* snap = snaps + (static_cast<size_t>(c.reg_offset) + e) * kParamStride;
-        if (s < 64) S.w3[s] = snap[kW3 + s];
-        __syncthreads();
-        const float b3 = snap[kB3];
-        for (int i = s; i < kNodes; i += 128) {
-            const float4* row = reinterpret_cast<const float4*>(F + static_cast<size_t>(i) * 64);
-            float y = b3;
-#pragma unroll 4
-            for (int q = 0; q < 16; ++q) {
-                const float4 f = row[q];
-                y = __fmaf_rn(S.w3[4 * q], f.x, y);
-                y = __fmaf_rn(S.w3[4 * q + 1], f.y, y);
-                y = __fmaf_rn(S.w3[4 * q + 2], f.z, y);
-                y = __fmaf_rn(S.w3[4 * q + 3], f.w, y);
-            }
-            etab[static_cast<size_t>(ci) * kNodes + i] = y;
-        }
-    }
-    if (d < 1) return;
-    __syncthreads();  // every read of the previous table is done before it is overwritten
-    // 2. feature table of date d = e-1 with the current network
+    float* F = feats + (static_cast<size_t>(c.reg_offset) + d) * kNodes * 64;
     const float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
     const float x1 = static_cast<float>(n - d) / static_cast<float>(n);
     if (s < 64) {
@@ -175,25 +156,22 @@ __global__ void __launch_bounds__(128)
     umma::fence_after_sync();
     const uint32_t tm = S.tmem_base;
     const NodeGrid g = S.grid;
-    uint32_t phase = 0;
-    bool ok = true;
-    for (int tile = 0; tile < kNodes / 128 && ok; ++tile) {
-        const int i = tile * 128 + s;
-        const float u = __fmaf_rn(static_cast<float>(i), g.h, g.lo);
-        const float x0 = 4.0f * (expf(u) - 1.0f);
-        layer1_node(S.w0, S.c1, x0, S.h1, s);
-        umma::fence_smem_to_async();
-        umma::fence_before_sync();
-        __syncthreads();
-        if (s == 0) {
-            umma::fence_after_sync();
-            for (int kk = 0; kk < 4; ++kk)
-                umma::mma_bf16(tm, desc(S.h1, 1024, kk), desc(S.w2, 1024, kk), kNodeIdesc, kk > 0);
-            umma::mma_commit(&S.mbar);
-        }
-        ok = __syncthreads_and(umma::mbar_wait(&S.mbar, phase, err, 41));
-        if (!ok) break;
-        phase ^= 1u;
+    // one 128-node tile: layer 1 on the CUDA cores, Z2 = H1 W2^T on the tensor core, GELU
+    const int i = tile * 128 + s;
+    const float u = __fmaf_rn(static_cast<float>(i), g.h, g.lo);
+    const float x0 = 4.0f * (expf(u) - 1.0f);
+    layer1_node(S.w0, S.c1, x0, S.h1, s);
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    if (s == 0) {
+        umma::fence_after_sync();
+        for (int kk = 0; kk < 4; ++kk)
+            umma::mma_bf16(tm, desc(S.h1, 1024, kk), desc(S.w2, 1024, kk), kNodeIdesc, kk > 0);
+        umma::mma_commit(&S.mbar);
+    }
+    const bool ok = __syncthreads_and(umma::mbar_wait(&S.mbar, 0u, err, 41));
+    if (ok) {
         umma::fence_after_sync();
         float4* dst = reinterpret_cast<float4*>(F + static_cast<size_t>(i) * 64);
         for (int cc = 0; cc < 4; ++cc) {
@@ -210,10 +188,9 @@ __global__ void __launch_bounds__(128)
                 dst[(cc * 16 + q) / 4] = v;
             }
         }
-        umma::fence_before_sync();
-        __syncthreads();  // h1 and the accumulator are reused by the next tile
+    } else {
+        umma::mbar_wait(&S.mbar, 0u, err, 42);  // the MMA that timed out, once more (bounded)
     }
-    if (!ok) umma::mbar_wait(&S.mbar, phase, err, 42);  // the MMA that timed out, once more (bounded)
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tm, 64);
@@ -223,6 +200,25 @@ __global__ void __launch_bounds__(128)
 // Binned path pass.
 // ---------------------------------------------------------------------------
 constexpr int kBinThreads = 256;  // five CTAs per SM (48 registers): latency-bound on the shared-memory atomics
+static_assert(kNodes == 2 * kBinThreads, "two bins per thread when the moments are folded");
+
+// The moments are accumulated with 32-bit shared-memory atomics (the native
+// ones; a 64-bit shared atomic add is several times slower) in limbs of at
+// most 16 bits per path, over epochs of at most kEpochChunks chunks, so no
+// limb sum can exceed 2^32: with tq in [0, 2^16], yb = yq + 2^24 in [0, 2^25]
+// and P = tq yb in [0, 2^41] the limbs are
+//   0: 1            1: tq
+//   2: tq^2 mod 2^16    3: tq^2 / 2^16     (tq^2 <= 2^32)
+//   4: yb mod 2^16      5: yb / 2^16
+//   6: P mod 2^16       7: P / 2^16 mod 2^16   8: P / 2^32
+// After each epoch the limbs are recombined exactly into the four 64-bit
+// moments (n 2^40 + sum tq, sum tq^2, sum yq, sum tq yq, the last two modulo
+// 2^64 as two's complement), which therefore equal the sums of the per-path
+// 64-bit terms bit for bit.
+constexpr int kLimbs = 9;
+constexpr uint32_t kEpochChunks = 32;
+static_assert(static_cast<uint64_t>(kEpochChunks) * kLsmChunk * 65536ull < (1ull << 32),
+              "limb sums of one epoch fit 32 bits");
 
 template <int PREC>
 __global__ void __launch_bounds__(kBinThreads, 5)
@@ -231,7 +227,8 @@ __global__ void __launch_bounds__(kBinThreads, 5)
                    const int* __restrict__ snap_ok, const float* __restrict__ etab,
                    unsigned long long* __restrict__ mom_part, Welford* __restrict__ final_part) {
     __shared__ float tab[kNodes];                              // continuation table of date e
-    __shared__ unsigned long long mom[kMoments][kNodes];       // moments of date e-1, bin by bin
+    __shared__ uint32_t lim[kLimbs][kNodes];                   // limbs of the moments of date e-1, bin by bin
+    __shared__ unsigned long long mom[kMoments][kNodes];       // the moments, epochs folded so far
     __shared__ Welford swf[kBinThreads / 32];
     __shared__ Sum64 s64[kBinThreads / 32];
     __shared__ NodeGrid s_grid[2];                             // dates e and e-1
@@ -265,8 +262,10 @@ __global__ void __launch_bounds__(kBinThreads, 5)
     }
     if (exercise)
         for (int i = s; i < kNodes; i += kBinThreads) tab[i] = etab[static_cast<size_t>(ci) * kNodes + i];
-    if (gram)
+    if (gram) {
+        for (int i = s; i < kLimbs * kNodes; i += kBinThreads) (&lim[0][0])[i] = 0u;
         for (int i = s; i < kMoments * kNodes; i += kBinThreads) (&mom[0][0])[i] = 0ull;
+    }
     __syncthreads();
     const NodeGrid ge = s_grid[0], gd = s_grid[1];
     const float yq_scale = static_cast<float>(kYScale) / gd.y_bound;
@@ -275,8 +274,30 @@ __global__ void __launch_bounds__(kBinThreads, 5)
     const uint32_t chunk1 = min(c.n_chunks, chunk0 + c.group_chunks);
     Welford w{0ull, 0.0, 0.0};
     Sum32 fin{0u, 0.0f, 0.0f, 0.0f, 0.0f};  // FP32 path: the last date's payoffs
+    // the limbs of the epoch just ended, recombined into mom and cleared
+    // (thread s folds bins s and s + kBinThreads)
+    auto fold_epoch = [&]() {
+        __syncthreads();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int b = s + h * kBinThreads;
+            unsigned long long l[kLimbs];
+#pragma unroll
+            for (int q = 0; q < kLimbs; ++q) {
+                l[q] = lim[q][b];
+                lim[q][b] = 0u;
+            }
+            const unsigned long long st = l[1];
+            mom[0][b] += (l[0] << kCountShift) + st;
+            mom[1][b] += l[2] + (l[3] << 16);
+            mom[2][b] += l[4] + (l[5] << 16) - (l[0] << 24);
+            mom[3][b] += l[6] + (l[7] << 16) + (l[8] << 32) - (st << 24);
+        }
+        __syncthreads();
+    };
     constexpr int kPer = kLsmChunk / kBinThreads;  // paths per thread and chunk
     for (uint32_t ch = chunk0; ch < chunk1; ++ch) {
+        if (gram && ch > chunk0 && (ch - chunk0) % kEpochChunks == 0) fold_epoch();
         // every path load of this thread's kPer paths first (independent, in flight together)
         T vv[kPer], se[kPer], sd[kPer];
         bool live[kPer];
@@ -334,10 +355,19 @@ __global__ void __launch_bounds__(kBinThreads, 5)
                     const int tq = __float2int_rn(t * static_cast<float>(kTScale));
                     const int yq = min(max(__float2int_rn(fminf(fmaxf(y * yq_scale, -16777216.0f), 16777216.0f)),
                                            -16777216), 16777216);
-                    atomicAdd(&mom[0][b], (1ull << kCountShift) + static_cast<unsigned long long>(tq));
-                    atomicAdd(&mom[1][b], static_cast<unsigned long long>(static_cast<long long>(tq) * tq));
-                    atomicAdd(&mom[2][b], static_cast<unsigned long long>(static_cast<long long>(yq)));
-                    atomicAdd(&mom[3][b], static_cast<unsigned long long>(static_cast<long long>(tq) * yq));
+                    const uint32_t ut = static_cast<uint32_t>(tq);           // [0, 2^16]
+                    const uint32_t yb = static_cast<uint32_t>(yq + 16777216);  // [0, 2^25]
+                    const unsigned long long tt = static_cast<unsigned long long>(ut) * ut;
+                    const unsigned long long pp = static_cast<unsigned long long>(ut) * yb;
+                    atomicAdd(&lim[0][b], 1u);
+                    atomicAdd(&lim[1][b], ut);
+                    atomicAdd(&lim[2][b], static_cast<uint32_t>(tt) & 0xFFFFu);
+                    atomicAdd(&lim[3][b], static_cast<uint32_t>(tt >> 16));
+                    atomicAdd(&lim[4][b], yb & 0xFFFFu);
+                    atomicAdd(&lim[5][b], yb >> 16);
+                    atomicAdd(&lim[6][b], static_cast<uint32_t>(pp) & 0xFFFFu);
+                    atomicAdd(&lim[7][b], static_cast<uint32_t>(pp >> 16) & 0xFFFFu);
+                    atomicAdd(&lim[8][b], static_cast<uint32_t>(pp >> 32));
                 }
             }
         }
@@ -363,7 +393,7 @@ __global__ void __launch_bounds__(kBinThreads, 5)
         }
     }
     if (gram) {
-        __syncthreads();
+        fold_epoch();
         unsigned long long* out = mom_part + static_cast<size_t>(g) * kMoments * kNodes;
         for (int i = s; i < kMoments * kNodes; i += kBinThreads) out[i] = (&mom[0][0])[i];
     }
@@ -425,7 +455,7 @@ __global__ void __launch_bounds__(kGramThreads)
         for (int q = 0; q < 5; ++q) wgt[q][s] = w[q];
     }
     // feature rows row0 .. row0 + kBinsPerSlice, with the constant 1 in column 64
-    const float* src = feats + static_cast<size_t>(ci) * kNodes * 64;
+    const float* src = feats + (static_cast<size_t>(c.reg_offset) + d) * kNodes * 64;
     for (int idx = s; idx < (kBinsPerSlice + 1) * (kFStride / 4); idx += kGramThreads) {
         const int r = idx / (kFStride / 4), q4 = idx % (kFStride / 4);
         float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -497,16 +527,24 @@ __global__ void __launch_bounds__(kGramThreads)
 
 }  // namespace
 
-cudaError_t launch_lsm_mlp_nodes(int precision, int k, int mode, const LsmDev* c, int c_first, int c_end,
-                                 const uint32_t* group_contract, uint32_t g_first, uint32_t g_end, const void* store,
-                                 double* cf, const float* nets, const float* snaps, const int* snap_ok,
-                                 float* feats, float* etab, unsigned long long* mom_part, float* gram_part,
-                                 Welford* final_part, uint32_t* err, cudaStream_t stream) {
+cudaError_t launch_lsm_mlp_features(int k, bool all_dates, int max_steps, const LsmDev* c, int c_first, int c_end,
+                                    const float* nets, float* feats, uint32_t* err, cudaStream_t stream) {
+    cudaGetLastError();
+    if (c_end <= c_first || (all_dates && max_steps < 2)) return cudaSuccess;
+    const dim3 grid(static_cast<unsigned>(c_end - c_first), kNodes / 128, all_dates ? static_cast<unsigned>(max_steps - 1) : 1u);
+    lsm_mlp_nodes<<<grid, 128, 0, stream>>>(k, all_dates ? 1 : 0, c, c_first, c_end, nets, feats, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lsm_mlp_binned(int precision, int k, int mode, const LsmDev* c, int c_first, int c_end,
+                                  const uint32_t* group_contract, uint32_t g_first, uint32_t g_end, const void* store,
+                                  double* cf, const int* snap_ok, const float* feats, const float* etab,
+                                  unsigned long long* mom_part, float* gram_part, Welford* final_part,
+                                  cudaStream_t stream) {
     cudaGetLastError();
     if (c_end <= c_first || g_end <= g_first) return cudaSuccess;
     const int n_contracts = c_end - c_first;
     const uint32_t n_groups = g_end - g_first;
-    lsm_mlp_nodes<<<n_contracts, 128, 0, stream>>>(k, c, c_first, c_end, nets, snaps, snap_ok, feats, etab, err);
     if (precision == 0)
         lsm_mlp_binned<0><<<n_groups, kBinThreads, 0, stream>>>(k, mode, c, group_contract, g_first, g_end, store, cf,
                                                                      snap_ok, etab, mom_part, final_part);
