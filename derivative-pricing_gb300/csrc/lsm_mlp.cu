@@ -597,233 +597,348 @@ __global__ void __launch_bounds__(128)
 // only positive semi-definite to a small fraction of its diagonal.  The
 // regressors are therefore scaled to unit diagonal and a ridge of kRidge is
 // added in those units; a pivot that still falls below half the ridge drops
-// its regressor (coefficient 0) instead of failing the date.  The partials of
-// the bin slices (lsm_mlp_gram_slices) are summed in FP64 in order; FP64
-// is slow on this part, so the 65 x 65 Cholesky factor is
-// computed in FP32 (every thread keeps its share of the triangle in
-// registers; one barrier per column), and two steps of iterative refinement
-// with FP64 residuals bring the solution to FP64 accuracy for the
-// ridge-bounded condition number.
+// its regressor (coefficient 0) instead of failing the date.
+//
+// FP64 is slow on this part, so the solve works in FP32 and in pairs of FP32
+// values (hi + lo, about 48 bits):
+//   1. the bin slices' partials are summed in order into pairs (error-free
+//      two-sums) and standardised as pairs;
+//   2. one sweep of 65 steps, one barrier each, factors the FP32 matrix
+//      A = L L^T (right-looking Cholesky) and at the same time applies the
+//      same row operations to the identity, which leaves W = L^-1: both live
+//      in registers as 4 x 4 blocks of their lower triangles, one block per
+//      thread (153 + 153 blocks of the 68 x 68 padded matrices), and each
+//      step broadcasts the pivot column of A and the pivot row of W through
+//      shared memory;
+//   3. x = W^T W b, then two steps of iterative refinement with residuals
+//      b - A x in pairs (x kept as a pair): two matrix-vector products per
+//      solve instead of two triangular substitutions of 65 dependent steps.
 //
 // snap_ok of the date: 1 = fitted, 2 = fewer than 4 in-the-money paths (no
 // exercise at this date, as src/pricers/lsm.cpp does), 0 = failed.
 // ---------------------------------------------------------------------------
-constexpr double kRidge = 1e-3;
-constexpr int kSolveThreads = 256;
-constexpr int kM = kGramDim - 1;                                      // 65 regressors (64 features + bias)
-constexpr int kTri = kM * (kM + 1) / 2;                               // lower triangle of the 65 x 65 system
+constexpr float kRidge = 1e-3f;
+constexpr int kM = kGramDim - 1;           // 65 regressors (64 features + bias)
+constexpr int kNB = 17;                    // 4 x 4 blocks per side
+constexpr int kPad = 4 * kNB;              // 68: the system padded with identity rows
+constexpr int kTriBlocks = kNB * (kNB + 1) / 2;  // 153 blocks of a lower triangle
+constexpr int kWBase = 160;                // first thread of the W role (a warp boundary)
+constexpr int kSolveThreads = 320;         // A role 0..152, W role 160..312
+static_assert(kTriBlocks <= kWBase && kWBase + kTriBlocks <= kSolveThreads && kWBase % 32 == 0, "solve roles");
+static_assert(4 * kM <= kSolveThreads && kPad <= kSolveThreads, "four residual threads per row");
 
 __device__ __forceinline__ int packed_index(int r, int q) {  // r <= q
     return r * kGramDim - r * (r - 1) / 2 + (q - r);
 }
+__device__ __forceinline__ int sym_index(int r, int q) { return r <= q ? packed_index(r, q) : packed_index(q, r); }
 
-// Pivots 32 QI .. 32 QI + 31 of the forward (L z = b) or backward (L^T x = z)
-// substitution: the pivot's owner keeps it in v[QI], known at compile time, so
-// the factor loads of a step do not wait for the previous step.
-template <int QI, bool kForward>
-__device__ __forceinline__ void subst_block(const float* L, const float* inv_diag, float (&v)[3], int lane) {
-    constexpr int kBegin = 32 * QI, kEnd = (32 * QI + 32 < kM) ? 32 * QI + 32 : kM;
-#pragma unroll 4
-    for (int n = 0; n < kEnd - kBegin; ++n) {
-        const int i = kForward ? kBegin + n : kEnd - 1 - n;
-        const float pv = __shfl_sync(0xffffffffu, v[QI] * inv_diag[i], i & 31);
+// pairs of floats: s + e = a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {  // |a| >= |b|
+    s = a + b;
+    e = b - (s - a);
+}
+// (h, l) + (bh, bl), renormalised
+__device__ __forceinline__ void pair_add(float& h, float& l, float bh, float bl) {
+    float s, e;
+    two_sum(h, bh, s, e);
+    e += l + bl;
+    fast_two_sum(s, e, h, l);
+}
+// (h, l) * f for a float f
+__device__ __forceinline__ void pair_scale(float h, float l, float f, float& oh, float& ol) {
+    const float p = h * f;
+    const float e = __fmaf_rn(h, f, -p) + l * f;
+    fast_two_sum(p, e, oh, ol);
+}
+
+// Arrays read or written as float4 first: each is a multiple of 16 bytes.
+struct __align__(16) SolveSmem {
+    float colA[2][kPad];                     // pivot column of A, double-buffered by step
+    float rowW[2][kPad];                     // pivot row of W, double-buffered by step
+    float part[kNB][kPad];                   // partial sums of the matrix-vector products
+    float vb[kPad], vr[kPad];                // right-hand side (hi), residual
+    float vz[kPad], vx[kPad];                // W v, W^T W v
+    float xh[kPad], xl[kPad];                // the solution, a pair
+    float bl[kPad];                          // low part of the right-hand side
+    float sc[kPad];                          // scale of each regressor (1 / sqrt of its diagonal)
+    float coef[kPad];                        // fitted W3, b3
+    int drop[kPad];
+    float gh[kGramPacked], gl[kGramPacked];  // the Gram matrix (then standardised), pairs; column 65 = rhs
+    int bad;
+    int few;
+};
+static_assert(kPad % 4 == 0, "float4 rows");
+
+// Lower-triangular block t (row-major over the triangle) -> block row and column.
+__device__ __forceinline__ void tri_block(int t, int& R, int& C) {
+    R = 0;
+    while ((R + 1) * (R + 2) / 2 <= t) ++R;
+    C = t - R * (R + 1) / 2;
+}
+
+// Step j = 4 J + JJ of the sweep (see above).  The A role owns block (R, C) of
+// the matrix being factored, the W role block (R, C) of L^-1 in the making;
+// m is the owned block.  Owners of the next pivot column (A) and row (W)
+// publish them into the other buffer.
+template <int JJ>
+__device__ __forceinline__ void chol_step(SolveSmem& S, int J, bool role_a, bool role_w, int R, int C, float (&m)[4][4],
+                                          int s) {
+    const int j = 4 * J + JJ;
+    const int buf = j & 1;
+    __syncthreads();
+    const float dj = S.colA[buf][j];
+    const bool drop = !(dj >= 0.5f * kRidge);
+    const float inv = drop ? 0.0f : rsqrtf(dj);
+    if (s == 0) S.drop[j] = drop ? 1 : 0;
+    if (role_a && C >= J) {
+        const float4 xr = *reinterpret_cast<const float4*>(&S.colA[buf][4 * R]);
+        const float4 xc = *reinterpret_cast<const float4*>(&S.colA[buf][4 * C]);
+        const float lr[4] = {xr.x * inv, xr.y * inv, xr.z * inv, xr.w * inv};
+        const float lc[4] = {xc.x * inv, xc.y * inv, xc.z * inv, xc.w * inv};
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            const int r = lane + 32 * q;
-            if (r == i) v[q] = pv;
-            else if (kForward ? (r > i && r < kM) : (r < i))
-                v[q] = __fmaf_rn(-(kForward ? L[i * kGramDim + r] : L[r * kGramDim + i]), pv, v[q]);
-        }
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (C > J || c > JJ) m[i][c] = __fmaf_rn(-lr[i], lc[c], m[i][c]);
+    }
+    if (role_w && R >= J && C <= J) {
+        const float4 xr = *reinterpret_cast<const float4*>(&S.colA[buf][4 * R]);
+        const float4 xw = *reinterpret_cast<const float4*>(&S.rowW[buf][4 * C]);
+        const float lr[4] = {xr.x * inv, xr.y * inv, xr.z * inv, xr.w * inv};
+        const float wr[4] = {xw.x * inv, xw.y * inv, xw.z * inv, xw.w * inv};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (R > J || i > JJ) m[i][c] = __fmaf_rn(-lr[i], wr[c], m[i][c]);
+                else if (i == JJ) m[i][c] = wr[c];
+            }
+    }
+    // publish the next pivot column of A and row of W (every owner, updated or not)
+    constexpr int kNext = (JJ + 1) & 3;
+    const int bnext = JJ == 3 ? J + 1 : J;
+    if (j + 1 < kM) {
+        if (role_a && C == bnext)
+            *reinterpret_cast<float4*>(&S.colA[buf ^ 1][4 * R]) = make_float4(m[0][kNext], m[1][kNext], m[2][kNext], m[3][kNext]);
+        if (role_w && R == bnext)
+            *reinterpret_cast<float4*>(&S.rowW[buf ^ 1][4 * C]) = make_float4(m[kNext][0], m[kNext][1], m[kNext][2], m[kNext][3]);
     }
 }
 
-// x = L^-T L^-1 b for the FP32 factor L, stored transposed in the upper
-// triangle of W (L[r][i] at W[i * kGramDim + r], r > i) with the reciprocal
-// diagonal in inv_diag, by one warp: lane l keeps entries l, l+32 and l+64 of
-// the vector in registers (z, then x, replace b in place) and each pivot value
-// is broadcast by a shuffle.  b is rhs rounded to FP32; x is added to acc in
-// FP64.  Dropped regressors give 0 (their inv_diag is 0).
-__device__ void chol_solve_warp(const float* L, const float* inv_diag, const double* rhs, double* acc, int lane) {
-    static_assert((kM + 31) / 32 == 3, "three entries per lane");
-    float v[3];
+// out = W v (transpose = false) or W^T v (transpose = true), W in the W role's
+// registers; the partial sums are added in a fixed order.
+__device__ __forceinline__ void w_matvec(SolveSmem& S, bool role_w, int R, int C, const float (&m)[4][4], const float* v,
+                                         float* out, bool transpose, int s) {
+    if (role_w) {
+        if (!transpose) {
+            const float4 x = *reinterpret_cast<const float4*>(&v[4 * C]);
+            float p[4];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        const int r = lane + 32 * q;
-        v[q] = r < kM ? static_cast<float>(rhs[r]) : 0.0f;
-    }
-    subst_block<0, true>(L, inv_diag, v, lane);
-    subst_block<1, true>(L, inv_diag, v, lane);
-    subst_block<2, true>(L, inv_diag, v, lane);
-    subst_block<2, false>(L, inv_diag, v, lane);
-    subst_block<1, false>(L, inv_diag, v, lane);
-    subst_block<0, false>(L, inv_diag, v, lane);
+            for (int i = 0; i < 4; ++i)
+                p[i] = __fmaf_rn(m[i][3], x.w, __fmaf_rn(m[i][2], x.z, __fmaf_rn(m[i][1], x.y, m[i][0] * x.x)));
+            *reinterpret_cast<float4*>(&S.part[C][4 * R]) = make_float4(p[0], p[1], p[2], p[3]);
+        } else {
+            const float4 x = *reinterpret_cast<const float4*>(&v[4 * R]);
+            float p[4];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        const int r = lane + 32 * q;
-        if (r < kM) acc[r] += static_cast<double>(v[q]);
+            for (int c = 0; c < 4; ++c)
+                p[c] = __fmaf_rn(m[3][c], x.w, __fmaf_rn(m[2][c], x.z, __fmaf_rn(m[1][c], x.y, m[0][c] * x.x)));
+            *reinterpret_cast<float4*>(&S.part[R][4 * C]) = make_float4(p[0], p[1], p[2], p[3]);
+        }
     }
+    __syncthreads();
+    if (s < kPad) {
+        const int blk = s >> 2;
+        float acc = 0.0f;
+        if (!transpose) {
+            for (int c = 0; c <= blk; ++c) acc += S.part[c][s];
+        } else {
+            for (int r = blk; r < kNB; ++r) acc += S.part[r][s];
+        }
+        out[s] = acc;
+    }
+    __syncthreads();
 }
 
 __global__ void __launch_bounds__(kSolveThreads)
     lsm_mlp_solve(int k, const LsmDev* __restrict__ cs, int c_first, int n_contracts, const float* __restrict__ gram_part,
                   const float* __restrict__ feats, float* __restrict__ nets, float* __restrict__ snaps,
                   int* __restrict__ snap_ok, float* __restrict__ etab) {
-    __shared__ double G[kGramPacked];   // Gram matrix, packed upper triangle; standardised in place
-    __shared__ float L[kM * kGramDim];  // FP32: working lower triangle; the factor, transposed, above it
-    __shared__ float inv_diag[kM];
-    __shared__ double sc[kM], xs[kM], res[kM];
-    __shared__ int bad;
+    __shared__ SolveSmem S;
     const int ci = c_first + static_cast<int>(blockIdx.x);
     if (ci >= n_contracts) return;
     const LsmDev c = cs[ci];
     const int d = c.n_steps - k - 1;
     if (d < 1) return;
-    const int s = threadIdx.x, lane = s & 31, warp = s >> 5;
-    {  // the bin slices' partials, summed in order (all loads issued first)
-        constexpr int kIters = (kGramPacked + kSolveThreads - 1) / kSolveThreads;
+    const int s = threadIdx.x;
+    // 1. the bin slices' partials, summed in order into pairs
+    {
         const float* part = gram_part + static_cast<size_t>(ci) * kNodeSlices * kGramPacked;
-        float pv[kIters][kNodeSlices];
+        for (int p = s; p < kGramPacked; p += kSolveThreads) {
+            float v[kNodeSlices];
 #pragma unroll
-        for (int u = 0; u < kIters; ++u) {
-            const int idx = s + kSolveThreads * u;
+            for (int sl = 0; sl < kNodeSlices; ++sl) v[sl] = part[static_cast<size_t>(sl) * kGramPacked + p];
+            float h = v[0], l = 0.0f;
 #pragma unroll
-            for (int sl = 0; sl < kNodeSlices; ++sl)
-                pv[u][sl] = idx < kGramPacked ? part[static_cast<size_t>(sl) * kGramPacked + idx] : 0.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < kIters; ++u) {
-            const int idx = s + kSolveThreads * u;
-            if (idx < kGramPacked) {
-                double v = 0.0;
-#pragma unroll
-                for (int sl = 0; sl < kNodeSlices; ++sl) v += static_cast<double>(pv[u][sl]);
-                G[idx] = v;
+            for (int sl = 1; sl < kNodeSlices; ++sl) {
+                float e;
+                two_sum(h, v[sl], h, e);
+                l += e;
             }
+            fast_two_sum(h, l, S.gh[p], S.gl[p]);
         }
     }
-    if (s == 0) bad = 0;
+    if (s == 0) S.bad = 0;
     __syncthreads();
-    const double count = G[packed_index(64, 64)];
-    if (!(count >= 4.0)) {
+    if (s == 0) S.few = !(S.gh[packed_index(64, 64)] + S.gl[packed_index(64, 64)] >= 4.0f) ? 1 : 0;
+    if (s < kPad) {
+        const float a = s < kM ? S.gh[packed_index(s, s)] : 0.0f;
+        S.sc[s] = s < kM ? (a > 0.0f ? rsqrtf(a) : 0.0f) : (s == kM ? 1.0f : 0.0f);  // the rhs column keeps scale 1
+    }
+    __syncthreads();
+    if (S.few) {
         if (s == 0) snap_ok[c.reg_offset + d] = 2;
         return;
     }
-    if (s < kM) {
-        const double a = G[packed_index(s, s)];
-        sc[s] = a > 0.0 ? 1.0 / sqrt(a) : 0.0;  // a feature that is zero on every path gets coefficient 0
+    // standardised pairs G_rq sc_r sc_q, plus the ridge on the diagonal (whose
+    // standardised value is 1 to the rounding of sc, or 0 for a regressor that
+    // is zero on every path)
+    const float ridge_lo = static_cast<float>(1e-3 - static_cast<double>(kRidge));
+    for (int e = s; e < kGramDim * kGramDim; e += kSolveThreads) {
+        const int r = e / kGramDim, q = e - r * kGramDim;
+        if (r > q) continue;
+        const int p = packed_index(r, q);
+        float h, l, th, tl;
+        pair_scale(S.gh[p], S.gl[p], S.sc[r], th, tl);
+        pair_scale(th, tl, S.sc[q], h, l);
+        if (r == q && r < kM) pair_add(h, l, kRidge, ridge_lo);
+        S.gh[p] = h;
+        S.gl[p] = l;
     }
     __syncthreads();
-    // The lower triangle, standardised, as FP32 in L; the packed FP64 copy is
-    // standardised too (for the residuals).
-    for (int e = s; e < kTri; e += kSolveThreads) {
-        int r = static_cast<int>((sqrtf(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
-        while (r * (r + 1) / 2 > e) --r;
-        while ((r + 1) * (r + 2) / 2 <= e) ++r;
-        const int q = e - r * (r + 1) / 2;
-        const int pi = packed_index(q, r);
-        double v = G[pi] * sc[r] * sc[q];
-        if (q == r) v = (sc[r] > 0.0 ? 1.0 : 0.0) + kRidge;
-        G[pi] = v;
-        L[r * kGramDim + q] = static_cast<float>(v);
+    // 2. roles and blocks; the right-hand side; the first pivot column and row
+    const bool role_a = s < kTriBlocks;
+    const bool role_w = s >= kWBase && s < kWBase + kTriBlocks;
+    int R = 0, C = 0;
+    tri_block(role_a ? s : (role_w ? s - kWBase : 0), R, C);
+    float m[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int r = 4 * R + i, cc = 4 * C + q;
+            float v = 0.0f;
+            if (role_a) v = (r < kM && cc < kM) ? S.gh[sym_index(r, cc)] : (r == cc ? 1.0f : 0.0f);
+            else if (role_w) v = r == cc ? 1.0f : 0.0f;
+            m[i][q] = v;
+        }
+    if (s < kPad) {
+        S.vb[s] = s < kM ? S.gh[packed_index(s, kM)] : 0.0f;
+        S.bl[s] = s < kM ? S.gl[packed_index(s, kM)] : 0.0f;
     }
-    if (s < kM) G[packed_index(s, 65)] *= sc[s];  // right-hand side
-    // Right-looking Cholesky in FP32, one barrier per column.  At column j
-    // thread t updates column q = j + 1 + (t mod 64) on rows r = q + t / 64,
-    // r + 4, ... with column j of the reduced matrix; its loads are all issued
-    // before its stores (no thread reads what another writes in the step), and
-    // row j of the upper triangle receives the factor's column j.
-    constexpr int kRowGroups = kSolveThreads / 64;
-    constexpr int kMaxRows = (kM + kRowGroups - 1) / kRowGroups;
-    for (int j = 0; j < kM; ++j) {
-        __syncthreads();
-        const float dj = L[j * kGramDim + j];
-        const bool drop = !(dj >= static_cast<float>(0.5 * kRidge));
-        const float inv = drop ? 0.0f : rsqrtf(dj);
-        const int q = j + 1 + (s & 63);
-        if (q < kM) {
-            const float lq = L[q * kGramDim + j] * inv;
-            float lr[kMaxRows], cur[kMaxRows];
-#pragma unroll
-            for (int m = 0; m < kMaxRows; ++m) {
-                const int r = q + (s >> 6) + kRowGroups * m;
-                lr[m] = r < kM ? L[r * kGramDim + j] : 0.0f;
-                cur[m] = r < kM ? L[r * kGramDim + q] : 0.0f;
-            }
-#pragma unroll
-            for (int m = 0; m < kMaxRows; ++m) {
-                const int r = q + (s >> 6) + kRowGroups * m;
-                if (r < kM) L[r * kGramDim + q] = __fmaf_rn(-(lr[m] * inv), lq, cur[m]);
+    if (role_a && C == 0) *reinterpret_cast<float4*>(&S.colA[0][4 * R]) = make_float4(m[0][0], m[1][0], m[2][0], m[3][0]);
+    if (role_w && R == 0) *reinterpret_cast<float4*>(&S.rowW[0][4 * C]) = make_float4(m[0][0], m[0][1], m[0][2], m[0][3]);
+    // the sweep: Cholesky of A and W = L^-1, 65 steps
+    for (int J = 0; J < kNB - 1; ++J) {
+        chol_step<0>(S, J, role_a, role_w, R, C, m, s);
+        chol_step<1>(S, J, role_a, role_w, R, C, m, s);
+        chol_step<2>(S, J, role_a, role_w, R, C, m, s);
+        chol_step<3>(S, J, role_a, role_w, R, C, m, s);
+    }
+    chol_step<0>(S, kNB - 1, role_a, role_w, R, C, m, s);  // pivot 64
+    __syncthreads();
+    // 3. x = W^T W b, then two refinement steps with residuals in pairs
+    w_matvec(S, role_w, R, C, m, S.vb, S.vz, false, s);
+    w_matvec(S, role_w, R, C, m, S.vz, S.vx, true, s);
+    if (s < kPad) {
+        S.xh[s] = s < kM ? S.vx[s] : 0.0f;
+        S.xl[s] = 0.0f;
+    }
+    __syncthreads();
+    for (int it = 0; it < 2; ++it) {
+        // residual of row i = s / 4 from 4 threads (columns j = s mod 4 + 4 t), added in a fixed order
+        const int i = s >> 2, sub = s & 3;
+        float rh = 0.0f, rl = 0.0f;
+        if (i < kM) {
+            for (int jj = sub; jj < kM; jj += 4) {
+                const int p = sym_index(i, jj);
+                const float ah = S.gh[p], al = S.gl[p], xh = S.xh[jj], xl = S.xl[jj];
+                const float ph = ah * xh;
+                const float pe = __fmaf_rn(ah, xh, -ph) + (ah * xl + al * xh);
+                pair_add(rh, rl, ph, pe);
             }
         }
-        if (s > j && s < kM) L[j * kGramDim + s] = L[s * kGramDim + j] * inv;
-        if (s == 0) inv_diag[j] = inv;  // 1 / L[j][j], 0 when the regressor is dropped
-    }
-    __syncthreads();
-    // solve, then refinement with FP64 residuals r = b - A x
-    if (s < kM) xs[s] = 0.0;
-    if (s < kM) res[s] = G[packed_index(s, 65)];
-    __syncthreads();
-    for (int it = 0; it < 3; ++it) {
-        if (warp == 0) chol_solve_warp(L, inv_diag, res, xs, lane);
-        __syncthreads();
-        if (it == 2) break;
-        if (s < kM) {  // one thread per row: 32 strided partial sums, then a pairwise tree
-            const int i = s;
-            double part[32];
 #pragma unroll
-            for (int l = 0; l < 32; ++l) {
-                double acc = 0.0;
-#pragma unroll
-                for (int j = l; j < kM; j += 32)
-                    if (inv_diag[j] != 0.0f) acc += G[i <= j ? packed_index(i, j) : packed_index(j, i)] * xs[j];
-                part[l] = acc;
+        for (int w = 1; w <= 2; w <<= 1) {  // lanes 4i .. 4i+3 of one warp
+            const float oh = __shfl_xor_sync(0xffffffffu, rh, w), ol = __shfl_xor_sync(0xffffffffu, rl, w);
+            if (sub & w) {
+                float th = oh, tl = ol;
+                pair_add(th, tl, rh, rl);
+                rh = th;
+                rl = tl;
+            } else {
+                pair_add(rh, rl, oh, ol);
             }
-#pragma unroll
-            for (int w = 16; w >= 1; w >>= 1)
-#pragma unroll
-                for (int l = 0; l < w; ++l) part[l] = part[l] + part[l + w];
-            res[i] = inv_diag[i] != 0.0f ? G[packed_index(i, 65)] - part[0] : 0.0;
+        }
+        if (sub == 0 && i < kM) {  // r_i = b_i - (A x)_i
+            float h = S.vb[i], l = S.bl[i];
+            pair_add(h, l, -rh, -rl);
+            S.vr[i] = h;
+        }
+        if (s >= kM && s < kPad) S.vr[s] = 0.0f;
+        __syncthreads();
+        w_matvec(S, role_w, R, C, m, S.vr, S.vz, false, s);
+        w_matvec(S, role_w, R, C, m, S.vz, S.vx, true, s);
+        if (s < kM) {
+            float h = S.xh[s], l = S.xl[s];
+            pair_add(h, l, S.vx[s], 0.0f);
+            S.xh[s] = h;
+            S.xl[s] = l;
         }
         __syncthreads();
     }
     if (s < kM) {
-        const double b = inv_diag[s] != 0.0f ? xs[s] * sc[s] : 0.0;
-        res[s] = b;  // beta
-        if (!(fabs(b) <= 1e30)) atomicOr(&bad, 1);  // also catches NaN
+        const double b = S.drop[s] ? 0.0 : (static_cast<double>(S.xh[s]) + static_cast<double>(S.xl[s])) *
+                                               static_cast<double>(S.sc[s]);
+        S.coef[s] = static_cast<float>(b);
+        if (!(fabs(b) <= 1e30)) atomicOr(&S.bad, 1);  // also catches NaN
     }
     __syncthreads();
     // snapshot of date d: current features + fitted output layer (W3 then b3)
     float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
     float* snap = snaps + (static_cast<size_t>(c.reg_offset) + d) * kParamStride;
-    const bool ok = bad == 0;
+    const bool ok = S.bad == 0;
     static_assert(kParamStride % 4 == 0 && kB3 == kW3 + 64, "snapshot layout");
     for (int i = s; i < kParamStride / 4; i += kSolveThreads)
         reinterpret_cast<float4*>(snap)[i] = reinterpret_cast<const float4*>(net)[i];
     __syncthreads();
     if (ok && s <= 64) {
-        const float val = static_cast<float>(res[s]);
+        const float val = S.coef[s];
         snap[kW3 + s] = val;
         net[kW3 + s] = val;  // fine-tuning continues from the fit
-        inv_diag[s] = val;   // W3, then b3 (inv_diag is free now)
     }
     if (s == 0) snap_ok[c.reg_offset + d] = ok ? 1 : 0;
     if (!ok) return;
     // The continuation table of date d for the exercise test at d (the next
     // backward iteration): E_i = b3 + W3 . F_i at every node, from the
     // feature table this fit used.
-    __syncthreads();
     const float* F = feats + (static_cast<size_t>(c.reg_offset) + d) * kNodes * 64;
-    const float b3 = inv_diag[64];
+    const float b3 = S.coef[64];
     for (int i = s; i < kNodes; i += kSolveThreads) {
         const float4* row = reinterpret_cast<const float4*>(F + static_cast<size_t>(i) * 64);
         float y = b3;
 #pragma unroll 4
         for (int q = 0; q < 16; ++q) {
             const float4 f = row[q];
-            y = __fmaf_rn(inv_diag[4 * q], f.x, y);
-            y = __fmaf_rn(inv_diag[4 * q + 1], f.y, y);
-            y = __fmaf_rn(inv_diag[4 * q + 2], f.z, y);
-            y = __fmaf_rn(inv_diag[4 * q + 3], f.w, y);
+            y = __fmaf_rn(S.coef[4 * q], f.x, y);
+            y = __fmaf_rn(S.coef[4 * q + 1], f.y, y);
+            y = __fmaf_rn(S.coef[4 * q + 2], f.z, y);
+            y = __fmaf_rn(S.coef[4 * q + 3], f.w, y);
         }
         etab[static_cast<size_t>(ci) * kNodes + i] = y;
     }

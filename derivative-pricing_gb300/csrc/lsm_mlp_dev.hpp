@@ -32,7 +32,7 @@ enum PassMode { kStep = 1, kGram = 2 };
 // features, built from per-bin moments of the paths) and for its exercise
 // decision (an interpolated continuation table).
 constexpr int kNodes = 512;
-constexpr int kNodeSlices = kNodes / 128;           // Gram CTAs per contract (128 bins each)
+constexpr int kNodeSlices = kNodes / 64;            // Gram CTAs per contract (64 bins each)
 constexpr int kMoments = 4;                          // per bin: n 2^40 + sum t, sum t^2, sum y, sum t y
 constexpr int kCountShift = 40;                      // n above sum t (< 2^39 for <= 2^23 paths per CTA)
 constexpr double kTScale = 65536.0;                  // t in [0, 1] as an integer of 16 bits

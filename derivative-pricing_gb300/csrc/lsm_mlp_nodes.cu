@@ -415,6 +415,7 @@ __global__ void __launch_bounds__(kGramThreads)
                         float* __restrict__ gram_part) {
     __shared__ __align__(16) float F[kBinsPerSlice + 1][kFStride];
     __shared__ float wgt[5][kBinsPerSlice];  // Saa, Sab, Sbb, Say, Sby of each bin
+    __shared__ unsigned long long msum[5][kBinsPerSlice];  // n, sum t, sum t^2, sum y, sum t y
     __shared__ double s_yb;
     const int ci = c_first + static_cast<int>(blockIdx.x), slice = blockIdx.y;
     if (ci >= n_contracts) return;
@@ -424,21 +425,47 @@ __global__ void __launch_bounds__(kGramThreads)
     const int s = threadIdx.x;
     const int row0 = slice * kBinsPerSlice;
     if (s == 0) s_yb = static_cast<double>(node_grid(c, d).y_bound);  // FP64 library calls: once per CTA
+    {
+        // The groups' moments of the slice's bins, summed with loads in flight:
+        // thread s takes bin s mod 64 and word s / 64 of every group (word 0
+        // holds n 2^40 + sum t, split per group).
+        static_assert(kBinsPerSlice * kMoments == kGramThreads, "one (bin, word) per thread");
+        const int bl = s % kBinsPerSlice, q = s / kBinsPerSlice;
+        const int b = row0 + bl;
+        unsigned long long a0 = 0ull, a1 = 0ull;
+        if (b <= kNodes - 2) {
+            const unsigned long long* p = mom_part + (static_cast<size_t>(c.group_begin) * kMoments + q) * kNodes + b;
+            constexpr uint32_t kBatch = 8;
+            for (uint32_t g0 = 0; g0 < c.n_groups; g0 += kBatch) {
+                unsigned long long v[kBatch];
+#pragma unroll
+                for (uint32_t u = 0; u < kBatch; ++u)
+                    v[u] = g0 + u < c.n_groups ? p[static_cast<size_t>(g0 + u) * kMoments * kNodes] : 0ull;
+#pragma unroll
+                for (uint32_t u = 0; u < kBatch; ++u) {
+                    if (q == 0) {
+                        a0 += v[u] >> kCountShift;
+                        a1 += v[u] & ((1ull << kCountShift) - 1ull);
+                    } else {
+                        a0 += v[u];
+                    }
+                }
+            }
+        }
+        if (q == 0) {
+            msum[0][bl] = a0;
+            msum[1][bl] = a1;
+        } else {
+            msum[q + 1][bl] = a0;
+        }
+    }
     __syncthreads();
     if (s < kBinsPerSlice) {
         const int b = row0 + s;
         float w[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         if (b <= kNodes - 2) {
-            // n, sum t, sum t^2, sum y, sum t y (the first word of a group holds n 2^40 + sum t)
-            unsigned long long m[5] = {0ull, 0ull, 0ull, 0ull, 0ull};
-            const unsigned long long* p = mom_part + static_cast<size_t>(c.group_begin) * kMoments * kNodes + b;
-            for (uint32_t gg = 0; gg < c.n_groups; ++gg) {
-                const unsigned long long first = p[static_cast<size_t>(gg) * kMoments * kNodes];
-                m[0] += first >> kCountShift;
-                m[1] += first & ((1ull << kCountShift) - 1ull);
-#pragma unroll
-                for (int q = 1; q < kMoments; ++q) m[q + 1] += p[(static_cast<size_t>(gg) * kMoments + q) * kNodes];
-            }
+            // n, sum t, sum t^2, sum y, sum t y
+            const unsigned long long m[5] = {msum[0][s], msum[1][s], msum[2][s], msum[3][s], msum[4][s]};
             const double yb = s_yb;
             const double cnt = static_cast<double>(m[0]);
             const double st = static_cast<double>(m[1]) / kTScale;
