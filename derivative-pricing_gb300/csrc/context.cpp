@@ -88,6 +88,7 @@ Ctx::~Ctx() {
     for (int i = 0; i < kAuxStreams; ++i) {
         if (aux_stream[i]) cudaStreamDestroy(aux_stream[i]);
         if (ev_join[i]) cudaEventDestroy(ev_join[i]);
+        if (ev_stage[i]) cudaEventDestroy(ev_stage[i]);
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (stream) cudaStreamDestroy(stream);
@@ -830,6 +831,7 @@ int Ctx::ensure_aux() {
     for (int i = 0; i < kAuxStreams && e == cudaSuccess; ++i) {
         e = cudaStreamCreateWithFlags(&aux_stream[i], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_join[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_stage[i], cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
     if (e != cudaSuccess) return cuda_fail(e, "auxiliary streams");

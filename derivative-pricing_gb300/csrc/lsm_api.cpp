@@ -224,15 +224,19 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
     if (e != cudaSuccess) return ctx.cuda_fail(e, "lsm begin capture");
     const LsmDev* d_dev = static_cast<const LsmDev*>(ctx.ext[kDev].ptr);
     const uint32_t* d_map = static_cast<const uint32_t*>(ctx.ext[kChunkMap].ptr);
+    // The chains start one after another: chain j+1's forward simulation
+    // (which fills the GPU) follows chain j's, and so overlaps chain j's first
+    // backward steps -- for the learned regression, its training, which runs
+    // one CTA per contract.
     cudaError_t le = cudaSuccess;
-    if (chains.size() > 1) le = cudaEventRecord(ctx.ev_fork, ctx.stream);
     for (size_t j = 0; j < chains.size() && le == cudaSuccess; ++j) {
         const Chain& ch = chains[j];
         cudaStream_t cs = j == 0 ? ctx.stream : ctx.aux_stream[j - 1];
-        if (j > 0) le = cudaStreamWaitEvent(cs, ctx.ev_fork, 0);
+        if (j > 0) le = cudaStreamWaitEvent(cs, ctx.ev_stage[j - 1], 0);
         if (le == cudaSuccess)
             le = launch_lsm_forward(precision, d_dev, static_cast<int>(n), d_map, ch.chunk_first, ch.chunk_count,
                                     ctx.ext[kStore].ptr, cs);
+        if (le == cudaSuccess && j + 1 < chains.size()) le = cudaEventRecord(ctx.ev_stage[j], cs);
         for (int k = 0; k < ch.max_steps && le == cudaSuccess; ++k) {
             if (mlp)
                 le = launch_lsm_mlp_iteration(precision, k, !frozen, d_dev, ch.c_first, ch.c_end, ch.max_steps,

@@ -101,10 +101,12 @@ __device__ __forceinline__ void refresh_w2_row(TrainSmem& S, int r) {
     }
 }
 
-__device__ __forceinline__ float adam(float& p, float& m, float& v, float g, float lr, float c1, float c2) {
+// Adam with the bias corrections passed as reciprocals (ic1 = 1 / (1 - 0.9^t),
+// ic2 = 1 / (1 - 0.999^t)).
+__device__ __forceinline__ float adam(float& p, float& m, float& v, float g, float lr, float ic1, float ic2) {
     m = 0.9f * m + 0.1f * g;
     v = 0.999f * v + 0.001f * g * g;
-    const float mh = m / c1, vh = v / c2;
+    const float mh = m * ic1, vh = v * ic2;
     p -= lr * mh / (sqrtf(vh) + 1e-8f);
     return p;
 }
@@ -161,14 +163,21 @@ __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff
     const float dy = S.w[s] > 0.0f ? 2.0f * diff * inv_n : 0.0f;
     S.dy[s] = dy;
     __syncthreads();
+    // column sums over the 128 samples: four interleaved partial sums per
+    // thread, added in a fixed order (short dependency chains)
     if (s < 64) {
-        float acc = 0.0f;
-        for (int q = 0; q < 128; ++q) acc = __fmaf_rn(S.dy[q], S.scratch[q * kRow + s], acc);
-        S.g[256 + s] = acc;  // dW3
-    } else if (s == 64) {
-        float acc = 0.0f;
-        for (int q = 0; q < 128; ++q) acc += S.dy[q];
-        S.g[320] = acc;  // db3
+        float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 4
+        for (int q = 0; q < 128; q += 4)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a[u] = __fmaf_rn(S.dy[q + u], S.scratch[(q + u) * kRow + s], a[u]);
+        S.g[256 + s] = (a[0] + a[1]) + (a[2] + a[3]);  // dW3
+    } else if (s < 96) {  // db3: one warp
+        const int l = s & 31;
+        float a = (S.dy[l] + S.dy[l + 32]) + (S.dy[l + 64] + S.dy[l + 96]);
+#pragma unroll
+        for (int w = 16; w >= 1; w >>= 1) a += __shfl_xor_sync(0xffffffffu, a, w);
+        if (l == 0) S.g[320] = a;
     }
     __syncthreads();
     // ---- back through GELU to dZ2 (BF16, both layouts) and its FP32 rows
@@ -203,9 +212,12 @@ __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff
         umma::mma_commit(&S.mbar);
     }
     if (s < 64) {  // db2 while the tensor core runs
-        float acc = 0.0f;
-        for (int q = 0; q < 128; ++q) acc += S.scratch[q * kRow + s];
-        S.g[192 + s] = acc;
+        float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 4
+        for (int q = 0; q < 128; q += 4)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a[u] += S.scratch[(q + u) * kRow + s];
+        S.g[192 + s] = (a[0] + a[1]) + (a[2] + a[3]);
     }
     const bool ok3 = __syncthreads_and(umma::mbar_wait(&S.mbar, phase, err, 3));
     if (!ok3) return false;
@@ -229,19 +241,22 @@ __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff
     }
     __syncthreads();
     if (s < 64) {
-        float gb = 0.0f, g0 = 0.0f, g1 = 0.0f;
-        for (int q = 0; q < 128; ++q) {
-            const float d = S.scratch[q * kRow + s];
-            gb += d;
-            g0 = __fmaf_rn(d, S.x0[q], g0);
-            g1 = __fmaf_rn(d, S.x1[q], g1);
-        }
-        S.g[128 + s] = gb;
-        S.g[2 * s] = g0;
-        S.g[2 * s + 1] = g1;
+        float gb[4] = {}, g0[4] = {}, g1[4] = {};
+#pragma unroll 4
+        for (int q = 0; q < 128; q += 4)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float d = S.scratch[(q + u) * kRow + s];
+                gb[u] += d;
+                g0[u] = __fmaf_rn(d, S.x0[q + u], g0[u]);
+                g1[u] = __fmaf_rn(d, S.x1[q + u], g1[u]);
+            }
+        S.g[128 + s] = (gb[0] + gb[1]) + (gb[2] + gb[3]);
+        S.g[2 * s] = (g0[0] + g0[1]) + (g0[2] + g0[3]);
+        S.g[2 * s + 1] = (g1[0] + g1[1]) + (g1[2] + g1[3]);
     }
-    const float c1 = 1.0f - powf(0.9f, static_cast<float>(t_adam));
-    const float c2 = 1.0f - powf(0.999f, static_cast<float>(t_adam));
+    const float c1 = 1.0f / (1.0f - powf(0.9f, static_cast<float>(t_adam)));
+    const float c2 = 1.0f / (1.0f - powf(0.999f, static_cast<float>(t_adam)));
     // ---- dW2 rows from tensor memory (lanes 0..63 = output neurons, readable
     // by warps 0-1 only), staged in shared memory so that all four warps share
     // the 4096 Adam updates: the FP32 copy goes into the first half of dz2t
@@ -285,10 +300,11 @@ __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff
         S.scratch[s] = l;  // scratch rows are free again
     }
     __syncthreads();
-    if (s == 0) {
-        float l = 0.0f;
-        for (int q = 0; q < 128; ++q) l += S.scratch[q];
-        S.loss = l;
+    if (s < 32) {
+        float l = (S.scratch[s] + S.scratch[s + 32]) + (S.scratch[s + 64] + S.scratch[s + 96]);
+#pragma unroll
+        for (int w = 16; w >= 1; w >>= 1) l += __shfl_xor_sync(0xffffffffu, l, w);
+        if (s == 0) S.loss = l;
     }
     __syncthreads();
     return true;
@@ -404,13 +420,20 @@ __global__ void __launch_bounds__(128, 1)
     const double inv_k = 1.0 / c.strike;
     const float x1 = static_cast<float>(n - date) / static_cast<float>(n);
     bool ok = true;
-    for (int st = 0; st < steps && ok; ++st) {
+    // this thread's sample of step st: the path's spot at the date and its cash flow
+    auto sample = [&](int st, double& sv, double& cfv) {
         const uint32_t h = mix32(static_cast<uint32_t>(c.seed) * 0x9E3779B1u ^ mix32((static_cast<uint32_t>(date) << 20) ^
                                                                                      (static_cast<uint32_t>(st) << 7) ^ s));
         const uint64_t i = static_cast<uint64_t>(h) % c.path_count;
-        // both loads in flight together (the cash flow is used only in the money)
-        const double sv = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(date - 1) * c.path_count + i);
-        const double cfv = cf_load<PREC>(cf, c.cf_offset + i);
+        sv = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(date - 1) * c.path_count + i);
+        cfv = cf_load<PREC>(cf, c.cf_offset + i);
+    };
+    double sv_next = 0.0, cf_next = 0.0;
+    if (steps > 0) sample(0, sv_next, cf_next);
+    for (int st = 0; st < steps && ok; ++st) {
+        const double sv = sv_next, cfv = cf_next;
+        // the next step's loads, in flight during this step
+        if (st + 1 < steps) sample(st + 1, sv_next, cf_next);
         const double ex = (c.type == 0 ? 1.0 : -1.0) * (sv - c.strike);
         const bool itm = ex > 0.0;
         S.x0[s] = static_cast<float>(4.0 * (sv * inv_k - 1.0));
@@ -658,8 +681,10 @@ __device__ __forceinline__ void pair_scale(float h, float l, float f, float& oh,
 
 // Arrays read or written as float4 first: each is a multiple of 16 bytes.
 struct __align__(16) SolveSmem {
-    float colA[2][kPad];                     // pivot column of A, double-buffered by step
-    float rowW[2][kPad];                     // pivot row of W, double-buffered by step
+    float panelA[2][kPad][4];                // pivot block column of A, double-buffered by block step
+    float panelW[2][4][kPad];                // pivot block row of W, double-buffered by block step
+    float lpan[kPad][4];                     // the factor's pivot columns of the block step, by row
+    float ld4[4][4], inv4[4];                // the diagonal block's factor (strictly lower) and reciprocal pivots
     float part[kNB][kPad];                   // partial sums of the matrix-vector products
     float vb[kPad], vr[kPad];                // right-hand side (hi), residual
     float vz[kPad], vx[kPad];                // W v, W^T W v
@@ -681,52 +706,130 @@ __device__ __forceinline__ void tri_block(int t, int& R, int& C) {
     C = t - R * (R + 1) / 2;
 }
 
-// Step j = 4 J + JJ of the sweep (see above).  The A role owns block (R, C) of
-// the matrix being factored, the W role block (R, C) of L^-1 in the making;
-// m is the owned block.  Owners of the next pivot column (A) and row (W)
-// publish them into the other buffer.
-template <int JJ>
-__device__ __forceinline__ void chol_step(SolveSmem& S, int J, bool role_a, bool role_w, int R, int C, float (&m)[4][4],
-                                          int s) {
-    const int j = 4 * J + JJ;
-    const int buf = j & 1;
+// The 4 x 4 diagonal block D of the pivot panel, factored: the strictly lower
+// factor Ld and the reciprocal pivots inv (0 for a dropped pivot), with the
+// same operations in the same order as one pivot at a time.
+__device__ __forceinline__ void diag_factor(float (&a)[4][4], float (&Ld)[4][4], float (&inv)[4]) {
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+        const float dj = a[jj][jj];
+        inv[jj] = dj >= 0.5f * kRidge ? rsqrtf(dj) : 0.0f;
+#pragma unroll
+        for (int i = jj + 1; i < 4; ++i) Ld[i][jj] = a[i][jj] * inv[jj];
+#pragma unroll
+        for (int i = jj + 1; i < 4; ++i)
+#pragma unroll
+            for (int c = jj + 1; c <= i; ++c) a[i][c] = __fmaf_rn(-Ld[i][jj], Ld[c][jj], a[i][c]);
+    }
+}
+
+__device__ __forceinline__ void load_rows(const float (*rows)[4], int r0, float (&x)[4][4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float4 v = *reinterpret_cast<const float4*>(rows[r0 + i]);
+        x[i][0] = v.x;
+        x[i][1] = v.y;
+        x[i][2] = v.z;
+        x[i][3] = v.w;
+    }
+}
+
+// Block step J of the sweep: pivots 4 J .. 4 J + 3.  The owners of block
+// column J of A and of block row J of W published them (the panels) before
+// the first barrier; one thread per row then factors the panel's diagonal
+// block and derives its row of the factor's four pivot columns; after the
+// second barrier every thread applies the rank-4 update to its block of A
+// (C > J) or the four row operations to its block of W, and the owners of the
+// next panels publish them.  Same operations, in the same order, as four
+// steps of one pivot each.
+__device__ __forceinline__ void chol_block(SolveSmem& S, int J, bool role_a, bool role_w, int R, int C,
+                                           float (&m)[4][4], int s) {
+    const int buf = J & 1;
     __syncthreads();
-    const float dj = S.colA[buf][j];
-    const bool drop = !(dj >= 0.5f * kRidge);
-    const float inv = drop ? 0.0f : rsqrtf(dj);
-    if (s == 0) S.drop[j] = drop ? 1 : 0;
-    if (role_a && C >= J) {
-        const float4 xr = *reinterpret_cast<const float4*>(&S.colA[buf][4 * R]);
-        const float4 xc = *reinterpret_cast<const float4*>(&S.colA[buf][4 * C]);
-        const float lr[4] = {xr.x * inv, xr.y * inv, xr.z * inv, xr.w * inv};
-        const float lc[4] = {xc.x * inv, xc.y * inv, xc.z * inv, xc.w * inv};
+    if (s < kPad) {
+        float dg[4][4], Ld[4][4] = {}, inv[4];
+        load_rows(S.panelA[buf], 4 * J, dg);
+        diag_factor(dg, Ld, inv);
+        if (s == 0) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+            for (int jj = 0; jj < 4; ++jj) {
+                S.drop[4 * J + jj] = inv[jj] == 0.0f ? 1 : 0;
+                S.inv4[jj] = inv[jj];
 #pragma unroll
-            for (int c = 0; c < 4; ++c)
-                if (C > J || c > JJ) m[i][c] = __fmaf_rn(-lr[i], lc[c], m[i][c]);
+                for (int i = 0; i < 4; ++i) S.ld4[i][jj] = Ld[i][jj];
+            }
+        }
+        if (s >= 4 * J + 4) {  // row s of the factor's pivot columns
+            const float4 v = *reinterpret_cast<const float4*>(S.panelA[buf][s]);
+            float p[4] = {v.x, v.y, v.z, v.w}, l[4];
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) {
+                l[jj] = p[jj] * inv[jj];
+#pragma unroll
+                for (int c = jj + 1; c < 4; ++c) p[c] = __fmaf_rn(-l[jj], Ld[c][jj], p[c]);
+            }
+            *reinterpret_cast<float4*>(S.lpan[s]) = make_float4(l[0], l[1], l[2], l[3]);
+        }
+    }
+    __syncthreads();
+    if (role_a && C > J) {
+        float lr[4][4], lc[4][4];
+        load_rows(S.lpan, 4 * R, lr);
+        load_rows(S.lpan, 4 * C, lc);
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) m[i][c] = __fmaf_rn(-lr[i][jj], lc[c][jj], m[i][c]);
     }
     if (role_w && R >= J && C <= J) {
-        const float4 xr = *reinterpret_cast<const float4*>(&S.colA[buf][4 * R]);
-        const float4 xw = *reinterpret_cast<const float4*>(&S.rowW[buf][4 * C]);
-        const float lr[4] = {xr.x * inv, xr.y * inv, xr.z * inv, xr.w * inv};
-        const float wr[4] = {xw.x * inv, xw.y * inv, xw.z * inv, xw.w * inv};
+        // block (J, C) of W after the four pivots
+        float y[4][4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < 4; ++i) {
+            const float4 v = *reinterpret_cast<const float4*>(&S.panelW[buf][i][4 * C]);
+            y[i][0] = v.x;
+            y[i][1] = v.y;
+            y[i][2] = v.z;
+            y[i][3] = v.w;
+        }
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            const float iv = S.inv4[jj];
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                if (R > J || i > JJ) m[i][c] = __fmaf_rn(-lr[i], wr[c], m[i][c]);
-                else if (i == JJ) m[i][c] = wr[c];
+                y[jj][c] = y[jj][c] * iv;
+#pragma unroll
+                for (int i = jj + 1; i < 4; ++i) y[i][c] = __fmaf_rn(-S.ld4[i][jj], y[jj][c], y[i][c]);
             }
+        }
+        if (R == J) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) m[i][c] = y[i][c];
+        } else {
+            float lr[4][4];
+            load_rows(S.lpan, 4 * R, lr);
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) m[i][c] = __fmaf_rn(-lr[i][jj], y[jj][c], m[i][c]);
+        }
     }
-    // publish the next pivot column of A and row of W (every owner, updated or not)
-    constexpr int kNext = (JJ + 1) & 3;
-    const int bnext = JJ == 3 ? J + 1 : J;
-    if (j + 1 < kM) {
-        if (role_a && C == bnext)
-            *reinterpret_cast<float4*>(&S.colA[buf ^ 1][4 * R]) = make_float4(m[0][kNext], m[1][kNext], m[2][kNext], m[3][kNext]);
-        if (role_w && R == bnext)
-            *reinterpret_cast<float4*>(&S.rowW[buf ^ 1][4 * C]) = make_float4(m[kNext][0], m[kNext][1], m[kNext][2], m[kNext][3]);
+    // publish the next panels (every owner, updated or not)
+    if (J + 1 < kNB) {
+        if (role_a && C == J + 1)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                *reinterpret_cast<float4*>(S.panelA[buf ^ 1][4 * R + i]) = make_float4(m[i][0], m[i][1], m[i][2], m[i][3]);
+        if (role_w && R == J + 1)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                *reinterpret_cast<float4*>(&S.panelW[buf ^ 1][i][4 * C]) = make_float4(m[i][0], m[i][1], m[i][2], m[i][3]);
     }
 }
 
@@ -779,18 +882,26 @@ __global__ void __launch_bounds__(kSolveThreads)
     // 1. the bin slices' partials, summed in order into pairs
     {
         const float* part = gram_part + static_cast<size_t>(ci) * kNodeSlices * kGramPacked;
-        for (int p = s; p < kGramPacked; p += kSolveThreads) {
-            float v[kNodeSlices];
+        constexpr int kIters = (kGramPacked + kSolveThreads - 1) / kSolveThreads;
+        float v[kIters][kNodeSlices];  // every load first, in flight together
 #pragma unroll
-            for (int sl = 0; sl < kNodeSlices; ++sl) v[sl] = part[static_cast<size_t>(sl) * kGramPacked + p];
-            float h = v[0], l = 0.0f;
+        for (int u = 0; u < kIters; ++u) {
+            const int p = s + u * kSolveThreads;
+#pragma unroll
+            for (int sl = 0; sl < kNodeSlices; ++sl)
+                v[u][sl] = p < kGramPacked ? part[static_cast<size_t>(sl) * kGramPacked + p] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < kIters; ++u) {
+            const int p = s + u * kSolveThreads;
+            float h = v[u][0], l = 0.0f;
 #pragma unroll
             for (int sl = 1; sl < kNodeSlices; ++sl) {
                 float e;
-                two_sum(h, v[sl], h, e);
+                two_sum(h, v[u][sl], h, e);
                 l += e;
             }
-            fast_two_sum(h, l, S.gh[p], S.gl[p]);
+            if (p < kGramPacked) fast_two_sum(h, l, S.gh[p], S.gl[p]);
         }
     }
     if (s == 0) S.bad = 0;
@@ -841,16 +952,17 @@ __global__ void __launch_bounds__(kSolveThreads)
         S.vb[s] = s < kM ? S.gh[packed_index(s, kM)] : 0.0f;
         S.bl[s] = s < kM ? S.gl[packed_index(s, kM)] : 0.0f;
     }
-    if (role_a && C == 0) *reinterpret_cast<float4*>(&S.colA[0][4 * R]) = make_float4(m[0][0], m[1][0], m[2][0], m[3][0]);
-    if (role_w && R == 0) *reinterpret_cast<float4*>(&S.rowW[0][4 * C]) = make_float4(m[0][0], m[0][1], m[0][2], m[0][3]);
-    // the sweep: Cholesky of A and W = L^-1, 65 steps
-    for (int J = 0; J < kNB - 1; ++J) {
-        chol_step<0>(S, J, role_a, role_w, R, C, m, s);
-        chol_step<1>(S, J, role_a, role_w, R, C, m, s);
-        chol_step<2>(S, J, role_a, role_w, R, C, m, s);
-        chol_step<3>(S, J, role_a, role_w, R, C, m, s);
-    }
-    chol_step<0>(S, kNB - 1, role_a, role_w, R, C, m, s);  // pivot 64
+    if (role_a && C == 0)
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            *reinterpret_cast<float4*>(S.panelA[0][4 * R + i]) = make_float4(m[i][0], m[i][1], m[i][2], m[i][3]);
+    if (role_w && R == 0)
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            *reinterpret_cast<float4*>(&S.panelW[0][i][4 * C]) = make_float4(m[i][0], m[i][1], m[i][2], m[i][3]);
+    // the sweep: Cholesky of A and W = L^-1, 17 block steps of 4 pivots (the
+    // last three pivots are the padding's, 1 each)
+    for (int J = 0; J < kNB; ++J) chol_block(S, J, role_a, role_w, R, C, m, s);
     __syncthreads();
     // 3. x = W^T W b, then two refinement steps with residuals in pairs
     w_matvec(S, role_w, R, C, m, S.vb, S.vz, false, s);
@@ -865,13 +977,24 @@ __global__ void __launch_bounds__(kSolveThreads)
         const int i = s >> 2, sub = s & 3;
         float rh = 0.0f, rl = 0.0f;
         if (i < kM) {
-            for (int jj = sub; jj < kM; jj += 4) {
-                const int p = sym_index(i, jj);
-                const float ah = S.gh[p], al = S.gl[p], xh = S.xh[jj], xl = S.xl[jj];
-                const float ph = ah * xh;
-                const float pe = __fmaf_rn(ah, xh, -ph) + (ah * xl + al * xh);
-                pair_add(rh, rl, ph, pe);
+            float qh = 0.0f, ql = 0.0f;  // a second chain: columns sub + 8 t and sub + 4 + 8 t
+            for (int jj = sub; jj < kM; jj += 8) {
+                {
+                    const int p = sym_index(i, jj);
+                    const float ah = S.gh[p], al = S.gl[p], xh = S.xh[jj], xl = S.xl[jj];
+                    const float ph = ah * xh;
+                    const float pe = __fmaf_rn(ah, xh, -ph) + (ah * xl + al * xh);
+                    pair_add(rh, rl, ph, pe);
+                }
+                if (jj + 4 < kM) {
+                    const int p = sym_index(i, jj + 4);
+                    const float ah = S.gh[p], al = S.gl[p], xh = S.xh[jj + 4], xl = S.xl[jj + 4];
+                    const float ph = ah * xh;
+                    const float pe = __fmaf_rn(ah, xh, -ph) + (ah * xl + al * xh);
+                    pair_add(qh, ql, ph, pe);
+                }
             }
+            pair_add(rh, rl, qh, ql);
         }
 #pragma unroll
         for (int w = 1; w <= 2; w <<= 1) {  // lanes 4i .. 4i+3 of one warp
@@ -903,10 +1026,9 @@ __global__ void __launch_bounds__(kSolveThreads)
         __syncthreads();
     }
     if (s < kM) {
-        const double b = S.drop[s] ? 0.0 : (static_cast<double>(S.xh[s]) + static_cast<double>(S.xl[s])) *
-                                               static_cast<double>(S.sc[s]);
-        S.coef[s] = static_cast<float>(b);
-        if (!(fabs(b) <= 1e30)) atomicOr(&S.bad, 1);  // also catches NaN
+        const float b = S.drop[s] ? 0.0f : __fmaf_rn(S.xl[s], S.sc[s], S.xh[s] * S.sc[s]);
+        S.coef[s] = b;
+        if (!(fabsf(b) <= 1e30f)) atomicOr(&S.bad, 1);  // also catches NaN
     }
     __syncthreads();
     // snapshot of date d: current features + fitted output layer (W3 then b3)
