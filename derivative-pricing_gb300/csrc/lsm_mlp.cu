@@ -56,6 +56,7 @@ namespace {
 
 constexpr uint32_t kIdesc = umma::idesc_bf16(128, 64);
 constexpr int kRow = 65;  // scratch row stride in floats (65: bank-conflict free)
+constexpr int kTrainThreads = 256;  // two threads per sample of a 128-sample tile
 
 struct __align__(1024) TrainSmem {
     __nv_bfloat16 h1[128 * 64];     // A [sample][in]    K = 64
@@ -114,23 +115,28 @@ __device__ __forceinline__ float adam(float& p, float& m, float& v, float g, flo
 // One forward/backward pass over the 128-sample tile staged in S.x0/x1/y/w
 // (n_eff = number of samples with weight > 0), then (optionally) an Adam
 // update.  grad_out, when given, receives the full gradient in parameter
-// layout.  Returns false on an MMA timeout.
+// layout.  Returns false on an MMA timeout.  kTrainThreads threads: thread s
+// serves sample s mod 128 and hidden units 32 h .. 32 h + 31 (h = s / 128);
+// warp w reads the tensor-memory lanes 32 (w mod 4) .. + 31 (its samples).
 __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff, bool update, float lr,
                            int t_adam, float* grad_out, uint32_t* err) {
     const int s = threadIdx.x;
     const int warp = s >> 5;
+    const int q = s & 127, half = s >> 7;
+    const int lanes = 32 * (warp & 3);
+    const int j0 = 32 * half;
     const float inv_n = 1.0f / static_cast<float>(n_eff > 0 ? n_eff : 1);
     // ---- layer 1 (CUDA cores) -> H1 (BF16, both layouts)
     {
-        const float x0 = S.x0[s], x1 = S.x1[s];
-        for (int j = 0; j < 64; j += 2) {
+        const float x0 = S.x0[q], x1 = S.x1[q];
+        for (int j = j0; j < j0 + 32; j += 2) {
             float t;
             const float za = __fmaf_rn(S.p[kW1 + 2 * j], x0, __fmaf_rn(S.p[kW1 + 2 * j + 1], x1, S.p[kB1 + j]));
             const float zb = __fmaf_rn(S.p[kW1 + 2 * j + 2], x0, __fmaf_rn(S.p[kW1 + 2 * j + 3], x1, S.p[kB1 + j + 1]));
             const __nv_bfloat162 hp = __floats2bfloat162_rn(gelu(za, t), gelu(zb, t));
-            *reinterpret_cast<__nv_bfloat162*>(at(S.h1, s, j, 64)) = hp;
-            *at(S.h1t, j, s, 128) = hp.x;
-            *at(S.h1t, j + 1, s, 128) = hp.y;
+            *reinterpret_cast<__nv_bfloat162*>(at(S.h1, q, j, 64)) = hp;
+            *at(S.h1t, j, q, 128) = hp.x;
+            *at(S.h1t, j + 1, q, 128) = hp.y;
         }
     }
     umma::fence_smem_to_async();
@@ -146,31 +152,36 @@ __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff
     if (!ok2) return false;
     phase ^= 1u;
     umma::fence_after_sync();
-    // ---- layer 2 epilogue, layer 3, loss
-    float yhat = S.p[kB3];
-    for (int c = 0; c < 4; ++c) {
+    // ---- layer 2 epilogue, layer 3 (each half's partial sum), loss
+    float yh = half == 0 ? S.p[kB3] : 0.0f;
+    for (int c = 2 * half; c < 2 * half + 2; ++c) {
         float zz[16];
-        umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, c * 16), zz);
-        for (int q = 0; q < 16; ++q) {
-            const int j = c * 16 + q;
+        umma::tmem_ld16(umma::tmem_addr(tm, lanes, c * 16), zz);
+        for (int u = 0; u < 16; ++u) {
+            const int j = c * 16 + u;
             float t;
-            const float h = gelu(zz[q] + S.p[kB2 + j], t);
-            yhat = __fmaf_rn(S.p[kW3 + j], h, yhat);
-            S.scratch[s * kRow + j] = h;
+            const float h = gelu(zz[u] + S.p[kB2 + j], t);
+            yh = __fmaf_rn(S.p[kW3 + j], h, yh);
+            S.scratch[q * kRow + j] = h;
         }
     }
-    const float diff = yhat - S.y[s];
-    const float dy = S.w[s] > 0.0f ? 2.0f * diff * inv_n : 0.0f;
-    S.dy[s] = dy;
+    if (half == 1) S.scratch[q * kRow + 64] = yh;  // column 64 of a scratch row is padding
     __syncthreads();
+    float diff = 0.0f;
+    if (half == 0) {
+        diff = (yh + S.scratch[q * kRow + 64]) - S.y[q];
+        S.dy[q] = S.w[q] > 0.0f ? 2.0f * diff * inv_n : 0.0f;
+    }
+    __syncthreads();
+    const float dy = S.dy[q];
     // column sums over the 128 samples: four interleaved partial sums per
     // thread, added in a fixed order (short dependency chains)
     if (s < 64) {
         float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll 4
-        for (int q = 0; q < 128; q += 4)
+        for (int r = 0; r < 128; r += 4)
 #pragma unroll
-            for (int u = 0; u < 4; ++u) a[u] = __fmaf_rn(S.dy[q + u], S.scratch[(q + u) * kRow + s], a[u]);
+            for (int u = 0; u < 4; ++u) a[u] = __fmaf_rn(S.dy[r + u], S.scratch[(r + u) * kRow + s], a[u]);
         S.g[256 + s] = (a[0] + a[1]) + (a[2] + a[3]);  // dW3
     } else if (s < 96) {  // db3: one warp
         const int l = s & 31;
@@ -181,23 +192,23 @@ __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff
     }
     __syncthreads();
     // ---- back through GELU to dZ2 (BF16, both layouts) and its FP32 rows
-    for (int c = 0; c < 4; ++c) {
+    for (int c = 2 * half; c < 2 * half + 2; ++c) {
         float zz[16];
-        umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, c * 16), zz);
-        for (int q = 0; q < 16; q += 2) {
-            const int j = c * 16 + q;
+        umma::tmem_ld16(umma::tmem_addr(tm, lanes, c * 16), zz);
+        for (int u = 0; u < 16; u += 2) {
+            const int j = c * 16 + u;
             float ta, tb;
-            const float za = zz[q] + S.p[kB2 + j], zb = zz[q + 1] + S.p[kB2 + j + 1];
+            const float za = zz[u] + S.p[kB2 + j], zb = zz[u + 1] + S.p[kB2 + j + 1];
             gelu(za, ta);
             gelu(zb, tb);
             const float da = dy * S.p[kW3 + j] * gelu_grad(za, ta);
             const float db = dy * S.p[kW3 + j + 1] * gelu_grad(zb, tb);
-            S.scratch[s * kRow + j] = da;
-            S.scratch[s * kRow + j + 1] = db;
+            S.scratch[q * kRow + j] = da;
+            S.scratch[q * kRow + j + 1] = db;
             const __nv_bfloat162 dp = __floats2bfloat162_rn(da, db);
-            *reinterpret_cast<__nv_bfloat162*>(at(S.dz2, s, j, 64)) = dp;
-            *at(S.dz2t, j, s, 128) = dp.x;
-            *at(S.dz2t, j + 1, s, 128) = dp.y;
+            *reinterpret_cast<__nv_bfloat162*>(at(S.dz2, q, j, 64)) = dp;
+            *at(S.dz2t, j, q, 128) = dp.x;
+            *at(S.dz2t, j + 1, q, 128) = dp.y;
         }
     }
     umma::fence_smem_to_async();
@@ -214,9 +225,9 @@ __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff
     if (s < 64) {  // db2 while the tensor core runs
         float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll 4
-        for (int q = 0; q < 128; q += 4)
+        for (int r = 0; r < 128; r += 4)
 #pragma unroll
-            for (int u = 0; u < 4; ++u) a[u] += S.scratch[(q + u) * kRow + s];
+            for (int u = 0; u < 4; ++u) a[u] += S.scratch[(r + u) * kRow + s];
         S.g[192 + s] = (a[0] + a[1]) + (a[2] + a[3]);
     }
     const bool ok3 = __syncthreads_and(umma::mbar_wait(&S.mbar, phase, err, 3));
@@ -226,55 +237,57 @@ __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff
     __syncthreads();
     // ---- dH1 -> dZ1 (through GELU), FP32 rows
     {
-        const float x0 = S.x0[s], x1 = S.x1[s];
-        for (int c = 0; c < 4; ++c) {
+        const float x0 = S.x0[q], x1 = S.x1[q];
+        for (int c = 2 * half; c < 2 * half + 2; ++c) {
             float dd[16];
-            umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 64 + c * 16), dd);
-            for (int q = 0; q < 16; ++q) {
-                const int j = c * 16 + q;
+            umma::tmem_ld16(umma::tmem_addr(tm, lanes, 64 + c * 16), dd);
+            for (int u = 0; u < 16; ++u) {
+                const int j = c * 16 + u;
                 float t;
                 const float z = __fmaf_rn(S.p[kW1 + 2 * j], x0, __fmaf_rn(S.p[kW1 + 2 * j + 1], x1, S.p[kB1 + j]));
                 gelu(z, t);
-                S.scratch[s * kRow + j] = dd[q] * gelu_grad(z, t);
+                S.scratch[q * kRow + j] = dd[u] * gelu_grad(z, t);
             }
         }
     }
     __syncthreads();
-    if (s < 64) {
-        float gb[4] = {}, g0[4] = {}, g1[4] = {};
+    if (s < 192) {  // db1, dW1[.][0], dW1[.][1]: one sum per thread
+        const int j = s & 63, kind = s >> 6;
+        const float* xs = kind == 1 ? S.x0 : S.x1;
+        float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll 4
-        for (int q = 0; q < 128; q += 4)
+        for (int r = 0; r < 128; r += 4)
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const float d = S.scratch[(q + u) * kRow + s];
-                gb[u] += d;
-                g0[u] = __fmaf_rn(d, S.x0[q + u], g0[u]);
-                g1[u] = __fmaf_rn(d, S.x1[q + u], g1[u]);
+                const float d = S.scratch[(r + u) * kRow + j];
+                a[u] = kind == 0 ? a[u] + d : __fmaf_rn(d, xs[r + u], a[u]);
             }
-        S.g[128 + s] = (gb[0] + gb[1]) + (gb[2] + gb[3]);
-        S.g[2 * s] = (g0[0] + g0[1]) + (g0[2] + g0[3]);
-        S.g[2 * s + 1] = (g1[0] + g1[1]) + (g1[2] + g1[3]);
+        const float sum = (a[0] + a[1]) + (a[2] + a[3]);
+        if (kind == 0) S.g[128 + j] = sum;
+        else S.g[2 * j + kind - 1] = sum;
     }
     const float c1 = 1.0f / (1.0f - powf(0.9f, static_cast<float>(t_adam)));
     const float c2 = 1.0f / (1.0f - powf(0.999f, static_cast<float>(t_adam)));
     // ---- dW2 rows from tensor memory (lanes 0..63 = output neurons, readable
-    // by warps 0-1 only), staged in shared memory so that all four warps share
-    // the 4096 Adam updates: the FP32 copy goes into the first half of dz2t
-    // (rows 0..63 of dZ2^T, whose MMA has completed; the next step rewrites them)
+    // by warps 0, 1, 4 and 5; each takes 32 of the 64 columns), staged in shared
+    // memory so that every thread shares the 4096 Adam updates: the FP32 copy
+    // goes into the first half of dz2t (rows 0..63 of dZ2^T, whose MMA has
+    // completed; the next step rewrites them)
     float* stage = reinterpret_cast<float*>(S.dz2t);
-    if (warp < 2) {
-        for (int c = 0; c < 4; ++c) {
+    if ((warp & 3) < 2) {
+        const int r = lanes + (s & 31);  // output neuron
+        for (int c = 2 * half; c < 2 * half + 2; ++c) {
             float dw[16];
-            umma::tmem_ld16(umma::tmem_addr(tm, 32 * warp, 128 + c * 16), dw);
+            umma::tmem_ld16(umma::tmem_addr(tm, lanes, 128 + c * 16), dw);
 #pragma unroll
-            for (int q = 0; q < 16; ++q) stage[s * 64 + ((c * 16 + q) ^ (s & 31))] = dw[q];  // XOR swizzle
+            for (int u = 0; u < 16; ++u) stage[r * 64 + ((c * 16 + u) ^ (r & 31))] = dw[u];  // XOR swizzle
         }
     }
     umma::fence_before_sync();
     __syncthreads();
     // consecutive threads take consecutive parameters: the parameter and moment
     // arrays are read and written without bank conflicts
-    for (int i = s; i < 64 * 64; i += 128) {
+    for (int i = s; i < 64 * 64; i += kTrainThreads) {
         const int row = i >> 6, col = i & 63;
         const float g = stage[row * 64 + (col ^ (row & 31))];
         const int idx = kW2 + i;
@@ -282,23 +295,20 @@ __device__ bool train_step(TrainSmem& S, uint32_t tm, uint32_t& phase, int n_eff
         if (update) adam(S.p[idx], S.m[idx], S.v[idx], g, lr, c1, c2);
     }
     // ---- the small parameters
-    for (int q = s; q < 321; q += 128) {
+    for (int u = s; u < 321; u += kTrainThreads) {
         int idx;
-        if (q < 128) idx = kW1 + q;
-        else if (q < 192) idx = kB1 + (q - 128);
-        else if (q < 256) idx = kB2 + (q - 192);
-        else if (q < 320) idx = kW3 + (q - 256);
+        if (u < 128) idx = kW1 + u;
+        else if (u < 192) idx = kB1 + (u - 128);
+        else if (u < 256) idx = kB2 + (u - 192);
+        else if (u < 320) idx = kW3 + (u - 256);
         else idx = kB3;
-        if (grad_out) grad_out[idx] = S.g[q];
-        if (update) adam(S.p[idx], S.m[idx], S.v[idx], S.g[q], lr, c1, c2);
+        if (grad_out) grad_out[idx] = S.g[u];
+        if (update) adam(S.p[idx], S.m[idx], S.v[idx], S.g[u], lr, c1, c2);
     }
     __syncthreads();
     if (update && s < 64) refresh_w2_row(S, s);
     // loss of the tile (before the update)
-    {
-        const float l = S.w[s] > 0.0f ? diff * diff * inv_n : 0.0f;
-        S.scratch[s] = l;  // scratch rows are free again
-    }
+    if (half == 0) S.scratch[q] = S.w[q] > 0.0f ? diff * diff * inv_n : 0.0f;  // scratch rows are free again
     __syncthreads();
     if (s < 32) {
         float l = (S.scratch[s] + S.scratch[s + 32]) + (S.scratch[s + 64] + S.scratch[s + 96]);
@@ -314,7 +324,7 @@ __device__ void train_setup(TrainSmem& S) {
     const int s = threadIdx.x;
     if (s == 0) umma::mbar_init(&S.mbar, 1);
     // dZ2^T rows 64..127 stay zero (M padding of the weight-gradient MMA)
-    for (int i = s; i < 128 * 128 / 2; i += 128) reinterpret_cast<uint32_t*>(S.dz2t)[i] = 0u;
+    for (int i = s; i < 128 * 128 / 2; i += kTrainThreads) reinterpret_cast<uint32_t*>(S.dz2t)[i] = 0u;
     if ((s >> 5) == 0) umma::tmem_alloc(&S.tmem_base, 256);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     umma::fence_before_sync();
@@ -381,7 +391,7 @@ __device__ __forceinline__ double path_s(const void* store, uint64_t idx) {
 // per-contract trainer for date n - k - 1
 // ---------------------------------------------------------------------------
 template <int PREC>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kTrainThreads, 1)
     lsm_mlp_train(int k, const LsmDev* __restrict__ cs, int c_first, int n_contracts, const void* __restrict__ store,
                   const double* __restrict__ cf, float* __restrict__ nets, float* __restrict__ snaps,
                   int* __restrict__ snap_ok, int* __restrict__ adam_t, MlpConfig cfg,
@@ -398,12 +408,12 @@ __global__ void __launch_bounds__(128, 1)
     float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
     if (k == 0) {
         init_params(S.p, c.seed);
-        for (int i = s; i < kParamStride; i += 128) {
+        for (int i = s; i < kParamStride; i += kTrainThreads) {
             S.m[i] = 0.0f;
             S.v[i] = 0.0f;
         }
     } else {
-        for (int i = s; i < kParamStride; i += 128) {
+        for (int i = s; i < kParamStride; i += kTrainThreads) {
             S.p[i] = net[i];
             S.m[i] = net[kParamStride + i];
             S.v[i] = net[2 * kParamStride + i];
@@ -429,27 +439,30 @@ __global__ void __launch_bounds__(128, 1)
         cfv = cf_load<PREC>(cf, c.cf_offset + i);
     };
     double sv_next = 0.0, cf_next = 0.0;
-    if (steps > 0) sample(0, sv_next, cf_next);
+    if (steps > 0 && s < 128) sample(0, sv_next, cf_next);
+    const bool sampler = s < 128;  // thread s < 128 draws sample s of each tile
     for (int st = 0; st < steps && ok; ++st) {
         const double sv = sv_next, cfv = cf_next;
         // the next step's loads, in flight during this step
-        if (st + 1 < steps) sample(st + 1, sv_next, cf_next);
+        if (sampler && st + 1 < steps) sample(st + 1, sv_next, cf_next);
         const double ex = (c.type == 0 ? 1.0 : -1.0) * (sv - c.strike);
-        const bool itm = ex > 0.0;
-        S.x0[s] = static_cast<float>(4.0 * (sv * inv_k - 1.0));
-        S.x1[s] = x1;
-        // Target: time value (continuation minus exercise value) over K.  The
-        // decision only needs its sign, and it is an order of magnitude
-        // smaller than the continuation value itself, so the network's
-        // relative error costs far fewer wrong decisions.
-        S.y[s] = itm ? static_cast<float>((cfv - ex) * inv_k) : 0.0f;
-        S.w[s] = itm ? 1.0f : 0.0f;
+        const bool itm = sampler && ex > 0.0;
+        if (sampler) {
+            S.x0[s] = static_cast<float>(4.0 * (sv * inv_k - 1.0));
+            S.x1[s] = x1;
+            // Target: time value (continuation minus exercise value) over K.  The
+            // decision only needs its sign, and it is an order of magnitude
+            // smaller than the continuation value itself, so the network's
+            // relative error costs far fewer wrong decisions.
+            S.y[s] = itm ? static_cast<float>((cfv - ex) * inv_k) : 0.0f;
+            S.w[s] = itm ? 1.0f : 0.0f;
+        }
         const int n_eff = __syncthreads_count(itm);
         ++t;
         ok = train_step(S, tm, phase, n_eff, true, lr, t, nullptr, err);
     }
     // persist the network (features and output layer) for the next dates
-    for (int i = s; i < kParamStride; i += 128) {
+    for (int i = s; i < kParamStride; i += kTrainThreads) {
         net[i] = S.p[i];
         net[kParamStride + i] = S.m[i];
         net[2 * kParamStride + i] = S.v[i];
@@ -1069,25 +1082,27 @@ __global__ void __launch_bounds__(kSolveThreads)
 // ---------------------------------------------------------------------------
 // checks: one gradient step, inference, a single GEMM
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kTrainThreads, 1)
     mlp_grad_kernel(const float* __restrict__ params, const float* __restrict__ x0, const float* __restrict__ x1,
                     const float* __restrict__ y, const float* __restrict__ wt, int n, float* __restrict__ grad,
                     float* __restrict__ loss, uint32_t* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
     const int s = threadIdx.x;
-    for (int i = s; i < kParamStride; i += 128) {
+    for (int i = s; i < kParamStride; i += kTrainThreads) {
         S.p[i] = i < kParams ? params[i] : 0.0f;
         S.m[i] = 0.0f;
         S.v[i] = 0.0f;
     }
     train_setup(S);
     if (s < 64) refresh_w2_row(S, s);
-    const bool live = s < n;
-    S.x0[s] = live ? x0[s] : 0.0f;
-    S.x1[s] = live ? x1[s] : 0.0f;
-    S.y[s] = live ? y[s] : 0.0f;
-    S.w[s] = live ? wt[s] : 0.0f;
+    const bool live = s < n && s < 128;
+    if (s < 128) {
+        S.x0[s] = live ? x0[s] : 0.0f;
+        S.x1[s] = live ? x1[s] : 0.0f;
+        S.y[s] = live ? y[s] : 0.0f;
+        S.w[s] = live ? wt[s] : 0.0f;
+    }
     const int n_eff = __syncthreads_count(live && wt[s] > 0.0f);
     uint32_t phase = 0;
     const bool ok = train_step(S, S.tmem_base, phase, n_eff, false, 0.0f, 1, grad, err);
@@ -1238,10 +1253,10 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
     };
     auto trainer = [&]() {
         if (precision == 0)
-            lsm_mlp_train<0><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, c_first, c_end, store, cf, nets, snaps,
+            lsm_mlp_train<0><<<n_contracts, kTrainThreads, sizeof(TrainSmem), stream>>>(k, c, c_first, c_end, store, cf, nets, snaps,
                                                                               snap_ok, adam_t, cfg, err);
         else
-            lsm_mlp_train<1><<<n_contracts, 128, sizeof(TrainSmem), stream>>>(k, c, c_first, c_end, store, cf, nets, snaps,
+            lsm_mlp_train<1><<<n_contracts, kTrainThreads, sizeof(TrainSmem), stream>>>(k, c, c_first, c_end, store, cf, nets, snaps,
                                                                               snap_ok, adam_t, cfg, err);
     };
     if (!train) {
@@ -1273,7 +1288,7 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
 cudaError_t launch_mlp_grad(const float* params, const float* x0, const float* x1, const float* y, const float* w,
                             int n, float* grad, float* loss, uint32_t* err, cudaStream_t stream) {
     cudaGetLastError();
-    mlp_grad_kernel<<<1, 128, sizeof(TrainSmem), stream>>>(params, x0, x1, y, w, n, grad, loss, err);
+    mlp_grad_kernel<<<1, kTrainThreads, sizeof(TrainSmem), stream>>>(params, x0, x1, y, w, n, grad, loss, err);
     return cudaGetLastError();
 }
 
