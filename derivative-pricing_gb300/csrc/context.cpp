@@ -89,6 +89,7 @@ Ctx::~Ctx() {
         if (aux_stream[i]) cudaStreamDestroy(aux_stream[i]);
         if (ev_join[i]) cudaEventDestroy(ev_join[i]);
         if (ev_stage[i]) cudaEventDestroy(ev_stage[i]);
+        if (ev_train[i]) cudaEventDestroy(ev_train[i]);
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (stream) cudaStreamDestroy(stream);
@@ -832,6 +833,7 @@ int Ctx::ensure_aux() {
         e = cudaStreamCreateWithFlags(&aux_stream[i], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_join[i], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_stage[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_train[i], cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
     if (e != cudaSuccess) return cuda_fail(e, "auxiliary streams");

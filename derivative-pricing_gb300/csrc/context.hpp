@@ -87,7 +87,7 @@ struct Ctx {
     // (fork from and join to `stream`); created on first use.
     static constexpr int kAuxStreams = 3;
     cudaStream_t aux_stream[kAuxStreams] = {};
-    cudaEvent_t ev_fork = nullptr, ev_join[kAuxStreams] = {}, ev_stage[kAuxStreams] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[kAuxStreams] = {}, ev_stage[kAuxStreams] = {}, ev_train[kAuxStreams] = {};
     int ensure_aux();
 
     // Per-launch timing: a ring of (start, stop) event pairs recorded around

@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kLsmThreads)
             double s = c.spot;
             for (int d = 0; d < c.n_steps; ++d) {
                 const double z = normal_from_bits_f64(philox_word0(pp, static_cast<uint32_t>(d), k));
-                s = s * exp(c.drift + c.vs * z);
+                s = gbm_step_f64(s, z, c.drift, c.vs);
                 S[static_cast<uint64_t>(d) * c.path_count + i] = s;
             }
         } else {
@@ -223,10 +223,10 @@ __global__ void __launch_bounds__(kLsmThreads)
                 for (int d = 0; d < c.n_steps; ++d) {
                     const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(d), k));
                     const float z2 = normal_from_bits_f32(philox_word0(pp2, static_cast<uint32_t>(d), k));
-                    x = __fmaf_rn(sg, z, x + mu);
-                    x2 = __fmaf_rn(sg, z2, x2 + mu);
-                    out[0] = s0 * __expf(x);
-                    out[kLsmThreads] = s0 * __expf(x2);
+                    x = gbm_log_step_f32(x, z, mu, sg);
+                    x2 = gbm_log_step_f32(x2, z2, mu, sg);
+                    out[0] = gbm_spot_f32(s0, x);
+                    out[kLsmThreads] = gbm_spot_f32(s0, x2);
                     out += c.path_count;
                 }
                 ++j;  // the partner path is done
@@ -235,8 +235,8 @@ __global__ void __launch_bounds__(kLsmThreads)
             float x = 0.0f;
             for (int d = 0; d < c.n_steps; ++d) {
                 const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(d), k));
-                x = __fmaf_rn(sg, z, x + mu);
-                S[static_cast<uint64_t>(d) * c.path_count + i] = s0 * __expf(x);
+                x = gbm_log_step_f32(x, z, mu, sg);
+                S[static_cast<uint64_t>(d) * c.path_count + i] = gbm_spot_f32(s0, x);
             }
         }
     }

@@ -89,6 +89,12 @@ __host__ __device__ inline void laguerre_poly(const double gamma[4], float poly[
 }
 
 #ifdef __CUDACC__
+// One date of a stored GBM path: FP32 paths step ln(S/S0) and store
+// S0 exp(x); FP64 paths multiply S by exp(drift + vs z).  Every kernel that
+// regenerates stored path values uses these, so they agree bit for bit.
+__device__ __forceinline__ float gbm_log_step_f32(float x, float z, float mu, float sg) { return __fmaf_rn(sg, z, x + mu); }
+__device__ __forceinline__ float gbm_spot_f32(float s0, float x) { return s0 * __expf(x); }
+__device__ __forceinline__ double gbm_step_f64(double s, double z, double drift, double vs) { return s * exp(drift + vs * z); }
 // FP32 continuation value at S from poly (the FP32 backward pass and the
 // FP32 frozen replay both use this, so their decisions coincide).
 __device__ __forceinline__ float continuation_poly32(float s, float inv_strike, const float p[4]) {

@@ -21,12 +21,13 @@ namespace {
 enum { kDev = 4, kChunkMap = 5, kStore = 6, kCf = 7, kReg = 8, kPartA = 9, kPartB = 10,
        kFinal = 11, kOut = 12, kNets = 13, kSnaps = 14, kSnapOk = 15, kAdamT = 16, kErr = 17,
        kGroupMap = 18, kGramPart = 19, kFeats = 20, kMomPart = 35, kFzDev = 36, kFzPart = 37,
-       kFzOut = 38, kETab = 39, kCounters = 40 };  // kPartB: group partials
+       kFzOut = 38, kETab = 39, kCounters = 40, kPreS = 41, kPreCf = 42 };  // kPartB: group partials
 
 // Concurrent chains of the backward pass (at most Ctx::kAuxStreams + 1):
 // QR regression, learned regression.
 constexpr int kLsmChains = 2;
 constexpr int kLsmChainsLearned = 2;
+constexpr double kLsmFirstChainShare = 0.5;
 static_assert(kLsmChains <= Ctx::kAuxStreams + 1 && kLsmChainsLearned <= Ctx::kAuxStreams + 1,
               "one stream per chain");
 
@@ -145,6 +146,9 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
         if (!rc) rc = ctx.reserve(ctx.ext[kSnaps], sizeof(float) * mlp::kParamStride * p.reg_rows, "mlp snapshots");
         if (!rc) rc = ctx.reserve(ctx.ext[kSnapOk], sizeof(int) * p.reg_rows, "mlp snapshot flags");
         if (!rc) rc = ctx.reserve(ctx.ext[kAdamT], sizeof(int) * n, "mlp adam steps");
+        const size_t pre = static_cast<size_t>(std::max(ctx.mlp_steps_first, 1)) * 128 * n;
+        if (!rc && !frozen) rc = ctx.reserve(ctx.ext[kPreS], sizeof(double) * pre, "mlp training samples");
+        if (!rc && !frozen) rc = ctx.reserve(ctx.ext[kPreCf], sizeof(double) * pre, "mlp training cash flows");
         if (!rc) rc = ctx.reserve(ctx.ext[kErr], 256, "mlp error word");
         if (!rc) rc = ctx.reserve(ctx.ext[kGroupMap], sizeof(uint32_t) * std::max<uint32_t>(p.total_groups, 1), "mlp group map");
         if (!rc) rc = ctx.reserve(ctx.ext[kGramPart], sizeof(float) * kGramPacked * kNodeSlices * n, "mlp gram partials");
@@ -204,7 +208,12 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
         const int want = static_cast<int>(std::min<size_t>(n, static_cast<size_t>(mlp ? kLsmChainsLearned : kLsmChains)));
         size_t ci = 0;
         for (int j = 0; j < want && ci < n; ++j) {
-            const uint64_t target = static_cast<uint64_t>(p.total_chunks) * (j + 1) / want;
+            // chain 0 starts first (the others' forward simulations follow its
+            // own) and takes kLsmFirstChainShare of the chunks; the rest split
+            // the remainder evenly
+            const double bound = want == 1 ? 1.0
+                                            : kLsmFirstChainShare + (1.0 - kLsmFirstChainShare) * j / (want - 1);
+            const uint64_t target = static_cast<uint64_t>(static_cast<double>(p.total_chunks) * bound);
             Chain ch;
             ch.chunk_first = p.dev[ci].chunk_begin;
             ch.g_first = ch.g_end = p.dev[ci].group_begin;
@@ -229,6 +238,30 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
     // backward steps -- for the learned regression, its training, which runs
     // one CTA per contract.
     cudaError_t le = cudaSuccess;
+    // The learned regression's first training runs beside each chain's
+    // forward simulation, on a stream of its own (aux_stream[chains - 1 + j]
+    // for chain j); the chain's first fit waits for it (ev_train[j]).
+    const bool side_training = mlp && !frozen;
+    static_assert(2 * kLsmChainsLearned - 1 <= Ctx::kAuxStreams, "a training stream per learned chain");
+    if (side_training) {
+        le = cudaEventRecord(ctx.ev_fork, ctx.stream);
+        for (size_t j = 0; j < chains.size() && le == cudaSuccess; ++j) {
+            const Chain& ch = chains[j];
+            cudaStream_t ts = ctx.aux_stream[chains.size() - 1 + j];
+            le = cudaStreamWaitEvent(ts, ctx.ev_fork, 0);
+            if (le == cudaSuccess)
+                le = launch_lsm_mlp_first_training(precision, d_dev, ch.c_first, ch.c_end, ch.max_steps,
+                                                   static_cast<float*>(ctx.ext[kNets].ptr),
+                                                   static_cast<float*>(ctx.ext[kSnaps].ptr),
+                                                   static_cast<int*>(ctx.ext[kSnapOk].ptr),
+                                                   static_cast<int*>(ctx.ext[kAdamT].ptr),
+                                                   static_cast<float*>(ctx.ext[kFeats].ptr),
+                                                   static_cast<double*>(ctx.ext[kPreS].ptr),
+                                                   static_cast<double*>(ctx.ext[kPreCf].ptr), cfg,
+                                                   static_cast<uint32_t*>(ctx.ext[kErr].ptr), ts);
+            if (le == cudaSuccess) le = cudaEventRecord(ctx.ev_train[j], ts);
+        }
+    }
     for (size_t j = 0; j < chains.size() && le == cudaSuccess; ++j) {
         const Chain& ch = chains[j];
         cudaStream_t cs = j == 0 ? ctx.stream : ctx.aux_stream[j - 1];
@@ -251,6 +284,7 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
                                               static_cast<float*>(ctx.ext[kETab].ptr),
                                               static_cast<unsigned long long*>(ctx.ext[kMomPart].ptr), cfg,
                                               static_cast<Welford*>(ctx.ext[kFinal].ptr),
+                                              side_training ? ctx.ev_train[j] : nullptr,
                                               static_cast<uint32_t*>(ctx.ext[kErr].ptr), cs);
             else
                 le = launch_lsm_iteration(precision, k, d_dev, static_cast<int>(n), d_map, ch.chunk_first,

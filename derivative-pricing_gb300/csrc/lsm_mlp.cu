@@ -387,6 +387,64 @@ __device__ __forceinline__ double path_s(const void* store, uint64_t idx) {
     return static_cast<double>(static_cast<const float*>(store)[idx]);
 }
 
+// The path behind sample s (of 128) of training step st at a date.
+__device__ __forceinline__ uint64_t train_sample_path(const LsmDev& c, int date, int st, int s) {
+    const uint32_t h = mix32(static_cast<uint32_t>(c.seed) * 0x9E3779B1u ^
+                             mix32((static_cast<uint32_t>(date) << 20) ^ (static_cast<uint32_t>(st) << 7) ^ s));
+    return static_cast<uint64_t>(h) % c.path_count;
+}
+
+// ---------------------------------------------------------------------------
+// Training samples of the first (latest) regression date, drawn without the
+// path store: sample s of step st is path i of the contract, regenerated from
+// its Philox stream up to date n with the forward simulation's arithmetic
+// (gbm_log_step_f32 / gbm_step_f64), so its spot at date n-1 and its terminal
+// cash flow (the payoff at date n, discounted once, rounded as the cash-flow
+// store rounds it) equal what the stores will hold bit for bit.  The training
+// then needs neither the forward simulation nor the terminal step and runs
+// alongside them.  One CTA per (contract, step), one thread per sample.
+// ---------------------------------------------------------------------------
+template <int PREC>
+__global__ void __launch_bounds__(128)
+    lsm_mlp_train_samples(const LsmDev* __restrict__ cs, int c_first, int n_contracts, int steps,
+                          double* __restrict__ pre_s, double* __restrict__ pre_cf) {
+    const int ci = c_first + static_cast<int>(blockIdx.x), st = static_cast<int>(blockIdx.y), s = threadIdx.x;
+    if (ci >= n_contracts || st >= steps) return;
+    const LsmDev c = cs[ci];
+    const int n = c.n_steps;
+    if (n - 1 < 1 || c.path_count == 0) return;  // no regression date, as the trainer
+    const uint64_t i = train_sample_path(c, n - 1, st, s);
+    const PhiloxKeys key = philox_keys(c.seed);
+    const PhiloxPath pp = philox_path(i, 0u, key);
+    double s_prev = 0.0, s_last = 0.0;
+    if (PREC == 0) {
+        double sp = c.spot;
+        for (int d = 0; d < n; ++d) {
+            const double z = normal_from_bits_f64(philox_word0(pp, static_cast<uint32_t>(d), key));
+            sp = gbm_step_f64(sp, z, c.drift, c.vs);
+            if (d == n - 2) s_prev = sp;
+        }
+        s_last = sp;
+    } else {
+        const float mu = static_cast<float>(c.drift), sg = static_cast<float>(c.vs), s0 = static_cast<float>(c.spot);
+        float x = 0.0f;
+        for (int d = 0; d < n; ++d) {
+            const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(d), key));
+            x = gbm_log_step_f32(x, z, mu, sg);
+            if (d == n - 2) s_prev = static_cast<double>(gbm_spot_f32(s0, x));
+        }
+        s_last = static_cast<double>(gbm_spot_f32(s0, x));
+    }
+    // the terminal step's cash flow (lsm_mlp_pass at k = 0)
+    const double phi = c.type == 0 ? 1.0 : -1.0;
+    const double x = phi * (s_last - c.strike);
+    double v = (x > 0.0 ? x : 0.0) * c.disc;
+    if (PREC == 1) v = static_cast<double>(static_cast<float>(v));
+    const size_t idx = (static_cast<size_t>(ci) * steps + st) * 128 + s;
+    pre_s[idx] = s_prev;
+    pre_cf[idx] = v;
+}
+
 // ---------------------------------------------------------------------------
 // per-contract trainer for date n - k - 1
 // ---------------------------------------------------------------------------
@@ -395,7 +453,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
     lsm_mlp_train(int k, const LsmDev* __restrict__ cs, int c_first, int n_contracts, const void* __restrict__ store,
                   const double* __restrict__ cf, float* __restrict__ nets, float* __restrict__ snaps,
                   int* __restrict__ snap_ok, int* __restrict__ adam_t, MlpConfig cfg,
-                  uint32_t* __restrict__ err) {
+                  const double* __restrict__ pre_s, const double* __restrict__ pre_cf, uint32_t* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
     const int ci = c_first + static_cast<int>(blockIdx.x);
@@ -430,11 +488,17 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
     const double inv_k = 1.0 / c.strike;
     const float x1 = static_cast<float>(n - date) / static_cast<float>(n);
     bool ok = true;
-    // this thread's sample of step st: the path's spot at the date and its cash flow
+    // this thread's sample of step st: the path's spot at the date and its cash
+    // flow, drawn beforehand (lsm_mlp_train_samples) or read from the stores
+    const bool drawn = k == 0 && pre_s != nullptr;
     auto sample = [&](int st, double& sv, double& cfv) {
-        const uint32_t h = mix32(static_cast<uint32_t>(c.seed) * 0x9E3779B1u ^ mix32((static_cast<uint32_t>(date) << 20) ^
-                                                                                     (static_cast<uint32_t>(st) << 7) ^ s));
-        const uint64_t i = static_cast<uint64_t>(h) % c.path_count;
+        if (drawn) {
+            const size_t idx = (static_cast<size_t>(ci) * steps + st) * 128 + s;
+            sv = pre_s[idx];
+            cfv = pre_cf[idx];
+            return;
+        }
+        const uint64_t i = train_sample_path(c, date, st, s);
         sv = path_s<PREC>(store, c.s_offset + static_cast<uint64_t>(date - 1) * c.path_count + i);
         cfv = cf_load<PREC>(cf, c.cf_offset + i);
     };
@@ -1232,12 +1296,40 @@ cudaError_t mlp_prepare() {
     return e;
 }
 
+cudaError_t launch_lsm_mlp_first_training(int precision, const LsmDev* c, int c_first, int c_end, int max_steps,
+                                          float* nets, float* snaps, int* snap_ok, int* adam_t, float* feats,
+                                          double* pre_s, double* pre_cf, const MlpConfig& cfg, uint32_t* err,
+                                          cudaStream_t stream) {
+    cudaGetLastError();
+    if (c_end <= c_first) return cudaSuccess;
+    const int n_contracts = c_end - c_first;
+    if (cfg.steps_first > 0) {
+        const dim3 grid(static_cast<unsigned>(n_contracts), static_cast<unsigned>(cfg.steps_first));
+        if (precision == 0)
+            lsm_mlp_train_samples<0><<<grid, 128, 0, stream>>>(c, c_first, c_end, cfg.steps_first, pre_s, pre_cf);
+        else
+            lsm_mlp_train_samples<1><<<grid, 128, 0, stream>>>(c, c_first, c_end, cfg.steps_first, pre_s, pre_cf);
+    }
+    // the trainer reads no store at k = 0 when the samples are given
+    if (precision == 0)
+        lsm_mlp_train<0><<<n_contracts, kTrainThreads, sizeof(TrainSmem), stream>>>(
+            0, c, c_first, c_end, nullptr, nullptr, nets, snaps, snap_ok, adam_t, cfg, pre_s, pre_cf, err);
+    else
+        lsm_mlp_train<1><<<n_contracts, kTrainThreads, sizeof(TrainSmem), stream>>>(
+            0, c, c_first, c_end, nullptr, nullptr, nets, snaps, snap_ok, adam_t, cfg, pre_s, pre_cf, err);
+    cudaError_t e = cudaGetLastError();
+    // fixed features: every date's table at once
+    if (e == cudaSuccess && cfg.steps == 0) e = launch_lsm_mlp_features(0, true, max_steps, c, c_first, c_end, nets, feats, err, stream);
+    return e;
+}
+
 cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const LsmDev* c, int c_first, int c_end,
                                      int max_steps, const uint32_t* group_contract, uint32_t g_first, uint32_t g_end,
                                      const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
                                      float* gram_part, float* feats, float* etab, unsigned long long* mom_part,
-                                     const MlpConfig& cfg, Welford* final_part, uint32_t* err, cudaStream_t stream) {
+                                     const MlpConfig& cfg, Welford* final_part, cudaEvent_t trained, uint32_t* err,
+                                     cudaStream_t stream) {
     cudaGetLastError();
     if (g_end <= g_first || c_end <= c_first) return cudaSuccess;
     const uint32_t n_groups = g_end - g_first;
@@ -1251,13 +1343,13 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
             lsm_mlp_pass<1><<<n_groups, 128, pass_smem, stream>>>(k, c, group_contract, g_first, g_end, store, cf,
                                                                       snaps, snap_ok, final_part, err);
     };
-    auto trainer = [&]() {
+    auto trainer = [&]() {  // fine-tuning at a later date (k > 0): samples from the stores
         if (precision == 0)
-            lsm_mlp_train<0><<<n_contracts, kTrainThreads, sizeof(TrainSmem), stream>>>(k, c, c_first, c_end, store, cf, nets, snaps,
-                                                                              snap_ok, adam_t, cfg, err);
+            lsm_mlp_train<0><<<n_contracts, kTrainThreads, sizeof(TrainSmem), stream>>>(
+                k, c, c_first, c_end, store, cf, nets, snaps, snap_ok, adam_t, cfg, nullptr, nullptr, err);
         else
-            lsm_mlp_train<1><<<n_contracts, kTrainThreads, sizeof(TrainSmem), stream>>>(k, c, c_first, c_end, store, cf, nets, snaps,
-                                                                              snap_ok, adam_t, cfg, err);
+            lsm_mlp_train<1><<<n_contracts, kTrainThreads, sizeof(TrainSmem), stream>>>(
+                k, c, c_first, c_end, store, cf, nets, snaps, snap_ok, adam_t, cfg, nullptr, nullptr, err);
     };
     if (!train) {
         step();
@@ -1267,11 +1359,11 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
     const bool fine_tune = cfg.steps > 0;
     cudaError_t e = cudaSuccess;
     if (k == 0) {
-        step();       // terminal cash flows, first discount
-        trainer();    // learn the features on the latest date
+        step();  // terminal cash flows, first discount
         mode = kGram;
-        // fixed features: every date's table at once, off the per-date chain
-        if (!fine_tune) e = launch_lsm_mlp_features(k, true, max_steps, c, c_first, c_end, nets, feats, err, stream);
+        // the first training (and, with fixed features, every date's feature
+        // table) ran on another stream (launch_lsm_mlp_first_training)
+        e = cudaStreamWaitEvent(stream, trained, 0);
     }
     // fine-tuned features: the table of date e-1 from the network as tuned so far
     if (e == cudaSuccess && fine_tune) e = launch_lsm_mlp_features(k, false, max_steps, c, c_first, c_end, nets, feats, err, stream);

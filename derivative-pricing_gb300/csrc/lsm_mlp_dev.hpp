@@ -92,10 +92,20 @@ cudaError_t launch_lsm_mlp_binned(int precision, int k, int mode, const LsmDev* 
 size_t mlp_train_smem_bytes();
 size_t mlp_infer_smem_bytes();
 cudaError_t mlp_prepare();  // opts the kernels into their dynamic shared memory
+// The first training of contracts [c_first, c_end) on their latest regression
+// date n-1 (Adam, cfg.steps_first steps; its samples drawn by regenerating
+// the sampled paths, so it needs neither the path store nor the terminal
+// step) and, with fixed features (cfg.steps == 0), every date's feature table.
+// pre_s / pre_cf: cfg.steps_first x 128 doubles per contract.
+cudaError_t launch_lsm_mlp_first_training(int precision, const LsmDev* c, int c_first, int c_end, int max_steps,
+                                          float* nets, float* snaps, int* snap_ok, int* adam_t, float* feats,
+                                          double* pre_s, double* pre_cf, const MlpConfig& cfg, uint32_t* err,
+                                          cudaStream_t stream);
 // One backward iteration k: exercise at date n-k, discount, and (train =
 // true) the Gram matrix and output-layer fit of date n-k-1 on node tables; at
-// k = 0 the features are first trained on that date.  train = false replays
-// given networks path by path (lsm_mlp_pass).  Buffers: gram_part
+// k = 0 the fit first waits for `trained` (recorded after
+// launch_lsm_mlp_first_training).  train = false replays given networks path
+// by path (lsm_mlp_pass).  Buffers: gram_part
 // n x kNodeSlices x kGramPacked floats, feats (sum of n_steps + 1) x kNodes x
 // 64 floats (rows as the snapshots), etab n x kNodes floats, mom_part groups x
 // kMoments x kNodes.
@@ -105,7 +115,8 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
                                      const void* store,
                                      double* cf, float* nets, float* snaps, int* snap_ok, int* adam_t,
                                      float* gram_part, float* feats, float* etab, unsigned long long* mom_part,
-                                     const MlpConfig& cfg, Welford* final_part, uint32_t* err, cudaStream_t stream);
+                                     const MlpConfig& cfg, Welford* final_part, cudaEvent_t trained, uint32_t* err,
+                                     cudaStream_t stream);
 cudaError_t launch_mlp_grad(const float* params, const float* x0, const float* x1, const float* y, const float* w,
                             int n, float* grad, float* loss, uint32_t* err, cudaStream_t stream);
 cudaError_t launch_mlp_forward(const float* params, const float* x0, const float* x1, int n, float* out,

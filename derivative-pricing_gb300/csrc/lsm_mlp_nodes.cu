@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(kBinThreads, 5)
                    uint32_t g_first, uint32_t total_groups, const void* __restrict__ store, double* __restrict__ cf,
                    const int* __restrict__ snap_ok, const float* __restrict__ etab,
                    unsigned long long* __restrict__ mom_part, Welford* __restrict__ final_part) {
-    __shared__ float tab[kNodes];                              // continuation table of date e
+    __shared__ float2 tab[kNodes];                             // continuation table of date e: value, slope to the next node
     __shared__ uint32_t lim[kLimbs][kNodes];                   // limbs of the moments of date e-1, bin by bin
     __shared__ unsigned long long mom[kMoments][kNodes];       // the moments, epochs folded so far
     __shared__ Welford swf[kBinThreads / 32];
@@ -261,7 +261,11 @@ __global__ void __launch_bounds__(kBinThreads, 5)
         s_grid[1] = gram ? node_grid(c, e - 1) : NodeGrid{0.0f, 0.0f, 0.0f, 1.0f};
     }
     if (exercise)
-        for (int i = s; i < kNodes; i += kBinThreads) tab[i] = etab[static_cast<size_t>(ci) * kNodes + i];
+        for (int i = s; i < kNodes; i += kBinThreads) {
+            const float* row = etab + static_cast<size_t>(ci) * kNodes;
+            const float v = row[i];
+            tab[i] = make_float2(v, i + 1 < kNodes ? row[i + 1] - v : 0.0f);
+        }
     if (gram) {
         for (int i = s; i < kLimbs * kNodes; i += kBinThreads) (&lim[0][0])[i] = 0u;
         for (int i = s; i < kMoments * kNodes; i += kBinThreads) (&mom[0][0])[i] = 0ull;
@@ -298,24 +302,29 @@ __global__ void __launch_bounds__(kBinThreads, 5)
     constexpr int kPer = kLsmChunk / kBinThreads;  // paths per thread and chunk
     for (uint32_t ch = chunk0; ch < chunk1; ++ch) {
         if (gram && ch > chunk0 && (ch - chunk0) % kEpochChunks == 0) fold_epoch();
-        // every path load of this thread's kPer paths first (independent, in flight together)
+        // every path load of this thread's kPer paths first (independent, in flight
+        // together), from the chunk's column bases at fixed offsets
+        const uint64_t p0 = static_cast<uint64_t>(ch) * kLsmChunk + s;  // this thread's first path
+        const uint64_t rem = c.path_count - static_cast<uint64_t>(ch) * kLsmChunk;  // paths in the chunk and after
+        T* cf_c = cft + p0;
+        const T* v_c = init ? S_path + static_cast<uint64_t>(n - 1) * c.path_count + p0 : cf_c;
+        const T* e_c = S_path + static_cast<uint64_t>(exercise ? e - 1 : 0) * c.path_count + p0;
+        const T* d_c = S_path + static_cast<uint64_t>(gram ? e - 2 : 0) * c.path_count + p0;
         T vv[kPer], se[kPer], sd[kPer];
         bool live[kPer];
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
-            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + q * kBinThreads + s;
-            live[q] = i < c.path_count;
+            live[q] = static_cast<uint64_t>(q * kBinThreads + s) < rem;
             vv[q] = se[q] = sd[q] = T(0);
             if (live[q]) {
-                vv[q] = init ? S_path[static_cast<uint64_t>(n - 1) * c.path_count + i] : cft[i];
-                if (exercise) se[q] = S_path[static_cast<uint64_t>(e - 1) * c.path_count + i];
-                if (gram) sd[q] = S_path[static_cast<uint64_t>(e - 2) * c.path_count + i];
+                vv[q] = v_c[q * kBinThreads];
+                if (exercise) se[q] = e_c[q * kBinThreads];
+                if (gram) sd[q] = d_c[q * kBinThreads];
             }
         }
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
             if (!live[q]) continue;
-            const uint64_t i = static_cast<uint64_t>(ch) * kLsmChunk + q * kBinThreads + s;
             T v = vv[q];
             if (init) {
                 const T x = phi * (v - strike);
@@ -327,7 +336,8 @@ __global__ void __launch_bounds__(kBinThreads, 5)
                     int b;
                     float t;
                     locate(ge, __logf(static_cast<float>(se[q]) * inv_kf), b, t);
-                    const float cont = __fmaf_rn(t, tab[b + 1] - tab[b], tab[b]);
+                    const float2 nb = tab[b];
+                    const float cont = __fmaf_rn(t, nb.y, nb.x);
                     if (cont < 0.0f) v = xx;  // predicted time value < 0: exercise
                 }
             }
@@ -340,7 +350,7 @@ __global__ void __launch_bounds__(kBinThreads, 5)
                         sum32_add(fin, v);
                     }
                 } else {
-                    cft[i] = v;
+                    cf_c[q * kBinThreads] = v;
                 }
             }
             if (gram) {
@@ -353,8 +363,8 @@ __global__ void __launch_bounds__(kBinThreads, 5)
                     // 32-bit conversions (a 64-bit one would run on the FP64 unit), widened by
                     // integer products: tq in [0, 2^16], |yq| <= 2^24
                     const int tq = __float2int_rn(t * static_cast<float>(kTScale));
-                    const int yq = min(max(__float2int_rn(fminf(fmaxf(y * yq_scale, -16777216.0f), 16777216.0f)),
-                                           -16777216), 16777216);
+                    // (the float clamp keeps yq in range, NaN included: fmaxf returns the bound)
+                    const int yq = __float2int_rn(fminf(fmaxf(y * yq_scale, -16777216.0f), 16777216.0f));
                     const uint32_t ut = static_cast<uint32_t>(tq);           // [0, 2^16]
                     const uint32_t yb = static_cast<uint32_t>(yq + 16777216);  // [0, 2^25]
                     const unsigned long long tt = static_cast<unsigned long long>(ut) * ut;
