@@ -23,8 +23,8 @@
 //                   values of ln(S/K) on the tensor core, paths binned with
 //                   exact integer moments, the Gram matrix of
 //                   [features | 1 | target] from the moments.
-//   lsm_mlp_pass    one CTA per group of chunks: the terminal step, and
-//                   replays of given networks with the network evaluated
+//   lsm_mlp_pass    one CTA per group of chunks: replays of given networks
+//                   (terminal step included) with the network evaluated
 //                   path by path (Z2 = H1 W2^T on the tensor core).
 //   lsm_mlp_solve   one CTA per contract: scaled ridge Cholesky solve (65 x 65,
 //                   FP32 factor, FP64-residual refinement) for the output
@@ -400,7 +400,7 @@ __device__ __forceinline__ uint64_t train_sample_path(const LsmDev& c, int date,
 // its Philox stream up to date n with the forward simulation's arithmetic
 // (gbm_log_step_f32 / gbm_step_f64), so its spot at date n-1 and its terminal
 // cash flow (the payoff at date n, discounted once, rounded as the cash-flow
-// store rounds it) equal what the stores will hold bit for bit.  The training
+// store holds it) equal what the stores will hold bit for bit.  The training
 // then needs neither the forward simulation nor the terminal step and runs
 // alongside them.  One CTA per (contract, step), one thread per sample.
 // ---------------------------------------------------------------------------
@@ -435,11 +435,17 @@ __global__ void __launch_bounds__(128)
         }
         s_last = static_cast<double>(gbm_spot_f32(s0, x));
     }
-    // the terminal step's cash flow (lsm_mlp_pass at k = 0)
-    const double phi = c.type == 0 ? 1.0 : -1.0;
-    const double x = phi * (s_last - c.strike);
-    double v = (x > 0.0 ? x : 0.0) * c.disc;
-    if (PREC == 1) v = static_cast<double>(static_cast<float>(v));
+    // the terminal step's cash flow, in the path precision as the binned pass
+    // computes it at k = 0 (lsm_mlp_binned: payoff, then one discount)
+    double v;
+    if (PREC == 0) {
+        const double phi = c.type == 0 ? 1.0 : -1.0;
+        const double x = phi * (s_last - c.strike);
+        v = (x > 0.0 ? x : 0.0) * c.disc;
+    } else {
+        const float x = c.phi_f * (static_cast<float>(s_last) - c.strike_f);
+        v = static_cast<double>((x > 0.0f ? x : 0.0f) * c.disc_f);
+    }
     const size_t idx = (static_cast<size_t>(ci) * steps + st) * 128 + s;
     pre_s[idx] = s_prev;
     pre_cf[idx] = v;
@@ -539,9 +545,9 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
 // Per-path step over a group of chunks: exercise at date e with the network of
 // that date evaluated path by path (layer 1 on the CUDA cores, Z2 = H1 W2^T on
 // the tensor core), discount, and the cash-flow update or, at e = 1, the final
-// Welford partial.  Used for the terminal step (k = 0: no exercise) and to
-// replay given networks (mcd_lsm_reprice_mlp); the fit itself runs on node
-// tables (lsm_mlp_nodes.cu).
+// Welford partial.  Replays given networks (mcd_lsm_reprice_mlp), terminal
+// step (k = 0: no exercise) included; the fit itself, terminal step included,
+// runs on node tables (lsm_mlp_nodes.cu).
 // ---------------------------------------------------------------------------
 constexpr int kGramDim = 66;  // 64 features, bias, target
 
@@ -1359,10 +1365,10 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
     const bool fine_tune = cfg.steps > 0;
     cudaError_t e = cudaSuccess;
     if (k == 0) {
-        step();  // terminal cash flows, first discount
-        mode = kGram;
-        // the first training (and, with fixed features, every date's feature
-        // table) ran on another stream (launch_lsm_mlp_first_training)
+        // The binned pass does the terminal step (payoff at date n, one
+        // discount) along with the moments of date n-1.  The first training
+        // (and, with fixed features, every date's feature table) ran on
+        // another stream (launch_lsm_mlp_first_training).
         e = cudaStreamWaitEvent(stream, trained, 0);
     }
     // fine-tuned features: the table of date e-1 from the network as tuned so far
