@@ -151,3 +151,17 @@ def test_learned_per_date_fine_tuning_changes_little(engine, grid):
     d = np.abs(tuned["price"] - base["price"]) / base["standard_error"]
     print(f"per-date fine-tuning (5 steps): max change {d.max():.3f} SE, mean {d.mean():.3f} SE")
     assert d.max() < 0.5 and d.mean() < 0.2
+
+
+def test_learned_fp32_within_one_se_of_learned_fp64(engine, grid):
+    """The learned regression's own FP64 oracle: the same method on FP64 paths
+    (FP64 path store, exercise tests and cash flows; the same network and
+    fit).  On every put of the full grid the FP32 price is within 1 SE of it
+    (measured: at most ~0.06 SE), at 1/35 of its time."""
+    c, _ = grid
+    f32 = engine.lsm_batch(c, "fp32", "mlp")
+    f64 = engine.lsm_batch(c, "fp64", "mlp")
+    assert (f32["reserved"] == 0).all() and (f64["reserved"] == 0).all()
+    d = np.abs(f32["price"] - f64["price"]) / f64["standard_error"]
+    print(f"learned FP32 vs learned FP64: max {d.max():.3f} SE, mean {d.mean():.3f} SE")
+    assert d.max() <= 1.0
