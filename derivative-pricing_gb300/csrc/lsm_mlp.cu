@@ -42,6 +42,7 @@
 
 #include <type_traits>
 
+#include "cp_async.cuh"
 #include "device_common.cuh"
 #include "lsm.hpp"
 #include "lsm_mlp_dev.hpp"
@@ -730,6 +731,7 @@ constexpr int kPad = 4 * kNB;              // 68: the system padded with identit
 constexpr int kTriBlocks = kNB * (kNB + 1) / 2;  // 153 blocks of a lower triangle
 constexpr int kWBase = 160;                // first thread of the W role (a warp boundary)
 constexpr int kSolveThreads = 320;         // A role 0..152, W role 160..312
+constexpr size_t kSolveFeatBytes = sizeof(float) * kNodes * 64;  // the solve's copy of a feature table
 static_assert(kTriBlocks <= kWBase && kWBase + kTriBlocks <= kSolveThreads && kWBase % 32 == 0, "solve roles");
 static_assert(4 * kM <= kSolveThreads && kPad <= kSolveThreads, "four residual threads per row");
 
@@ -956,12 +958,32 @@ __global__ void __launch_bounds__(kSolveThreads)
                   const float* __restrict__ feats, float* __restrict__ nets, float* __restrict__ snaps,
                   int* __restrict__ snap_ok, float* __restrict__ etab) {
     __shared__ SolveSmem S;
+    extern __shared__ __align__(16) float s_feat[];  // the date's feature table (kSolveFeatBytes, dynamic)
     const int ci = c_first + static_cast<int>(blockIdx.x);
     if (ci >= n_contracts) return;
     const LsmDev c = cs[ci];
     const int d = c.n_steps - k - 1;
     if (d < 1) return;
     const int s = threadIdx.x;
+    // The date's feature table, for the continuation table at the end, copied
+    // in while the fit runs: row i's 16-byte piece q at piece q ^ (i mod 8)
+    // (the rows are 256 bytes apart; the XOR keeps eight rows' reads on
+    // different banks).
+    {
+        const float* F = feats + (static_cast<size_t>(c.reg_offset) + d) * kNodes * 64;
+        for (int u = s; u < kNodes * 16; u += kSolveThreads) {
+            const int row = u >> 4, piece = u & 15;
+            cp_async16(s_feat + row * 64 + 4 * (piece ^ (row & 7)), F + static_cast<size_t>(row) * 64 + 4 * piece);
+        }
+        cp_async_commit();
+    }
+    // The snapshot of date d: the current network (its output layer is
+    // replaced by the fit below).
+    float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
+    float* snap = snaps + (static_cast<size_t>(c.reg_offset) + d) * kParamStride;
+    static_assert(kParamStride % 4 == 0 && kB3 == kW3 + 64, "snapshot layout");
+    for (int i = s; i < kParamStride / 4; i += kSolveThreads)
+        reinterpret_cast<float4*>(snap)[i] = reinterpret_cast<const float4*>(net)[i];
     // 1. the bin slices' partials, summed in order into pairs
     {
         const float* part = gram_part + static_cast<size_t>(ci) * kNodeSlices * kGramPacked;
@@ -997,6 +1019,7 @@ __global__ void __launch_bounds__(kSolveThreads)
     __syncthreads();
     if (S.few) {
         if (s == 0) snap_ok[c.reg_offset + d] = 2;
+        cp_async_wait_all();  // no copy outlives the CTA
         return;
     }
     // standardised pairs G_rq sc_r sc_q, plus the ridge on the diagonal (whose
@@ -1113,15 +1136,10 @@ __global__ void __launch_bounds__(kSolveThreads)
         S.coef[s] = b;
         if (!(fabsf(b) <= 1e30f)) atomicOr(&S.bad, 1);  // also catches NaN
     }
-    __syncthreads();
-    // snapshot of date d: current features + fitted output layer (W3 then b3)
-    float* net = nets + static_cast<size_t>(ci) * 3 * kParamStride;
-    float* snap = snaps + (static_cast<size_t>(c.reg_offset) + d) * kParamStride;
+    cp_async_wait_all();
+    __syncthreads();  // the snapshot copy and the feature table are complete
+    // fitted output layer of date d (W3 then b3) into the snapshot
     const bool ok = S.bad == 0;
-    static_assert(kParamStride % 4 == 0 && kB3 == kW3 + 64, "snapshot layout");
-    for (int i = s; i < kParamStride / 4; i += kSolveThreads)
-        reinterpret_cast<float4*>(snap)[i] = reinterpret_cast<const float4*>(net)[i];
-    __syncthreads();
     if (ok && s <= 64) {
         const float val = S.coef[s];
         snap[kW3 + s] = val;
@@ -1132,14 +1150,13 @@ __global__ void __launch_bounds__(kSolveThreads)
     // The continuation table of date d for the exercise test at d (the next
     // backward iteration): E_i = b3 + W3 . F_i at every node, from the
     // feature table this fit used.
-    const float* F = feats + (static_cast<size_t>(c.reg_offset) + d) * kNodes * 64;
     const float b3 = S.coef[64];
     for (int i = s; i < kNodes; i += kSolveThreads) {
-        const float4* row = reinterpret_cast<const float4*>(F + static_cast<size_t>(i) * 64);
+        const float* row = s_feat + i * 64;
         float y = b3;
 #pragma unroll 4
         for (int q = 0; q < 16; ++q) {
-            const float4 f = row[q];
+            const float4 f = *reinterpret_cast<const float4*>(row + 4 * (q ^ (i & 7)));
             y = __fmaf_rn(S.coef[4 * q], f.x, y);
             y = __fmaf_rn(S.coef[4 * q + 1], f.y, y);
             y = __fmaf_rn(S.coef[4 * q + 2], f.z, y);
@@ -1299,6 +1316,7 @@ cudaError_t mlp_prepare() {
     if (e == cudaSuccess) e = set_smem(lsm_mlp_pass<0>, sizeof(PassSmem));
     if (e == cudaSuccess) e = set_smem(lsm_mlp_pass<1>, sizeof(PassSmem));
     if (e == cudaSuccess) e = set_smem(mlp_forward_kernel, sizeof(InferSmem));
+    if (e == cudaSuccess) e = set_smem(lsm_mlp_solve, kSolveFeatBytes);
     return e;
 }
 
@@ -1377,8 +1395,8 @@ cudaError_t launch_lsm_mlp_iteration(int precision, int k, bool train, const Lsm
         e = launch_lsm_mlp_binned(precision, k, mode, c, c_first, c_end, group_contract, g_first, g_end, store, cf,
                                   snap_ok, feats, etab, mom_part, gram_part, final_part, stream);
     if (e != cudaSuccess) return e;
-    lsm_mlp_solve<<<n_contracts, kSolveThreads, 0, stream>>>(k, c, c_first, c_end, gram_part, feats, nets, snaps, snap_ok,
-                                                              etab);
+    lsm_mlp_solve<<<n_contracts, kSolveThreads, kSolveFeatBytes, stream>>>(k, c, c_first, c_end, gram_part, feats, nets,
+                                                                            snaps, snap_ok, etab);
     if (k > 0 && fine_tune) trainer();  // optional fine-tuning of the features
     return cudaGetLastError();
 }

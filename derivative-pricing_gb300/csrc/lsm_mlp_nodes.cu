@@ -47,6 +47,7 @@
 
 #include <type_traits>
 
+#include "cp_async.cuh"
 #include "device_common.cuh"
 #include "lsm.hpp"
 #include "lsm_mlp_dev.hpp"
@@ -434,6 +435,21 @@ __global__ void __launch_bounds__(kGramThreads)
     if (d < 1) return;
     const int s = threadIdx.x;
     const int row0 = slice * kBinsPerSlice;
+    // feature rows row0 .. row0 + kBinsPerSlice, with the constant 1 in column 64:
+    // the table's pieces copied in while the moments are summed
+    {
+        const float* src = feats + (static_cast<size_t>(c.reg_offset) + d) * kNodes * 64;
+        for (int idx = s; idx < (kBinsPerSlice + 1) * (kFStride / 4); idx += kGramThreads) {
+            const int r = idx / (kFStride / 4), q4 = idx % (kFStride / 4);
+            if (row0 + r < kNodes && q4 < 16) {
+                cp_async16(&F[r][4 * q4], src + static_cast<size_t>(row0 + r) * 64 + 4 * q4);
+            } else {
+                const float one = row0 + r < kNodes ? 1.0f : 0.0f;
+                *reinterpret_cast<float4*>(&F[r][4 * q4]) = make_float4(one, 0.0f, 0.0f, 0.0f);
+            }
+        }
+        cp_async_commit();
+    }
     if (s == 0) s_yb = static_cast<double>(node_grid(c, d).y_bound);  // FP64 library calls: once per CTA
     {
         // The groups' moments of the slice's bins, summed with loads in flight:
@@ -491,17 +507,7 @@ __global__ void __launch_bounds__(kGramThreads)
 #pragma unroll
         for (int q = 0; q < 5; ++q) wgt[q][s] = w[q];
     }
-    // feature rows row0 .. row0 + kBinsPerSlice, with the constant 1 in column 64
-    const float* src = feats + (static_cast<size_t>(c.reg_offset) + d) * kNodes * 64;
-    for (int idx = s; idx < (kBinsPerSlice + 1) * (kFStride / 4); idx += kGramThreads) {
-        const int r = idx / (kFStride / 4), q4 = idx % (kFStride / 4);
-        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (row0 + r < kNodes) {
-            if (q4 < 16) v = reinterpret_cast<const float4*>(src + static_cast<size_t>(row0 + r) * 64)[q4];
-            else v.x = 1.0f;
-        }
-        *reinterpret_cast<float4*>(&F[r][4 * q4]) = v;
-    }
+    cp_async_wait_all();
     __syncthreads();
     float* out = gram_part + (static_cast<size_t>(ci) * kNodeSlices + slice) * kGramPacked;
     if (s < kBlockTasks) {
