@@ -109,12 +109,12 @@ PATH_KERNEL_SOURCES = ("derivative-pricing_gb300/csrc/gbm_paths.cu",
                        "derivative-pricing_gb300/csrc/device_common.cuh",
                        "derivative-pricing_gb300/csrc/engine.hpp")
 PATH_KERNEL_PROFILE = {
-    "sources": "f006e8ced231ecaa",
+    "sources": "bd4a0512aa792e85",
     "case_path_steps": 6807363601.0,
     # variant -> smsp__inst_executed.sum of one launch
-    "warp_inst": {"0": 16330586321, "1": 18149444628, "2": 21357413808, "3": 16459246064, "4": 16332895236},
+    "warp_inst": {"0": 15205895145, "1": 16932465571, "2": 19960539871, "3": 15461878018, "4": 15332180663},
     # variant -> dram__bytes_read.sum + dram__bytes_write.sum of one launch
-    "dram_bytes": {"0": 373504, "1": 456192, "2": 891392, "3": 5614336, "4": 598016},
+    "dram_bytes": {"0": 514560, "1": 525312, "2": 698880, "3": 3397120, "4": 473856},
 }
 
 
