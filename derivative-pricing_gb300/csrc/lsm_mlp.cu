@@ -40,6 +40,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "cp_async.cuh"
@@ -403,53 +404,56 @@ __device__ __forceinline__ uint64_t train_sample_path(const LsmDev& c, int date,
 // cash flow (the payoff at date n, discounted once, rounded as the cash-flow
 // store holds it) equal what the stores will hold bit for bit.  The training
 // then needs neither the forward simulation nor the terminal step and runs
-// alongside them.  One CTA per (contract, step), one thread per sample.
+// alongside them.  CTAs per contract over the steps (grid-stride), one thread
+// per sample; 2 KB of device memory per step and contract.
 // ---------------------------------------------------------------------------
 template <int PREC>
 __global__ void __launch_bounds__(128)
     lsm_mlp_train_samples(const LsmDev* __restrict__ cs, int c_first, int n_contracts, int steps,
                           double* __restrict__ pre_s, double* __restrict__ pre_cf) {
-    const int ci = c_first + static_cast<int>(blockIdx.x), st = static_cast<int>(blockIdx.y), s = threadIdx.x;
-    if (ci >= n_contracts || st >= steps) return;
+    const int ci = c_first + static_cast<int>(blockIdx.x), s = threadIdx.x;
+    if (ci >= n_contracts) return;
     const LsmDev c = cs[ci];
     const int n = c.n_steps;
     if (n - 1 < 1 || c.path_count == 0) return;  // no regression date, as the trainer
-    const uint64_t i = train_sample_path(c, n - 1, st, s);
-    const PhiloxKeys key = philox_keys(c.seed);
-    const PhiloxPath pp = philox_path(i, 0u, key);
-    double s_prev = 0.0, s_last = 0.0;
-    if (PREC == 0) {
-        double sp = c.spot;
-        for (int d = 0; d < n; ++d) {
-            const double z = normal_from_bits_f64(philox_word0(pp, static_cast<uint32_t>(d), key));
-            sp = gbm_step_f64(sp, z, c.drift, c.vs);
-            if (d == n - 2) s_prev = sp;
+    for (int st = static_cast<int>(blockIdx.y); st < steps; st += static_cast<int>(gridDim.y)) {
+        const uint64_t i = train_sample_path(c, n - 1, st, s);
+        const PhiloxKeys key = philox_keys(c.seed);
+        const PhiloxPath pp = philox_path(i, 0u, key);
+        double s_prev = 0.0, s_last = 0.0;
+        if (PREC == 0) {
+            double sp = c.spot;
+            for (int d = 0; d < n; ++d) {
+                const double z = normal_from_bits_f64(philox_word0(pp, static_cast<uint32_t>(d), key));
+                sp = gbm_step_f64(sp, z, c.drift, c.vs);
+                if (d == n - 2) s_prev = sp;
+            }
+            s_last = sp;
+        } else {
+            const float mu = static_cast<float>(c.drift), sg = static_cast<float>(c.vs), s0 = static_cast<float>(c.spot);
+            float x = 0.0f;
+            for (int d = 0; d < n; ++d) {
+                const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(d), key));
+                x = gbm_log_step_f32(x, z, mu, sg);
+                if (d == n - 2) s_prev = static_cast<double>(gbm_spot_f32(s0, x));
+            }
+            s_last = static_cast<double>(gbm_spot_f32(s0, x));
         }
-        s_last = sp;
-    } else {
-        const float mu = static_cast<float>(c.drift), sg = static_cast<float>(c.vs), s0 = static_cast<float>(c.spot);
-        float x = 0.0f;
-        for (int d = 0; d < n; ++d) {
-            const float z = normal_from_bits_f32(philox_word0(pp, static_cast<uint32_t>(d), key));
-            x = gbm_log_step_f32(x, z, mu, sg);
-            if (d == n - 2) s_prev = static_cast<double>(gbm_spot_f32(s0, x));
+        // the terminal step's cash flow, in the path precision as the binned pass
+        // computes it at k = 0 (lsm_mlp_binned: payoff, then one discount)
+        double v;
+        if (PREC == 0) {
+            const double phi = c.type == 0 ? 1.0 : -1.0;
+            const double x = phi * (s_last - c.strike);
+            v = (x > 0.0 ? x : 0.0) * c.disc;
+        } else {
+            const float x = c.phi_f * (static_cast<float>(s_last) - c.strike_f);
+            v = static_cast<double>((x > 0.0f ? x : 0.0f) * c.disc_f);
         }
-        s_last = static_cast<double>(gbm_spot_f32(s0, x));
+        const size_t idx = (static_cast<size_t>(ci) * steps + st) * 128 + s;
+        pre_s[idx] = s_prev;
+        pre_cf[idx] = v;
     }
-    // the terminal step's cash flow, in the path precision as the binned pass
-    // computes it at k = 0 (lsm_mlp_binned: payoff, then one discount)
-    double v;
-    if (PREC == 0) {
-        const double phi = c.type == 0 ? 1.0 : -1.0;
-        const double x = phi * (s_last - c.strike);
-        v = (x > 0.0 ? x : 0.0) * c.disc;
-    } else {
-        const float x = c.phi_f * (static_cast<float>(s_last) - c.strike_f);
-        v = static_cast<double>((x > 0.0f ? x : 0.0f) * c.disc_f);
-    }
-    const size_t idx = (static_cast<size_t>(ci) * steps + st) * 128 + s;
-    pre_s[idx] = s_prev;
-    pre_cf[idx] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -1328,7 +1332,7 @@ cudaError_t launch_lsm_mlp_first_training(int precision, const LsmDev* c, int c_
     if (c_end <= c_first) return cudaSuccess;
     const int n_contracts = c_end - c_first;
     if (cfg.steps_first > 0) {
-        const dim3 grid(static_cast<unsigned>(n_contracts), static_cast<unsigned>(cfg.steps_first));
+        const dim3 grid(static_cast<unsigned>(n_contracts), static_cast<unsigned>(std::min(cfg.steps_first, 1024)));
         if (precision == 0)
             lsm_mlp_train_samples<0><<<grid, 128, 0, stream>>>(c, c_first, c_end, cfg.steps_first, pre_s, pre_cf);
         else

@@ -292,8 +292,9 @@ int mcd_lsm_batch(mcd_ctx* ctx, const mcd_lsm_contract* contracts, size_t n, int
  * date with fewer than 4 in-the-money paths has no exercise; a contract whose
  * fit produced non-finite weights is priced by the QR regression instead
  * (mcd_lsm_result.reserved = 1).  Schedule: steps_first Adam steps at the
- * latest date (default 100, learning rate lr_first), steps at each earlier
- * date (default 0: features fixed, learning rate lr). */
+ * latest date (default 100, learning rate lr_first; their samples take 2 KB
+ * of device memory per step and contract), steps at each earlier date
+ * (default 0: features fixed, learning rate lr). */
 int mcd_lsm_set_mlp_config(mcd_ctx* ctx, int steps_first, int steps, double lr_first, double lr);
 /* Networks of contract `contract` of the last learned run:
  * weights (monitoring_points+1) x 4417 floats (layout: W1[64][2], b1[64],
