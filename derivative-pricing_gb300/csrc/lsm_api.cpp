@@ -193,10 +193,11 @@ int upload_and_run(Ctx& ctx, const LsmPlan& p, int precision, bool frozen, std::
     // The contracts run as up to kLsmChains independent chains (contiguous
     // ranges of about equal chunk counts), each captured on its own stream: a
     // date ends with a tail of little parallelism -- the QR pass's last chunk
-    // folds and per-contract solve, the learned fit's per-contract node
-    // tables, Gram slices and solve -- and another chain's work fills the GPU
-    // meanwhile.  Chains share no data but the QR second-pass counters (see
-    // launch_lsm_iteration) and the learned kernels' error word.
+    // folds and per-contract solve, the learned fit's Gram slices and
+    // per-contract solve -- and another chain's work fills the GPU meanwhile.
+    // Chains share no data but the QR second-pass counters (see
+    // launch_lsm_iteration) and the learned kernels' error word; a price does
+    // not depend on the number of chains.
     struct Chain {
         uint32_t chunk_first = 0, chunk_count = 0, g_first = 0, g_end = 0;
         int c_first = 0, c_end = 0, max_steps = 0;

@@ -19,21 +19,22 @@
 //                        iteration.  (The continuation table of a date, E_i =
 //                        b3 + W3 . F_i, is written by the solve that fits W3.)
 //   lsm_mlp_binned       one CTA per group of chunks: exercise at date e where
-//                        the interpolated continuation value is negative,
-//                        discount, cash-flow update, and for the paths in the
-//                        money at date e-1 the per-bin moments n, sum t,
-//                        sum t^2, sum y, sum t y (y = time value / K) as exact
-//                        integers (t to 16 bits, y to 24 bits of its bound;
-//                        n and sum t share one word) with four shared-memory
-//                        atomics per path: the sums do not depend on
-//                        the order of the additions, so the result is
-//                        deterministic.
+//                        the interpolated continuation value is negative (at
+//                        k = 0 the terminal payoff instead), discount,
+//                        cash-flow update, and for the paths in the money at
+//                        date e-1 the per-bin moments n, sum t, sum t^2, sum y,
+//                        sum t y (y = time value / K) as exact integers (t to
+//                        16 bits, y to 24 bits of its bound), added as 32-bit
+//                        limbs with nine shared-memory atomics per path and
+//                        folded into 64-bit sums every 32 chunks: the sums do
+//                        not depend on the order of the additions, so the
+//                        result is deterministic.
 //   lsm_mlp_gram_slices  kNodeSlices CTAs per contract: the Gram matrix of
 //                        [f | 1 | y] over the paths from the moments,
 //                        G = sum over bins of (1-t)^2 F_i F_i^T + t(1-t)
 //                        (F_i F_{i+1}^T + F_{i+1} F_i^T) + t^2 F_{i+1} F_{i+1}^T
 //                        (and the right-hand side likewise), one partial per
-//                        128 bins; lsm_mlp_solve sums them in order.
+//                        64 bins; lsm_mlp_solve sums them in order.
 //
 // The least-squares fit over the interpolated features is exact (no path is
 // left out and no feature rounded to BF16 on its way to the Gram matrix); the
