@@ -632,13 +632,15 @@ cudaError_t launch_greeks_kernel(int precision, int variant, int grid, const Dev
         switch (variant) {
             case 0: return launch_one<0, 2>(MCD_GREEKS_ARGS);
             case 1: return launch_one<0, 4>(MCD_GREEKS_ARGS);
-            default: return launch_one<0, 6>(MCD_GREEKS_ARGS);
+            case 2: return launch_one<0, 6>(MCD_GREEKS_ARGS);
+            default: return launch_one<0, 8>(MCD_GREEKS_ARGS);
         }
     }
     switch (variant) {
         case 0: return launch_one<1, 2>(MCD_GREEKS_ARGS);
         case 1: return launch_one<1, 4>(MCD_GREEKS_ARGS);
-        default: return launch_one<1, 6>(MCD_GREEKS_ARGS);
+        case 2: return launch_one<1, 6>(MCD_GREEKS_ARGS);
+        default: return launch_one<1, 8>(MCD_GREEKS_ARGS);
     }
 #undef MCD_GREEKS_ARGS
 }
@@ -660,13 +662,15 @@ cudaError_t greeks_kernel_occupancy(int precision, int variant, int* blocks) {
         switch (variant) {
             case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<0, 2>, kSlabThreads, 0);
             case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<0, 4>, kSlabThreads, 0);
-            default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<0, 6>, kSlabThreads, 0);
+            case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<0, 6>, kSlabThreads, 0);
+            default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<0, 8>, kSlabThreads, 0);
         }
     }
     switch (variant) {
         case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<1, 2>, kSlabThreads, 0);
         case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<1, 4>, kSlabThreads, 0);
-        default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<1, 6>, kSlabThreads, 0);
+        case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<1, 6>, kSlabThreads, 0);
+        default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, greeks_kernel<1, 8>, kSlabThreads, 0);
     }
 }
 

@@ -54,7 +54,7 @@ cudaError_t launch_greeks_kernel(int precision, int variant, int grid, const Dev
 cudaError_t launch_greeks_merge(const DevContract* contracts, int n_contracts, const uint32_t* item_prefix,
                                 const Welford* partials, double* out, cudaStream_t stream);
 cudaError_t greeks_kernel_occupancy(int precision, int variant, int* blocks_per_sm);
-constexpr int kGreeksVariants = 3;  // __launch_bounds__ min-blocks 2, 4, 6
+constexpr int kGreeksVariants = 4;  // __launch_bounds__ min-blocks 2, 4, 6, 8
 constexpr int kGreeksOutStride = 2 * kNumGreeks + 1;
 
 }  // namespace mcdg

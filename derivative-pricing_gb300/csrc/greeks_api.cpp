@@ -280,7 +280,7 @@ int mcd_greeks_batch(mcd_ctx* handle, const mcd_contract* contracts, size_t n, d
 int mcd_greeks_set_launch_shape(mcd_ctx* handle, int precision, int variant, int ctas_per_sm) try {
     MCD_CTX_OR_FAIL(handle, ctx);
     if (precision != 0 && precision != 1) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "bad precision");
-    if (variant < 0 || variant >= kGreeksVariants) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "variant must be 0..2");
+    if (variant < 0 || variant >= kGreeksVariants) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "variant must be 0..3");
     if (ctas_per_sm < 0 || ctas_per_sm > 64) return ctx->fail(MCD_ERR_INVALID_ARGUMENT, "ctas_per_sm must be 0..64");
     ctx->greeks_shape[precision] = LaunchShape{variant, ctas_per_sm};
     return MCD_OK;

@@ -355,8 +355,8 @@ typedef struct {
  * states must stay positive (bumps < 1). */
 int mcd_greeks_batch(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, double spot_bump_rel,
                      double vol_bump_rel, int precision, mcd_greeks_result* results);
-/* Launch shape of the sensitivity kernel (variant 0..2: register budget for
- * 2, 4 or 6 resident CTAs; ctas_per_sm 0 = occupancy limit) and its tuner, which
+/* Launch shape of the sensitivity kernel (variant 0..3: register budget for
+ * 2, 4, 6 or 8 resident CTAs; ctas_per_sm 0 = occupancy limit) and its tuner, which
  * times every candidate on the given batch and keeps the fastest. */
 int mcd_greeks_set_launch_shape(mcd_ctx* ctx, int precision, int variant, int ctas_per_sm);
 int mcd_greeks_autotune(mcd_ctx* ctx, const mcd_contract* contracts, size_t n, double spot_bump_rel,
