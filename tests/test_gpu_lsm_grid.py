@@ -93,7 +93,7 @@ def test_fp32_qr_grid_tracks_reference(engine, grid):
 
 def test_learned_grid_against_the_exact_bermudan_value(engine, grid, gpu_lib):
     """The learned regression (BF16 tensor-core network, FP32 paths) on the
-    full grid, judged against the exact value of the 50-date Bermudan put (CRR
+    full grid, checked against the exact value of the 50-date Bermudan put (CRR
     lattice with exercise at the LSM dates) and against the FP64 QR price.
 
     * Every learned price within 3 SE of the exact value (as every Monte Carlo
